@@ -1,0 +1,129 @@
+/*
+ * mdg — GB300-native Lennard-Jones short-range engine behind MDACP's call points.
+ *
+ * C ABI of libmdg.so.  Plain pointers and sizes only.  One handle is one
+ * periodic box (one MDACP unit spanning the whole system, as `mpirun -np 1`
+ * with one OpenMP unit runs it); it owns all device memory and one CUDA
+ * stream.  Every call returns MDG_OK (0) or an error code; mdg_last_error()
+ * returns the message of the last failure on that handle.  A handle must be
+ * used by one host thread at a time.
+ *
+ * Particle arrays cross the boundary in the reference's layout: `double
+ * [n][4]` with the fourth lane as padding (Variables::q / Variables::p,
+ * variables.h:16-18), indexed by the caller's particle order.  Internally
+ * particles are kept sorted by cell; results are returned in the caller's
+ * order.
+ *
+ * Physics (reference semantics): the smoothly truncated LJ potential
+ * V(r) = 4(r^-12 - r^-6 + C2 r^2 + C0) with eps = sigma = m = 1 and C0, C2 from
+ * the cut-off (variables.cc:16-28); drift-kick-drift stepping
+ * (mdmanager.cc:116-157); Langevin without the second half-drift unless
+ * langevin_half_drift_compat = 0 (mdmanager.cc:186-192); Nose-Hoover as
+ * mdmanager.cc:160-175.  Pair list: every image pair within rc + margin of a
+ * particle, formed as the reference forms its ghost pairs (image position
+ * first, then the difference; mdunit.cc:167, meshlist.cc:262-266).  A list is
+ * rebuilt when a particle has moved more than margin/2 since the last build.
+ */
+#ifndef MDG_H
+#define MDG_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDG_OK 0
+#define MDG_ERR_INVALID 1      /* bad argument or parameter */
+#define MDG_ERR_CUDA 2         /* CUDA runtime error */
+#define MDG_ERR_CAPACITY 3     /* more particles than the handle's capacity */
+#define MDG_ERR_STATE 4        /* non-finite or escaped particle coordinate */
+#define MDG_ERR_NOT_READY 5    /* no state loaded */
+
+enum mdg_precision { MDG_FP64 = 0, MDG_MIXED = 1 };
+enum mdg_thermostat { MDG_NVE = 0, MDG_LANGEVIN = 1, MDG_NOSEHOOVER = 2 };
+
+typedef struct mdg_params {
+  int32_t capacity;        /* maximum particles (Variables N, mdconfig.h:11) */
+  int32_t precision;       /* mdg_precision (.cfg Precision=fp64|mixed) */
+  double box[3];           /* SystemSizeX/Y/Z (simulationinfo.cc:38-57) */
+  double cutoff;           /* CutoffLength; CUTOFF_LENGTH (mdconfig.h:15) */
+  double margin;           /* BufferLength (simulationinfo.cc:6) */
+  double dt;               /* TimeStep */
+  int32_t thermostat;      /* mdg_thermostat (ControlTemperature + HeatbathType) */
+  int32_t langevin_half_drift_compat; /* LangevinHalfDriftCompat, 1 = reference */
+  double temperature;      /* AimedTemperature */
+  double gamma;            /* HeatbathGamma */
+  double tau;              /* HeatbathTau */
+  uint64_t seed;           /* Seed of the Langevin noise stream */
+  int32_t list_capacity;   /* neighbour slots per particle; 0 = sized from the first build */
+  int32_t device;          /* CUDA device ordinal */
+  int32_t use_graphs;      /* 1 = replay steps as CUDA graphs */
+  int32_t reserved;
+} mdg_params;
+
+typedef struct mdg_stats {
+  int64_t steps;           /* steps advanced since the last mdg_set_state */
+  int64_t rebuilds;        /* pair-list builds since the last mdg_set_state */
+  int32_t list_capacity;   /* current neighbour slots per particle */
+  int32_t max_neighbours;  /* largest row at the last build */
+  int64_t listed_pairs;    /* directed pairs in the current list */
+  int32_t cells[3];        /* cell grid */
+  int32_t particles;
+  double zeta;             /* Nose-Hoover friction (Variables::Zeta) */
+  double elapsed_ms;       /* device time of the last mdg_calculate call */
+} mdg_stats;
+
+typedef struct mdg_handle mdg_handle;
+
+/* Library version string. */
+const char *mdg_version(void);
+/* Fills *p with the reference defaults (rc 3.0, margin 0.3, dt 0.001, NVE, ...). */
+void mdg_params_default(mdg_params *p);
+
+/* Replaces MDManager construction (mdmanager.cc:11-47) for one box on one GPU. */
+int mdg_create(const mdg_params *p, mdg_handle **out);
+int mdg_destroy(mdg_handle *h);
+const char *mdg_last_error(const mdg_handle *h);
+
+/* Replaces MDUnit::AddParticle / Variables::q,p filling (mdunit.cc:35-49,
+ * variables.cc:31-42): n particles, q4/p4 host arrays [n][4].  Resets the step
+ * and rebuild counters and the Langevin stream position. */
+int mdg_set_state(mdg_handle *h, const double *q4, const double *p4, int32_t n);
+/* Copies the current state back in the caller's order; either pointer may be NULL.
+ * Positions are those of the reference at the same point: wrapped at the last
+ * rebuild only (variables.cc:59-79). */
+int mdg_get_state(mdg_handle *h, double *q4, double *p4);
+
+/* Replaces MDManager::MakePairList (mdmanager.cc:262-280): wrap, bin, build. */
+int mdg_make_pairlist(mdg_handle *h);
+/* Replaces nsteps calls of MDManager::Calculate (mdmanager.cc:116-148). */
+int mdg_calculate(mdg_handle *h, int32_t nsteps);
+/* Replaces KineticEnergyObserver, PotentialEnergyObserver and VirialObserver
+ * (observer.cc:5-79) at the current positions: out[0] = sum p^2/2,
+ * out[1] = sum of pair energies, out[2] = sum of pair virials / 3. */
+int mdg_observe(mdg_handle *h, double out[3]);
+/* Forces at the current positions in the handle's precision, caller's order,
+ * host [n][4] (ForceCalculator::CalculateForce with p = 0 and dt = 1,
+ * fcalculator.cc:35-50). */
+int mdg_forces(mdg_handle *h, double *f4);
+/* Directed pairs of the current list: rec[3k..3k+2] = {i, j, image code} with
+ * code = (sx+1) + 3(sy+1) + 9(sz+1) for the image j + (sx,sy,sz) L of j
+ * (the pair set MeshList::SearchMesh registers, meshlist.cc:219-271, both
+ * directions).  *count receives the total; at most cap records are written. */
+int mdg_pairs(mdg_handle *h, int32_t *rec, int64_t cap, int64_t *count);
+
+/* MDManager::SetSeed (mdmanager.cc:177-183). */
+int mdg_set_seed(mdg_handle *h, uint64_t seed);
+/* MDManager::SetControlTemperature / SetAimedTemperature (mdmanager.h:77-78)
+ * and HeatbathType: thermostat = mdg_thermostat. */
+int mdg_set_thermostat(mdg_handle *h, int32_t thermostat, double temperature);
+int mdg_get_stats(mdg_handle *h, mdg_stats *s);
+
+/* Device-resident state exchange on the handle's stream (caller-owned device
+ * buffers, [n][4] doubles, caller's order). */
+int mdg_set_state_device(mdg_handle *h, const double *q4_dev, const double *p4_dev, int32_t n);
+int mdg_get_state_device(mdg_handle *h, double *q4_dev, double *p4_dev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,589 @@
+// C ABI of libmdg.so (include/mdg.h): handle life cycle, state exchange and
+// the step driver that stands in for MDManager::Calculate.
+//
+// A step is enqueued as the rebuild sequence (a no-op unless the device flag
+// says the list expired) followed by the fused step kernel.  Steps are
+// replayed from CUDA graphs captured for both parities of the double-buffered
+// mid-step positions.  The host synchronises once per mdg_calculate call and
+// reads the device flags: a neighbour row that overflowed stops the remaining
+// kernels of the call at the step where it happened (they become no-ops), the
+// list is regrown and the run continues from that step.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mdg.h"
+#include "mdg_internal.cuh"
+
+using mdg::DevFlags;
+
+struct mdg_handle {
+  mdg_params prm;
+  std::string err;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  mdg::Geom g;
+  mdg::Dev d;
+  DevFlags *hflags = nullptr;  // pinned mirror
+  double *hobs = nullptr, *dobs = nullptr;
+  int cap = 0;
+  bool has_state = false;
+  bool nh_init = true;
+  int par = 0;
+  cudaGraphExec_t gx_pair[2] = {nullptr, nullptr};
+  cudaGraphExec_t gx_one[2] = {nullptr, nullptr};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  long long steps_host = 0;  // completed steps as last read from the device
+};
+
+namespace {
+
+const char *kVersion = "mdg 0.1 (sm_103a)";
+
+int fail(mdg_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define MDG_CK(call)                                                                                  \
+  do {                                                                                                \
+    cudaError_t e_ = (call);                                                                          \
+    if (e_ != cudaSuccess)                                                                            \
+      return fail(h, MDG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));               \
+  } while (0)
+
+void drop_graphs(mdg_handle *h) {
+  for (int k = 0; k < 2; k++) {
+    if (h->gx_pair[k]) cudaGraphExecDestroy(h->gx_pair[k]);
+    if (h->gx_one[k]) cudaGraphExecDestroy(h->gx_one[k]);
+    h->gx_pair[k] = h->gx_one[k] = nullptr;
+  }
+}
+
+template <class T>
+cudaError_t dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void **)p, count * sizeof(T));
+}
+
+void dfree_all(mdg_handle *h) {
+  mdg::Dev &d = h->d;
+  void *ptrs[] = {d.q_end, d.q_mid[0], d.q_mid[1], d.p, d.q_build, d.t_q, d.t_p, d.qf, d.loc[0], d.loc[1], d.id,
+                  d.inv, d.cell, d.t_id, d.t_cell, d.order, d.cell_count, d.cell_fill, d.cell_start, d.block_sums,
+                  d.nl, d.ncount, d.partials, d.flags, d.io4, d.io4b, h->dobs};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  memset(&h->d, 0, sizeof(h->d));
+  h->dobs = nullptr;
+}
+
+int lang_on(const mdg_handle *h) { return h->prm.thermostat == MDG_LANGEVIN; }
+
+// Sets the pieces of Geom that depend on the parameters (not on n).
+int setup_geometry(mdg_handle *h) {
+  mdg::Geom &g = h->g;
+  const mdg_params &p = h->prm;
+  const double sl = p.cutoff + p.margin;
+  long long ncell = 1;
+  for (int k = 0; k < 3; k++) {
+    g.L[k] = p.box[k];
+    int nc = (int)(p.box[k] / sl);
+    // every pair within sl must lie in neighbouring cells even after rounding
+    while (nc > 0 && p.box[k] / (double)nc < sl * (1.0 + 1e-12)) nc--;
+    if (nc < 2 || p.box[k] <= 2.0 * sl)
+      return fail(h, MDG_ERR_INVALID, "box side must exceed twice the search length cutoff+margin");
+    g.nc[k] = nc;
+    g.w[k] = p.box[k] / (double)nc;
+    g.inv_w[k] = 1.0 / g.w[k];
+    g.w32[k] = (float)g.w[k];
+    g.dl32[k] = (float)(p.box[k] - (double)nc * (double)g.w32[k]);
+    ncell *= nc;
+  }
+  if (ncell > 4096LL * 4096LL) return fail(h, MDG_ERR_INVALID, "too many cells");
+  g.ncell = (int)ncell;
+  g.sl2 = sl * sl;
+  g.rc2 = p.cutoff * p.cutoff;
+  g.pre2 = (float)((sl + 1e-3) * (sl + 1e-3));
+  g.rc2f = (float)g.rc2;
+  // Variables::Variables (variables.cc:16-28)
+  const double s2 = 1.0 / (p.cutoff * p.cutoff);
+  const double s6 = s2 * s2 * s2, s8 = s6 * s2, s12 = s6 * s6, s14 = s12 * s2;
+  g.c2 = 6.0 * s14 - 3.0 * s8;
+  g.c0 = -s12 + s6 - g.c2 / s2;
+  g.c2x8 = g.c2 * 8.0;
+  g.c2x8f = (float)g.c2x8;
+  g.dt = p.dt;
+  g.dt2 = p.dt * 0.5;
+  g.half_margin2 = 0.25 * p.margin * p.margin;
+  g.gamma = p.gamma;
+  g.temperature = p.temperature;
+  g.tau = p.tau;
+  g.hb_d = std::sqrt(2.0 * p.gamma * p.temperature / p.dt);
+  g.seed = p.seed;
+  return MDG_OK;
+}
+
+int estimate_list_cap(const mdg_handle *h, int n) {
+  const mdg_params &p = h->prm;
+  const double sl = p.cutoff + p.margin;
+  const double rho = (double)n / (p.box[0] * p.box[1] * p.box[2]);
+  double est = rho * 4.18879020478639 * sl * sl * sl;
+  int cap = (int)(est * 1.5 + 24.0);
+  return (cap + 7) & ~7;
+}
+
+int alloc_list(mdg_handle *h, int list_cap) {
+  if (h->d.nl) cudaFree(h->d.nl);
+  h->d.nl = nullptr;
+  MDG_CK(dalloc(&h->d.nl, (size_t)list_cap * (size_t)h->cap));
+  h->g.list_cap = list_cap;
+  drop_graphs(h);
+  return MDG_OK;
+}
+
+int read_flags(mdg_handle *h) {
+  MDG_CK(cudaMemcpyAsync(h->hflags, h->d.flags, sizeof(DevFlags), cudaMemcpyDeviceToHost, h->stream));
+  MDG_CK(cudaStreamSynchronize(h->stream));
+  return MDG_OK;
+}
+
+// After a halt on overflow: undo the counters of the step that did not run,
+// regrow the rows and clear the halt (the rebuild request stays set).
+int recover_overflow(mdg_handle *h, bool in_step) {
+  DevFlags f = *h->hflags;
+  if (in_step) {
+    f.steps -= 1;
+    if (lang_on(h)) f.lang -= 1;
+  }
+  int need = f.overflow_max;
+  int cap = (int)(need * 1.25) + 8;
+  cap = (cap + 7) & ~7;
+  if (cap <= h->g.list_cap) cap = h->g.list_cap + 8;
+  f.halt = 0;
+  f.overflow_max = 0;
+  f.rebuild = 1;
+  MDG_CK(cudaMemcpyAsync(h->d.flags, &f, sizeof(DevFlags), cudaMemcpyHostToDevice, h->stream));
+  MDG_CK(cudaStreamSynchronize(h->stream));
+  return alloc_list(h, cap);
+}
+
+// A bad coordinate stops the run inside the binning kernel, possibly with
+// partial cell counts; they are cleared here and the halt stays set (every
+// kernel is a no-op) until the next mdg_set_state.
+int halt_error(mdg_handle *h) {
+  cudaMemsetAsync(h->d.cell_count, 0, (size_t)h->g.ncell * sizeof(int), h->stream);
+  cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.ncell * sizeof(int), h->stream);
+  cudaStreamSynchronize(h->stream);
+  char buf[160];
+  snprintf(buf, sizeof buf, "particle coordinate non-finite or outside the box at a rebuild (slot %d)",
+           h->hflags->bad_slot);
+  return fail(h, MDG_ERR_STATE, buf);
+}
+
+// Builds the list now if it is due (always when force is set).
+int ensure_list(mdg_handle *h, bool force) {
+  for (int attempt = 0; attempt < 16; attempt++) {
+    if (force) mdg::launch_set_rebuild(h->d, h->stream);
+    mdg::launch_rebuild(h->g, h->d, h->par, h->num_sms, h->stream, false, false);
+    int rc = read_flags(h);
+    if (rc) return rc;
+    if (h->hflags->halt == 0) return MDG_OK;
+    if (h->hflags->halt != mdg::kHaltOverflow) return halt_error(h);
+    rc = recover_overflow(h, false);
+    if (rc) return rc;
+    force = true;
+  }
+  return fail(h, MDG_ERR_CAPACITY, "neighbour list could not be sized");
+}
+
+void enqueue_step(mdg_handle *h, int par) {
+  mdg::launch_rebuild(h->g, h->d, par, h->num_sms, h->stream, true, lang_on(h) != 0);
+  mdg::launch_step(h->g, h->d, par, h->prm.thermostat, h->prm.langevin_half_drift_compat, h->prm.precision,
+                   h->stream);
+}
+
+int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps) {
+  cudaGraph_t graph = nullptr;
+  MDG_CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < nsteps; k++) enqueue_step(h, par ^ (k & 1));
+  MDG_CK(cudaStreamEndCapture(h->stream, &graph));
+  cudaError_t e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(h, MDG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  return MDG_OK;
+}
+
+int enqueue_steps(mdg_handle *h, int nsteps) {
+  int par = h->par;
+  if (!h->prm.use_graphs) {
+    for (int k = 0; k < nsteps; k++) {
+      enqueue_step(h, par);
+      par ^= 1;
+    }
+    h->par = par;
+    return cudaGetLastError() == cudaSuccess ? MDG_OK : fail(h, MDG_ERR_CUDA, "kernel launch failed");
+  }
+  int left = nsteps;
+  if (left >= 2) {
+    if (!h->gx_pair[par]) {
+      int rc = capture(h, &h->gx_pair[par], par, 2);
+      if (rc) return rc;
+    }
+    while (left >= 2) {
+      MDG_CK(cudaGraphLaunch(h->gx_pair[par], h->stream));
+      left -= 2;
+    }
+  }
+  if (left == 1) {
+    if (!h->gx_one[par]) {
+      int rc = capture(h, &h->gx_one[par], par, 1);
+      if (rc) return rc;
+    }
+    MDG_CK(cudaGraphLaunch(h->gx_one[par], h->stream));
+    par ^= 1;
+  }
+  h->par = par;
+  return MDG_OK;
+}
+
+int check_handle(mdg_handle *h, bool need_state) {
+  if (!h) return MDG_ERR_INVALID;
+  if (need_state && !h->has_state) return fail(h, MDG_ERR_NOT_READY, "no particle state loaded");
+  cudaError_t e = cudaSetDevice(h->prm.device);
+  if (e != cudaSuccess) return fail(h, MDG_ERR_CUDA, cudaGetErrorString(e));
+  return MDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mdg_version(void) { return kVersion; }
+
+void mdg_params_default(mdg_params *p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->capacity = 1000000;
+  p->precision = MDG_FP64;
+  p->box[0] = p->box[1] = p->box[2] = 50.0;
+  p->cutoff = 3.0;   // CUTOFF_LENGTH (mdconfig.h:15)
+  p->margin = 0.3;   // BufferLength (simulationinfo.cc:6)
+  p->dt = 0.001;     // TimeStep default (simulationinfo.cc:9)
+  p->thermostat = MDG_NVE;
+  p->langevin_half_drift_compat = 1;
+  p->temperature = 1.0;  // AimedTemperature default
+  p->gamma = 0.1;        // HeatbathGamma default
+  p->tau = 0.1;          // HeatbathTau default
+  p->seed = 1;
+  p->use_graphs = 1;
+}
+
+int mdg_create(const mdg_params *p, mdg_handle **out) {
+  if (!p || !out) return MDG_ERR_INVALID;
+  *out = nullptr;
+  if (p->capacity <= 0 || p->capacity > mdg::kMaxParticles) return MDG_ERR_INVALID;
+  if (!(p->cutoff > 0.0) || !(p->margin >= 0.0) || !(p->dt > 0.0)) return MDG_ERR_INVALID;
+  if (p->precision != MDG_FP64 && p->precision != MDG_MIXED) return MDG_ERR_INVALID;
+  if (p->thermostat < MDG_NVE || p->thermostat > MDG_NOSEHOOVER) return MDG_ERR_INVALID;
+  mdg_handle *h = new mdg_handle();
+  h->prm = *p;
+  memset(&h->g, 0, sizeof(h->g));
+  memset(&h->d, 0, sizeof(h->d));
+  int rc = setup_geometry(h);
+  if (rc) {
+    delete h;
+    return rc;
+  }
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, p->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&h->hflags, sizeof(DevFlags));
+  if (e == cudaSuccess) e = cudaMallocHost((void **)&h->hobs, 4 * sizeof(double));
+  const size_t cap = (size_t)p->capacity;
+  h->cap = p->capacity;
+  mdg::Dev &d = h->d;
+  const size_t ncell = (size_t)h->g.ncell;
+  const size_t nred = (cap + 127) / 128 + 1;
+  if (e == cudaSuccess) e = dalloc(&d.q_end, cap);
+  if (e == cudaSuccess) e = dalloc(&d.q_mid[0], cap);
+  if (e == cudaSuccess) e = dalloc(&d.q_mid[1], cap);
+  if (e == cudaSuccess) e = dalloc(&d.p, cap);
+  if (e == cudaSuccess) e = dalloc(&d.q_build, cap);
+  if (e == cudaSuccess) e = dalloc(&d.t_q, cap);
+  if (e == cudaSuccess) e = dalloc(&d.t_p, cap);
+  if (e == cudaSuccess) e = dalloc(&d.qf, cap);
+  if (e == cudaSuccess && p->precision == MDG_MIXED) e = dalloc(&d.loc[0], cap);
+  if (e == cudaSuccess && p->precision == MDG_MIXED) e = dalloc(&d.loc[1], cap);
+  if (e == cudaSuccess) e = dalloc(&d.id, cap);
+  if (e == cudaSuccess) e = dalloc(&d.inv, cap);
+  if (e == cudaSuccess) e = dalloc(&d.cell, cap);
+  if (e == cudaSuccess) e = dalloc(&d.t_id, cap);
+  if (e == cudaSuccess) e = dalloc(&d.t_cell, cap);
+  if (e == cudaSuccess) e = dalloc(&d.order, cap);
+  if (e == cudaSuccess) e = dalloc(&d.cell_count, ncell);
+  if (e == cudaSuccess) e = dalloc(&d.cell_fill, ncell);
+  if (e == cudaSuccess) e = dalloc(&d.cell_start, ncell + 1);
+  if (e == cudaSuccess) e = dalloc(&d.block_sums, 4096);
+  if (e == cudaSuccess) e = dalloc(&d.ncount, cap);
+  if (e == cudaSuccess) e = dalloc(&d.partials, 3 * nred);
+  if (e == cudaSuccess) e = dalloc(&d.flags, 1);
+  if (e == cudaSuccess) e = dalloc(&d.io4, cap);
+  if (e == cudaSuccess) e = dalloc(&d.io4b, cap);
+  if (e == cudaSuccess) e = dalloc(&h->dobs, 4);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.cell_count, 0, ncell * sizeof(int), h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.cell_fill, 0, ncell * sizeof(int), h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.flags, 0, sizeof(DevFlags), h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  d.nblocks_red = (int)nred;
+  h->g.stride = h->cap;
+  if (e != cudaSuccess) {
+    std::string msg = cudaGetErrorString(e);
+    mdg_destroy(h);
+    fprintf(stderr, "mdg_create: %s\n", msg.c_str());
+    return MDG_ERR_CUDA;
+  }
+  *out = h;
+  return MDG_OK;
+}
+
+int mdg_destroy(mdg_handle *h) {
+  if (!h) return MDG_OK;
+  cudaSetDevice(h->prm.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
+  dfree_all(h);
+  if (h->hflags) cudaFreeHost(h->hflags);
+  if (h->hobs) cudaFreeHost(h->hobs);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return MDG_OK;
+}
+
+const char *mdg_last_error(const mdg_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+static int set_state_common(mdg_handle *h, int32_t n) {
+  h->g.n = n;
+  if (!h->d.nl || h->prm.list_capacity > 0 || h->g.list_cap < 8) {
+    int lc = h->prm.list_capacity > 0 ? ((h->prm.list_capacity + 7) & ~7) : estimate_list_cap(h, n);
+    if (!h->d.nl || lc != h->g.list_cap) {
+      int rc = alloc_list(h, lc);
+      if (rc) return rc;
+    }
+  }
+  DevFlags f;
+  memset(&f, 0, sizeof f);
+  f.rebuild = 1;
+  f.bad_slot = INT_MAX;
+  f.exp1 = 1.0;
+  *h->hflags = f;
+  MDG_CK(cudaMemsetAsync(h->d.cell_count, 0, (size_t)h->g.ncell * sizeof(int), h->stream));
+  MDG_CK(cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.ncell * sizeof(int), h->stream));
+  MDG_CK(cudaMemcpyAsync(h->d.flags, h->hflags, sizeof(DevFlags), cudaMemcpyHostToDevice, h->stream));
+  MDG_CK(cudaStreamSynchronize(h->stream));
+  drop_graphs(h);
+  h->has_state = true;
+  h->nh_init = true;
+  h->par = 0;
+  h->steps_host = 0;
+  return MDG_OK;
+}
+
+int mdg_set_state(mdg_handle *h, const double *q4, const double *p4, int32_t n) {
+  int rc = check_handle(h, false);
+  if (rc) return rc;
+  if (!q4 || !p4 || n <= 0) return fail(h, MDG_ERR_INVALID, "null state or n <= 0");
+  if (n > h->cap) return fail(h, MDG_ERR_CAPACITY, "more particles than the handle capacity");
+  MDG_CK(cudaMemcpyAsync(h->d.io4, q4, (size_t)n * sizeof(double4_32a), cudaMemcpyHostToDevice, h->stream));
+  MDG_CK(cudaMemcpyAsync(h->d.io4b, p4, (size_t)n * sizeof(double4_32a), cudaMemcpyHostToDevice, h->stream));
+  h->g.n = n;
+  mdg::launch_sort_in(h->g, h->d, h->d.io4, h->d.io4b, h->stream);
+  return set_state_common(h, n);
+}
+
+int mdg_set_state_device(mdg_handle *h, const double *q4, const double *p4, int32_t n) {
+  int rc = check_handle(h, false);
+  if (rc) return rc;
+  if (!q4 || !p4 || n <= 0) return fail(h, MDG_ERR_INVALID, "null state or n <= 0");
+  if (n > h->cap) return fail(h, MDG_ERR_CAPACITY, "more particles than the handle capacity");
+  h->g.n = n;
+  mdg::launch_sort_in(h->g, h->d, (const double4_32a *)q4, (const double4_32a *)p4, h->stream);
+  return set_state_common(h, n);
+}
+
+int mdg_get_state(mdg_handle *h, double *q4, double *p4) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  mdg::launch_unsort(h->g, h->d, q4 ? h->d.io4 : nullptr, p4 ? h->d.io4b : nullptr, h->stream);
+  const size_t bytes = (size_t)h->g.n * sizeof(double4_32a);
+  if (q4) MDG_CK(cudaMemcpyAsync(q4, h->d.io4, bytes, cudaMemcpyDeviceToHost, h->stream));
+  if (p4) MDG_CK(cudaMemcpyAsync(p4, h->d.io4b, bytes, cudaMemcpyDeviceToHost, h->stream));
+  MDG_CK(cudaStreamSynchronize(h->stream));
+  return MDG_OK;
+}
+
+int mdg_get_state_device(mdg_handle *h, double *q4, double *p4) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  mdg::launch_unsort(h->g, h->d, (double4_32a *)q4, (double4_32a *)p4, h->stream);
+  MDG_CK(cudaGetLastError());
+  return MDG_OK;
+}
+
+int mdg_make_pairlist(mdg_handle *h) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  return ensure_list(h, true);
+}
+
+int mdg_calculate(mdg_handle *h, int32_t nsteps) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  if (nsteps < 0) return fail(h, MDG_ERR_INVALID, "negative step count");
+  if (nsteps == 0) return MDG_OK;
+  if (h->prm.thermostat == MDG_NOSEHOOVER && h->nh_init) {
+    mdg::launch_nh_init(h->g, h->d, h->stream);
+    h->nh_init = false;
+  }
+  MDG_CK(cudaEventRecord(h->ev0, h->stream));
+  long long done = 0;
+  for (int attempt = 0; attempt < 64 && done < nsteps; attempt++) {
+    const unsigned long long before = (unsigned long long)h->steps_host;
+    rc = enqueue_steps(h, (int)(nsteps - done));
+    if (rc) return rc;
+    rc = read_flags(h);
+    if (rc) return rc;
+    long long completed = (long long)(h->hflags->steps - before);
+    if (h->hflags->halt == 0) {
+      done += completed;
+      h->steps_host = (long long)h->hflags->steps;
+      continue;
+    }
+    if (h->hflags->halt != mdg::kHaltOverflow) return halt_error(h);
+    completed -= 1;
+    done += completed;
+    rc = recover_overflow(h, true);
+    if (rc) return rc;
+    h->steps_host = (long long)h->hflags->steps - 1;
+  }
+  MDG_CK(cudaEventRecord(h->ev1, h->stream));
+  MDG_CK(cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  if (done != nsteps) return fail(h, MDG_ERR_CAPACITY, "neighbour list could not be sized");
+  return MDG_OK;
+}
+
+int mdg_observe(mdg_handle *h, double out[3]) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  if (!out) return fail(h, MDG_ERR_INVALID, "null output");
+  rc = ensure_list(h, false);
+  if (rc) return rc;
+  mdg::launch_observe(h->g, h->d, h->dobs, h->stream);
+  MDG_CK(cudaMemcpyAsync(h->hobs, h->dobs, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  MDG_CK(cudaStreamSynchronize(h->stream));
+  out[0] = h->hobs[0];
+  out[1] = h->hobs[1];
+  out[2] = h->hobs[2];
+  return MDG_OK;
+}
+
+int mdg_forces(mdg_handle *h, double *f4) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  if (!f4) return fail(h, MDG_ERR_INVALID, "null output");
+  rc = ensure_list(h, false);
+  if (rc) return rc;
+  mdg::launch_forces(h->g, h->d, h->prm.precision, h->par, h->stream);
+  MDG_CK(cudaMemcpyAsync(f4, h->d.io4, (size_t)h->g.n * sizeof(double4_32a), cudaMemcpyDeviceToHost, h->stream));
+  MDG_CK(cudaStreamSynchronize(h->stream));
+  return MDG_OK;
+}
+
+int mdg_pairs(mdg_handle *h, int32_t *rec, int64_t cap, int64_t *count) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  if (!count) return fail(h, MDG_ERR_INVALID, "null count");
+  rc = ensure_list(h, false);
+  if (rc) return rc;
+  const int n = h->g.n;
+  std::vector<int> cnt(n);
+  MDG_CK(cudaMemcpyAsync(cnt.data(), h->d.ncount, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  MDG_CK(cudaStreamSynchronize(h->stream));
+  std::vector<long long> off(n + 1, 0);
+  for (int i = 0; i < n; i++) off[i + 1] = off[i] + cnt[i];
+  *count = off[n];
+  if (!rec || cap <= 0) return MDG_OK;
+  long long *doff = nullptr;
+  int32_t *drec = nullptr;
+  MDG_CK(dalloc(&doff, (size_t)n + 1));
+  cudaError_t e = dalloc(&drec, (size_t)off[n] * 3);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(doff, off.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) {
+    mdg::launch_pairs(h->g, h->d, doff, drec, h->stream);
+    const int64_t m = cap < off[n] ? cap : off[n];
+    e = cudaMemcpyAsync(rec, drec, (size_t)m * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(doff);
+  cudaFree(drec);
+  if (e != cudaSuccess) return fail(h, MDG_ERR_CUDA, cudaGetErrorString(e));
+  return MDG_OK;
+}
+
+int mdg_set_seed(mdg_handle *h, uint64_t seed) {
+  int rc = check_handle(h, false);
+  if (rc) return rc;
+  h->prm.seed = seed;
+  h->g.seed = seed;
+  drop_graphs(h);
+  return MDG_OK;
+}
+
+int mdg_set_thermostat(mdg_handle *h, int32_t thermostat, double temperature) {
+  int rc = check_handle(h, false);
+  if (rc) return rc;
+  if (thermostat < MDG_NVE || thermostat > MDG_NOSEHOOVER) return fail(h, MDG_ERR_INVALID, "bad thermostat");
+  h->prm.thermostat = thermostat;
+  h->prm.temperature = temperature;
+  rc = setup_geometry(h);
+  if (rc) return rc;
+  h->nh_init = true;
+  drop_graphs(h);
+  return MDG_OK;
+}
+
+int mdg_get_stats(mdg_handle *h, mdg_stats *s) {
+  int rc = check_handle(h, false);
+  if (rc) return rc;
+  if (!s) return fail(h, MDG_ERR_INVALID, "null stats");
+  memset(s, 0, sizeof(*s));
+  if (h->has_state) {
+    rc = read_flags(h);
+    if (rc) return rc;
+    s->steps = (int64_t)h->hflags->steps;
+    s->rebuilds = (int64_t)h->hflags->rebuilds;
+    s->max_neighbours = h->hflags->max_count;
+    s->listed_pairs = (int64_t)h->hflags->pairs;
+    s->zeta = h->hflags->zeta;
+  }
+  s->list_capacity = h->g.list_cap;
+  for (int k = 0; k < 3; k++) s->cells[k] = h->g.nc[k];
+  s->particles = h->has_state ? h->g.n : 0;
+  s->elapsed_ms = h->last_ms;
+  return MDG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,246 @@
+// Pair-list rebuild, part 1: periodic wrap, cell binning and the stable
+// reorder of particles by cell.
+//
+// Replaces MeshList::MakeMesh (meshlist.cc:153-205, counting sort into
+// cells), MeshList::Sort (meshlist.cc:117-150, reorder of q/p by cell) and the
+// wrap of Variables::AdjustPeriodicBoundary (variables.cc:59-79, applied only
+// at a rebuild).  Every kernel here is a no-op unless flags->rebuild is set, so
+// the whole sequence can sit in every captured step and cost one near-empty
+// wave when no rebuild is due.  Grids are a few waves of the SM count with
+// grid-stride loops.
+//
+// Order inside a cell is by caller particle index, which makes the slot order
+// (and with it every later summation order) independent of the atomics used
+// to fill the cells.
+#include "mdg_internal.cuh"
+
+namespace mdg {
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ bool rebuild_off(const DevFlags *f) { return f->halt != 0 || f->rebuild == 0; }
+
+// Exclusive scan of one int per thread over a 1024-thread block; returns the
+// block total in *total.
+__device__ int block_exclusive_scan(int v, int *total) {
+  __shared__ int warp_tot[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int t = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    warp_tot[lane] = t;  // inclusive
+  }
+  __syncthreads();
+  const int warp_off = wid ? warp_tot[wid - 1] : 0;
+  *total = warp_tot[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+// Wraps q_end into the box with the reference rule (one +-L per component),
+// bins it and counts cell occupancy.  Thread 0 also advances the step and
+// Langevin counters of a step that is starting.
+__global__ void k_wrap_bin(Geom g, Dev d, int count_step, int lang_step) {
+  DevFlags *f = d.flags;
+  if (count_step && blockIdx.x == 0 && threadIdx.x == 0 && f->halt == 0) {
+    f->steps += 1;
+    if (lang_step) f->lang += 1;
+  }
+  if (rebuild_off(f)) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+    double4_32a q = d.q_end[i];
+    double x[3] = {q.x, q.y, q.z};
+    int c[3];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      double v = x[k];
+      if (v < 0.0) v += g.L[k];
+      else if (v > g.L[k]) v -= g.L[k];
+      if (!(v >= 0.0 && v <= g.L[k])) bad = true;  // also catches NaN
+      x[k] = v;
+      int ci = bad ? 0 : (int)(v * g.inv_w[k]);
+      c[k] = ci < 0 ? 0 : (ci >= g.nc[k] ? g.nc[k] - 1 : ci);
+    }
+    if (bad) {
+      halt_with(f, kHaltBadState);
+      atomicMin(&f->bad_slot, i);
+      continue;
+    }
+    q.x = x[0]; q.y = x[1]; q.z = x[2];
+    d.q_end[i] = q;
+    const int cc = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+    d.cell[i] = cc;
+    atomicAdd(&d.cell_count[cc], 1);
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(Geom g, Dev d) {
+  if (rebuild_off(d.flags)) return;
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++)
+    if (base + k < g.ncell) s += d.cell_count[base + k];
+  int total;
+  block_exclusive_scan(s, &total);
+  if (threadIdx.x == 0) d.block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_top(int nblocks, Dev d) {
+  if (rebuild_off(d.flags)) return;
+  const int base = threadIdx.x * kScanItems;
+  int v[kScanItems], s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    v[k] = (base + k < nblocks) ? d.block_sums[base + k] : 0;
+    s += v[k];
+  }
+  int total;
+  int off = block_exclusive_scan(s, &total);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    if (base + k < nblocks) d.block_sums[base + k] = off;
+    off += v[k];
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(Geom g, Dev d) {
+  if (rebuild_off(d.flags)) return;
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int v[kScanItems], s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    v[k] = (base + k < g.ncell) ? d.cell_count[base + k] : 0;
+    s += v[k];
+  }
+  int total;
+  int off = block_exclusive_scan(s, &total) + d.block_sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++) {
+    if (base + k < g.ncell) {
+      d.cell_start[base + k] = off;
+      d.cell_count[base + k] = 0;
+      d.cell_fill[base + k] = 0;
+    }
+    off += v[k];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.cell_start[g.ncell] = g.n;
+}
+
+__global__ void k_scatter(Geom g, Dev d) {
+  if (rebuild_off(d.flags)) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
+    const int c = d.cell[i];
+    d.order[d.cell_start[c] + atomicAdd(&d.cell_fill[c], 1)] = i;
+  }
+}
+
+// Insertion sort of each cell's slots by caller index (cells hold tens of particles).
+__global__ void k_cell_sort(Geom g, Dev d) {
+  if (rebuild_off(d.flags)) return;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < g.ncell; c += gridDim.x * blockDim.x) {
+    const int a = d.cell_start[c], b = d.cell_start[c + 1];
+    for (int k = a + 1; k < b; k++) {
+      const int v = d.order[k], key = d.id[v];
+      int m = k - 1;
+      while (m >= a && d.id[d.order[m]] > key) {
+        d.order[m + 1] = d.order[m];
+        m--;
+      }
+      d.order[m + 1] = v;
+    }
+  }
+}
+
+__global__ void k_reorder(Geom g, Dev d) {
+  if (rebuild_off(d.flags)) return;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.n; k += gridDim.x * blockDim.x) {
+    const int o = d.order[k];
+    d.t_q[k] = d.q_end[o];
+    d.t_p[k] = d.p[o];
+    d.t_id[k] = d.id[o];
+    d.t_cell[k] = d.cell[o];
+  }
+}
+
+// Copies the sorted staging back, records the build positions and derives the
+// positions the next force evaluation uses: q_mid = q + p dt/2 (the first
+// half-drift, fcalculator.cc:21-32, rounded as two separate operations).
+__global__ void k_finalize(Geom g, Dev d, int q_mid_dst) {
+  double4_32a *q_mid = d.q_mid[q_mid_dst];
+  if (rebuild_off(d.flags)) return;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.n; k += gridDim.x * blockDim.x) {
+    const double4_32a q = d.t_q[k], p = d.t_p[k];
+    const int id = d.t_id[k], c = d.t_cell[k];
+    d.q_end[k] = q;
+    d.p[k] = p;
+    d.id[k] = id;
+    d.cell[k] = c;
+    d.inv[id] = k;
+    d.q_build[k] = q;
+    d.qf[k] = make_float4((float)q.x, (float)q.y, (float)q.z, 0.0f);
+    double4_32a m = q;
+    m.x = __dadd_rn(q.x, __dmul_rn(p.x, g.dt2));
+    m.y = __dadd_rn(q.y, __dmul_rn(p.y, g.dt2));
+    m.z = __dadd_rn(q.z, __dmul_rn(p.z, g.dt2));
+    q_mid[k] = m;
+    if (d.loc[q_mid_dst]) {
+      const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+      const double ox = ((double)cx + 0.5) * (double)g.w32[0];
+      const double oy = ((double)cy + 0.5) * (double)g.w32[1];
+      const double oz = ((double)cz + 0.5) * (double)g.w32[2];
+      d.loc[q_mid_dst][k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), 0.0f);
+    }
+  }
+}
+
+__global__ void k_set_rebuild(DevFlags *f) {
+  if (f->halt == 0) f->rebuild = 1;
+}
+
+}  // namespace
+
+// Declared in mdg_list.cu.
+void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s);
+
+void launch_set_rebuild(const Dev &d, cudaStream_t s) { k_set_rebuild<<<1, 1, 0, s>>>(d.flags); }
+
+void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cudaStream_t s, bool count_step,
+                    bool lang_step) {
+  const int threads = 256;
+  int grid = (g.n + threads - 1) / threads;
+  const int cap = num_sms * 8;
+  if (grid > cap) grid = cap;
+  if (grid < 1) grid = 1;
+  int cgrid = (g.ncell + threads - 1) / threads;
+  if (cgrid > cap) cgrid = cap;
+  const int nb = (g.ncell + kScanTile - 1) / kScanTile;
+  k_wrap_bin<<<grid, threads, 0, s>>>(g, d, count_step ? 1 : 0, lang_step ? 1 : 0);
+  k_scan_reduce<<<nb, kScanThreads, 0, s>>>(g, d);
+  k_scan_top<<<1, kScanThreads, 0, s>>>(nb, d);
+  k_scan_apply<<<nb, kScanThreads, 0, s>>>(g, d);
+  k_scatter<<<grid, threads, 0, s>>>(g, d);
+  k_cell_sort<<<cgrid, threads, 0, s>>>(g, d);
+  k_reorder<<<grid, threads, 0, s>>>(g, d);
+  k_finalize<<<grid, threads, 0, s>>>(g, d, q_mid_dst);
+  launch_build_list(g, d, num_sms, s);
+}
+
+}  // namespace mdg

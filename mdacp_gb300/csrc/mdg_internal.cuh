@@ -1,0 +1,111 @@
+// Internal declarations shared by the mdg CUDA translation units.
+//
+// Device data layout (one box, n particles, slots sorted by cell):
+//   q_end[n]   double4_32a  positions at the step boundary (the reference's q)
+//   q_mid[2][n] double4_32a positions after the first half-drift; the step kernel
+//                       reads one buffer and writes the other
+//   p[n]       double4_32a  momenta (= velocities, m = 1)
+//   q_build[n] double4_32a  positions at the last list build (displacement check)
+//   id[n]      int      caller's particle index of each slot; inv[id] = slot
+//   cell[n]    int      home cell of each slot at the last build
+//   nl[cap*n]  uint32   neighbour list, ELL layout: entry k of slot i at k*stride+i
+//                       bits 0..25 partner slot, bits 26..31 stencil offset
+//                       (ox+1) | (oy+1)<<2 | (oz+1)<<4
+//   ncount[n]  int      entries in row i
+//   loc[n]     float4   (mixed form) position relative to the home-cell centre
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mdg.h"
+
+namespace mdg {
+
+// 32-byte read-only load of a double4_32a as two 16-byte non-coherent loads.
+__device__ __forceinline__ double4_32a ldg4(const double4_32a *p) {
+  const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+  return make_double4_32a(a.x, a.y, b.x, b.y);
+}
+
+constexpr int kJBits = 26;
+constexpr uint32_t kJMask = (1u << kJBits) - 1u;
+constexpr int kMaxParticles = 1 << kJBits;
+
+// halt codes
+constexpr int kHaltOverflow = 1;
+constexpr int kHaltBadState = 2;
+
+struct DevFlags {
+  int rebuild;                  // rebuild the list at the start of the next step
+  int halt;                     // nonzero: an error stopped the run; kernels are no-ops
+  int overflow_max;             // largest row requested when a row overflowed
+  int max_count;                // largest row at the last build
+  unsigned long long steps;     // steps begun since the state was set
+  unsigned long long lang;      // Langevin stream position (applications begun)
+  unsigned long long rebuilds;  // completed list builds
+  unsigned long long pairs;     // directed pairs at the last build
+  int bad_slot;
+  int pad0;
+  double zeta;                  // Nose-Hoover zeta (Variables::Zeta) after the last step
+  double zeta_a;                // zeta after the first update of the coming step
+  double exp1;                  // exp(-dt/2 * zeta_a)
+  double t_cur;                 // temperature of the current momenta
+};
+
+struct Geom {
+  double L[3];
+  double w[3];        // cell widths
+  double inv_w[3];
+  int nc[3];
+  int ncell;
+  int n;              // particles
+  int stride;         // ELL row stride (allocated particle capacity)
+  int list_cap;       // entries per row
+  double sl2, rc2;    // (rc+margin)^2, rc^2
+  float pre2;         // FP32 prefilter threshold (rc+margin+1e-3)^2
+  float rc2f;
+  double c0, c2, c2x8;
+  double dt, dt2;
+  double half_margin2;
+  // thermostats
+  double gamma, temperature, tau, hb_d;  // hb_d = sqrt(2 gamma T / dt)
+  uint64_t seed;
+  // mixed form
+  float w32[3];       // cell widths rounded to float
+  float dl32[3];      // L - nc * w32
+  float c2x8f;
+};
+
+struct Dev {
+  double4_32a *q_end, *q_mid[2], *p, *q_build;
+  double4_32a *t_q, *t_p;   // reorder staging
+  float4 *qf;           // float copy of wrapped q_end (list prefilter)
+  float4 *loc[2];       // mixed-form local positions at q_mid[0] / q_mid[1]
+  int *id, *inv, *cell, *t_id, *t_cell, *order;
+  int *cell_count, *cell_fill, *cell_start, *block_sums;
+  uint32_t *nl;
+  int *ncount;
+  double *partials;     // reduction scratch
+  int nblocks_red;
+  DevFlags *flags;
+  double4_32a *io4;         // caller-order staging for get/set/forces
+  double4_32a *io4b;
+};
+
+// host-side launchers (stream-ordered; none synchronises)
+void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cudaStream_t s, bool count_step,
+                    bool lang_step);
+void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compat, int mixed, cudaStream_t s);
+void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s);
+void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s);
+void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s);
+void launch_unsort(const Geom &g, const Dev &d, double4_32a *qo, double4_32a *po, cudaStream_t s);
+void launch_sort_in(const Geom &g, const Dev &d, const double4_32a *qi, const double4_32a *pi, cudaStream_t s);
+void launch_pairs(const Geom &g, const Dev &d, const long long *row_off, int32_t *rec, cudaStream_t s);
+void launch_set_rebuild(const Dev &d, cudaStream_t s);
+
+// device helpers
+__device__ __forceinline__ void halt_with(DevFlags *f, int code) { atomicCAS(&f->halt, 0, code); }
+
+}  // namespace mdg

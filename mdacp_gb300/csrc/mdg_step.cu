@@ -1,0 +1,435 @@
+// One MD step as one kernel, plus the observers and the state exchange.
+//
+// k_step replaces, for one step of MDManager::Calculate (mdmanager.cc:116-148):
+//   ForceCalculator::CalculateForce (fcalculator.cc:35-50, 229-290): the LJ
+//     pair force of the smoothly truncated potential, applied as p += F dt;
+//   the thermostat of MDManager::CalculateLangevin / CalculateNoseHoover
+//     (mdmanager.cc:160-192, fcalculator.cc:743-778);
+//   the second half-drift ForceCalculator::UpdatePositionHalf (fcalculator.cc:21-32)
+//     and the first half-drift of the following step;
+//   the expiry test of PairList::IsPairListExpired (pairlist.cc:26-45), here the
+//     displacement criterion |q - q_build| > margin/2.
+// It is a gather over the full neighbour list: one thread per particle, no
+// atomics, no reaction scatter (the "Reactless" form, fcalculator.cc:504-542).
+//
+// FP64 form: the pair force is evaluated in double precision.  1/r^2 comes
+// from the hardware reciprocal estimate (rcp.approx.ftz.f64) refined by one
+// Householder step of order three, y <- y (1 + e + e^2), e = 1 - r^2 y, which
+// cubes the relative error of the estimate.
+// Mixed form: particle positions relative to their home-cell centre in
+// float; the pair force in float; the per-particle sums in compensated float
+// (Knuth's TwoSum); momentum and position updates in double.
+#include "mdg_internal.cuh"
+
+namespace mdg {
+
+namespace {
+
+constexpr int kStepThreads = 128;
+
+__device__ __forceinline__ double rcp_hh3(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double e = fma(-x, y, 1.0);
+  return fma(y, fma(e, e, e), y);
+}
+
+// Knuth TwoSum accumulation: s + c carries the sum to about twice float precision.
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x) {
+  const float t = s + x;
+  const float bp = t - s;
+  const float err = (s - (t - bp)) + (x - bp);
+  s = t;
+  c += err;
+}
+
+struct CellPos {
+  int cx, cy, cz;
+  bool edge;
+};
+
+__device__ __forceinline__ CellPos cell_pos(const Geom &g, int c) {
+  CellPos r;
+  r.cx = c % g.nc[0];
+  const int t = c / g.nc[0];
+  r.cy = t % g.nc[1];
+  r.cz = t / g.nc[1];
+  r.edge = r.cx == 0 || r.cy == 0 || r.cz == 0 || r.cx == g.nc[0] - 1 || r.cy == g.nc[1] - 1 || r.cz == g.nc[2] - 1;
+  return r;
+}
+
+// Image of partner position qj seen from a particle in cell cp through stencil
+// offset bits of entry e: +-L where the offset crosses the periodic boundary.
+__device__ __forceinline__ void apply_image(const Geom &g, const CellPos &cp, uint32_t e, double4_32a &qj) {
+  const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+  if (ox == 0 && cp.cx == 0) qj.x -= g.L[0];
+  else if (ox == 2 && cp.cx == g.nc[0] - 1) qj.x += g.L[0];
+  if (oy == 0 && cp.cy == 0) qj.y -= g.L[1];
+  else if (oy == 2 && cp.cy == g.nc[1] - 1) qj.y += g.L[1];
+  if (oz == 0 && cp.cz == 0) qj.z -= g.L[2];
+  else if (oz == 2 && cp.cz == g.nc[2] - 1) qj.z += g.L[2];
+}
+
+// Sum over the row of slot i of f(r) (q_j - q_i), f(r) = 24 r^-8 - 48 r^-14 + 8 C2,
+// the force on i (fcalculator.cc:263-277 without the dt factor).
+__device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const double4_32a *__restrict__ pos, int i) {
+  const double4_32a qi = pos[i];
+  const CellPos cp = cell_pos(g, d.cell[i]);
+  const int cnt = d.ncount[i];
+  const uint32_t *row = d.nl + i;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  for (int k = 0; k < cnt; k++) {
+    const uint32_t e = __ldg(row + (size_t)k * g.stride);
+    double4_32a qj = ldg4(pos + (e & kJMask));
+    if (cp.edge) apply_image(g, cp, e, qj);
+    const double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 <= g.rc2) {
+      const double inv = rcp_hh3(r2);
+      const double i6 = inv * inv * inv;
+      const double df = (i6 * inv) * fma(-48.0, i6, 24.0) + g.c2x8;
+      fx = fma(df, dx, fx);
+      fy = fma(df, dy, fy);
+      fz = fma(df, dz, fz);
+    }
+  }
+  return make_double3(fx, fy, fz);
+}
+
+// Mixed form of force_fp64 on home-cell-local float positions.  The offset
+// between the home cells of i and j is ox*w + s*(L - nc*w) per axis, s the
+// periodic wrap of the stencil step.
+__device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i) {
+  const float4 li = loc[i];
+  const CellPos cp = cell_pos(g, d.cell[i]);
+  const float mx0 = -g.w32[0] - (cp.cx == 0 ? g.dl32[0] : 0.0f), px0 = g.w32[0] + (cp.cx == g.nc[0] - 1 ? g.dl32[0] : 0.0f);
+  const float mx1 = -g.w32[1] - (cp.cy == 0 ? g.dl32[1] : 0.0f), px1 = g.w32[1] + (cp.cy == g.nc[1] - 1 ? g.dl32[1] : 0.0f);
+  const float mx2 = -g.w32[2] - (cp.cz == 0 ? g.dl32[2] : 0.0f), px2 = g.w32[2] + (cp.cz == g.nc[2] - 1 ? g.dl32[2] : 0.0f);
+  const int cnt = d.ncount[i];
+  const uint32_t *row = d.nl + i;
+  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  const float rc2 = g.rc2f, c2x8 = g.c2x8f;
+  for (int k = 0; k < cnt; k++) {
+    const uint32_t e = __ldg(row + (size_t)k * g.stride);
+    const float4 lj = __ldg(loc + (e & kJMask));
+    const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+    const float offx = ox == 0 ? mx0 : (ox == 2 ? px0 : 0.0f);
+    const float offy = oy == 0 ? mx1 : (oy == 2 ? px1 : 0.0f);
+    const float offz = oz == 0 ? mx2 : (oz == 2 ? px2 : 0.0f);
+    const float dx = (lj.x - li.x) + offx, dy = (lj.y - li.y) + offy, dz = (lj.z - li.z) + offz;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 <= rc2) {
+      float inv;
+      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+      const float i6 = inv * inv * inv;
+      const float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8;
+      two_sum_acc(sx, cx, df * dx);
+      two_sum_acc(sy, cy, df * dy);
+      two_sum_acc(sz, cz, df * dz);
+    }
+  }
+  return make_double3((double)sx + (double)cx, (double)sy + (double)cy, (double)sz + (double)cz);
+}
+
+__device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) { return __umulhi(a, b); }
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and Box-Muller in float:
+// the Langevin noise stream, keyed by seed, counted by (particle, step).
+__device__ __forceinline__ void langevin_normals(uint64_t seed, uint32_t id, uint64_t step, double z[3]) {
+  uint32_t c0 = id, c1 = (uint32_t)step, c2 = (uint32_t)(step >> 32), c3 = 0x4C4A4D44u;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    const uint32_t hi0 = mulhi32(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    const uint32_t hi1 = mulhi32(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+  }
+  const float s24 = 5.9604644775390625e-08f;
+  const float u1 = (float)((c0 >> 8) + 1u) * s24, u2 = (float)(c1 >> 8) * s24;
+  const float u3 = (float)((c2 >> 8) + 1u) * s24, u4 = (float)(c3 >> 8) * s24;
+  const float twopi = 6.28318530717958647692f;
+  const float ra = sqrtf(-2.0f * logf(u1)), rb = sqrtf(-2.0f * logf(u3));
+  z[0] = (double)(ra * cosf(twopi * u2));
+  z[1] = (double)(ra * sinf(twopi * u2));
+  z[2] = (double)(rb * cosf(twopi * u4));
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+  __syncthreads();
+  return t;
+}
+
+template <int THERMO, int COMPAT, int MIXED>
+__global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
+  const DevFlags *f = d.flags;
+  if (f->halt != 0) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = i < g.n;
+  const double4_32a *qm = d.q_mid[par];
+  double4_32a *qn = d.q_mid[par ^ 1];
+  double ke = 0.0;
+  if (active) {
+    const double3 F = MIXED ? force_mixed(g, d, d.loc[par], i) : force_fp64(g, d, qm, i);
+    double4_32a p = d.p[i];
+    if (THERMO == MDG_NOSEHOOVER) {
+      const double e1 = f->exp1;
+      p.x *= e1; p.y *= e1; p.z *= e1; p.w *= e1;
+      p.x += F.x * g.dt; p.y += F.y * g.dt; p.z += F.z * g.dt;
+      p.x *= e1; p.y *= e1; p.z *= e1; p.w *= e1;
+    } else {
+      p.x += F.x * g.dt; p.y += F.y * g.dt; p.z += F.z * g.dt;
+    }
+    if (THERMO == MDG_LANGEVIN) {
+      double z[3];
+      langevin_normals(g.seed, (uint32_t)d.id[i], f->lang - 1ull, z);
+      p.x += (-g.gamma * p.x + g.hb_d * z[0]) * g.dt;
+      p.y += (-g.gamma * p.y + g.hb_d * z[1]) * g.dt;
+      p.z += (-g.gamma * p.z + g.hb_d * z[2]) * g.dt;
+    }
+    const double4_32a q0 = qm[i];
+    double4_32a qe = q0, q1;
+    if (!(THERMO == MDG_LANGEVIN && COMPAT)) {
+      qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, g.dt2));
+      qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, g.dt2));
+      qe.z = __dadd_rn(q0.z, __dmul_rn(p.z, g.dt2));
+    }
+    q1 = qe;
+    q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, g.dt2));
+    q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, g.dt2));
+    q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, g.dt2));
+    const double4_32a qb = d.q_build[i];
+    const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
+    if (ux * ux + uy * uy + uz * uz > g.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
+      d.flags->rebuild = 1;
+    d.p[i] = p;
+    d.q_end[i] = qe;
+    qn[i] = q1;
+    if (MIXED) {
+      const int c = d.cell[i];
+      const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+      d.loc[par ^ 1][i] = make_float4((float)(q1.x - ((double)cx + 0.5) * (double)g.w32[0]),
+                             (float)(q1.y - ((double)cy + 0.5) * (double)g.w32[1]),
+                             (float)(q1.z - ((double)cz + 0.5) * (double)g.w32[2]), 0.0f);
+    }
+    if (THERMO == MDG_NOSEHOOVER)
+      ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+  }
+  if (THERMO == MDG_NOSEHOOVER) {
+    __shared__ double sh[kStepThreads / 32];
+    const double t = block_sum(ke, sh);
+    if (threadIdx.x == 0) d.partials[blockIdx.x] = t;
+  }
+}
+
+// Nose-Hoover bookkeeping after a step (mdmanager.cc:169-174) and before the
+// next (mdmanager.cc:161-164): T from the block sums in fixed order.
+__global__ void k_nh_update(Geom g, Dev d, int nparts, int first) {
+  DevFlags *f = d.flags;
+  if (f->halt != 0) return;
+  __shared__ double sh[32];
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) v += d.partials[b];
+  const double ke = block_sum(v, sh);
+  if (threadIdx.x == 0) {
+    const double T = ke / (double)g.n / 1.5;
+    const double dt2 = g.dt * 0.5;
+    const double t1 = (T - g.temperature) / (g.tau * g.tau);
+    const double zeta = first ? f->zeta : f->zeta_a + t1 * dt2;
+    f->zeta = zeta;
+    f->t_cur = T;
+    f->zeta_a = zeta + t1 * dt2;
+    f->exp1 = exp(-dt2 * f->zeta_a);
+  }
+}
+
+__global__ void __launch_bounds__(kStepThreads) k_kinetic(Geom g, Dev d) {
+  __shared__ double sh[kStepThreads / 32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double ke = 0.0;
+  if (i < g.n) {
+    const double4_32a p = d.p[i];
+    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+  }
+  const double t = block_sum(ke, sh);
+  if (threadIdx.x == 0) d.partials[blockIdx.x] = t;
+}
+
+// Observers at the step-boundary positions q_end: kinetic energy
+// (observer.cc:5-15), pair energy (observer.cc:17-48) and virial
+// (observer.cc:50-79), each pair evaluated with the reference's expression
+// and rounding and weighted 1/2 (each pair is listed from both sides).
+__global__ void __launch_bounds__(kStepThreads) k_observe(Geom g, Dev d) {
+  __shared__ double sh[kStepThreads / 32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double ke = 0.0, pe = 0.0, vir = 0.0;
+  if (i < g.n) {
+    const double4_32a p = d.p[i];
+    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+    const double4_32a qi = d.q_end[i];
+    const CellPos cp = cell_pos(g, d.cell[i]);
+    const int cnt = d.ncount[i];
+    for (int k = 0; k < cnt; k++) {
+      const uint32_t e = d.nl[(size_t)k * g.stride + i];
+      double4_32a qj = d.q_end[e & kJMask];
+      if (cp.edge) apply_image(g, cp, e, qj);
+      const double dx = __dsub_rn(qi.x, qj.x), dy = __dsub_rn(qi.y, qj.y), dz = __dsub_rn(qi.z, qj.z);
+      const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+      if (r2 > g.rc2) continue;
+      const double r4 = __dmul_rn(r2, r2), r6 = __dmul_rn(r4, r2), r8 = __dmul_rn(r6, r2), r10 = __dmul_rn(r8, r2),
+                   r12 = __dmul_rn(r10, r2);
+      const double e_ij = 4.0 * (1.0 / r12 - 1.0 / r6 + __dmul_rn(g.c2, r2) + g.c0);
+      const double df = (__dsub_rn(__dmul_rn(24.0, r6), 48.0) / (__dmul_rn(__dmul_rn(r6, r6), r2)) + g.c2x8) * r2;
+      pe += 0.5 * e_ij;
+      vir += 0.5 * df;
+    }
+  }
+  const double a = block_sum(ke, sh);
+  const double b = block_sum(pe, sh);
+  const double c = block_sum(vir, sh);
+  if (threadIdx.x == 0) {
+    d.partials[3 * blockIdx.x + 0] = a;
+    d.partials[3 * blockIdx.x + 1] = b;
+    d.partials[3 * blockIdx.x + 2] = c;
+  }
+}
+
+__global__ void k_observe_final(Dev d, int nparts, double *out) {
+  __shared__ double sh[32];
+  double a = 0.0, b = 0.0, c = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+    a += d.partials[3 * k + 0];
+    b += d.partials[3 * k + 1];
+    c += d.partials[3 * k + 2];
+  }
+  const double ta = block_sum(a, sh), tb = block_sum(b, sh), tc = block_sum(c, sh);
+  if (threadIdx.x == 0) {
+    out[0] = ta;
+    out[1] = tb;
+    out[2] = tc / 3.0;
+  }
+}
+
+// Forces at q_end in the handle's precision, written in caller order to io4.
+template <int MIXED>
+__global__ void __launch_bounds__(kStepThreads) k_forces(Geom g, Dev d, const float4 *loc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  const double3 F = MIXED ? force_mixed(g, d, loc, i) : force_fp64(g, d, d.q_end, i);
+  d.io4[d.id[i]] = make_double4_32a(F.x, F.y, F.z, 0.0);
+}
+
+// Float positions of q_end relative to the home-cell centres (k_forces<1> input).
+__global__ void k_loc_from_end(Geom g, Dev d, float4 *loc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  const double4_32a q = d.q_end[i];
+  const int c = d.cell[i];
+  const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+  loc[i] = make_float4((float)(q.x - ((double)cx + 0.5) * (double)g.w32[0]),
+                         (float)(q.y - ((double)cy + 0.5) * (double)g.w32[1]),
+                         (float)(q.z - ((double)cz + 0.5) * (double)g.w32[2]), 0.0f);
+}
+
+__global__ void k_unsort(Geom g, Dev d, double4_32a *qo, double4_32a *po) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  const int id = d.id[i];
+  if (qo) qo[id] = d.q_end[i];
+  if (po) po[id] = d.p[i];
+}
+
+__global__ void k_sort_in(Geom g, Dev d, const double4_32a *qi, const double4_32a *pi) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  double4_32a q = qi[i], p = pi[i];
+  q.w = 0.0;
+  p.w = 0.0;
+  d.q_end[i] = q;
+  d.p[i] = p;
+  d.id[i] = i;
+  d.inv[i] = i;
+}
+
+__global__ void k_pairs(Geom g, Dev d, const long long *row_off, int32_t *rec) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  const CellPos cp = cell_pos(g, d.cell[i]);
+  const int cnt = d.ncount[i];
+  long long o = row_off[i];
+  for (int k = 0; k < cnt; k++) {
+    const uint32_t e = d.nl[(size_t)k * g.stride + i];
+    const int j = (int)(e & kJMask);
+    const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+    const int sx = (ox == 0 && cp.cx == 0) ? -1 : ((ox == 2 && cp.cx == g.nc[0] - 1) ? 1 : 0);
+    const int sy = (oy == 0 && cp.cy == 0) ? -1 : ((oy == 2 && cp.cy == g.nc[1] - 1) ? 1 : 0);
+    const int sz = (oz == 0 && cp.cz == 0) ? -1 : ((oz == 2 && cp.cz == g.nc[2] - 1) ? 1 : 0);
+    rec[3 * (o + k) + 0] = d.id[i];
+    rec[3 * (o + k) + 1] = d.id[j];
+    rec[3 * (o + k) + 2] = (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1);
+  }
+}
+
+inline int blocks_for(int n) { return n > 0 ? (n + kStepThreads - 1) / kStepThreads : 1; }
+
+}  // namespace
+
+void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compat, int mixed, cudaStream_t s) {
+  const int grid = blocks_for(g.n);
+#define MDG_STEP(T, C, M) k_step<T, C, M><<<grid, kStepThreads, 0, s>>>(g, d, par)
+  if (thermostat == MDG_LANGEVIN) {
+    if (compat) { if (mixed) MDG_STEP(MDG_LANGEVIN, 1, 1); else MDG_STEP(MDG_LANGEVIN, 1, 0); }
+    else { if (mixed) MDG_STEP(MDG_LANGEVIN, 0, 1); else MDG_STEP(MDG_LANGEVIN, 0, 0); }
+  } else if (thermostat == MDG_NOSEHOOVER) {
+    if (mixed) MDG_STEP(MDG_NOSEHOOVER, 0, 1); else MDG_STEP(MDG_NOSEHOOVER, 0, 0);
+    k_nh_update<<<1, 1024, 0, s>>>(g, d, grid, 0);
+  } else {
+    if (mixed) MDG_STEP(MDG_NVE, 0, 1); else MDG_STEP(MDG_NVE, 0, 0);
+  }
+#undef MDG_STEP
+}
+
+void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s) {
+  const int grid = blocks_for(g.n);
+  k_kinetic<<<grid, kStepThreads, 0, s>>>(g, d);
+  k_nh_update<<<1, 1024, 0, s>>>(g, d, grid, 1);
+}
+
+void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s) {
+  const int grid = blocks_for(g.n);
+  k_observe<<<grid, kStepThreads, 0, s>>>(g, d);
+  k_observe_final<<<1, 1024, 0, s>>>(d, grid, out_dev);
+}
+
+void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s) {
+  const int grid = blocks_for(g.n);
+  if (mixed) {
+    // the buffer the next step overwrites before reading it
+    k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
+    k_forces<1><<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
+  } else {
+    k_forces<0><<<grid, kStepThreads, 0, s>>>(g, d, nullptr);
+  }
+}
+
+void launch_unsort(const Geom &g, const Dev &d, double4_32a *qo, double4_32a *po, cudaStream_t s) {
+  k_unsort<<<blocks_for(g.n), kStepThreads, 0, s>>>(g, d, qo, po);
+}
+
+void launch_sort_in(const Geom &g, const Dev &d, const double4_32a *qi, const double4_32a *pi, cudaStream_t s) {
+  k_sort_in<<<blocks_for(g.n), kStepThreads, 0, s>>>(g, d, qi, pi);
+}
+
+void launch_pairs(const Geom &g, const Dev &d, const long long *row_off, int32_t *rec, cudaStream_t s) {
+  k_pairs<<<blocks_for(g.n), kStepThreads, 0, s>>>(g, d, row_off, rec);
+}
+
+}  // namespace mdg

@@ -1,0 +1,159 @@
+"""Host-side mirror of MDACP's MDManager for one periodic box on one GPU.
+
+Method names follow the reference (mdmanager.h:32-83): MakePairList ->
+make_pairlist, Calculate -> calculate, Temperature / Pressure / TotalEnergy /
+KineticEnergy / PotentialEnergy, SetSeed, SetControlTemperature,
+SetAimedTemperature, GetTotalParticleNumber.  Every call goes through the C
+ABI of libmdg.so (include/mdg.h); nothing here computes physics.
+"""
+import ctypes
+
+import numpy as np
+
+from . import native
+from .config import Parameter, SimulationInfo
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _as4(x):
+    x = np.asarray(x, dtype=np.float64)
+    out = np.zeros((len(x), 4), dtype=np.float64)
+    out[:, :3] = x[:, :3]
+    return out
+
+
+class MDManager:
+    def __init__(self, box, capacity=None, cutoff=3.0, margin=0.3, dt=0.001, precision="fp64",
+                 thermostat="nve", temperature=1.0, gamma=0.1, tau=0.1, seed=1, langevin_half_drift_compat=True,
+                 list_capacity=0, device=0, use_graphs=True, n=None):
+        self.lib = native.load()
+        prm = native.Params()
+        self.lib.mdg_params_default(ctypes.byref(prm))
+        box = np.broadcast_to(np.asarray(box, dtype=np.float64), (3,))
+        prm.box[:] = [float(v) for v in box]
+        prm.capacity = int(capacity or n or 1000000)
+        prm.cutoff, prm.margin, prm.dt = float(cutoff), float(margin), float(dt)
+        prm.precision = {"fp64": native.FP64, "mixed": native.MIXED}[precision]
+        prm.thermostat = {"nve": native.NVE, "langevin": native.LANGEVIN, "nosehoover": native.NOSEHOOVER}[thermostat]
+        prm.temperature, prm.gamma, prm.tau = float(temperature), float(gamma), float(tau)
+        prm.seed = int(seed)
+        prm.langevin_half_drift_compat = 1 if langevin_half_drift_compat else 0
+        prm.list_capacity = int(list_capacity)
+        prm.device = int(device)
+        prm.use_graphs = 1 if use_graphs else 0
+        self.params = prm
+        self.L = np.array(prm.box[:])
+        h = ctypes.c_void_p()
+        native.check(self.lib.mdg_create(ctypes.byref(prm), ctypes.byref(h)))
+        self._h = h
+        self.n = 0
+
+    @classmethod
+    def from_cfg(cls, param, n, **overrides):
+        """Builds a manager from .cfg keys (SimulationInfo semantics plus the mdg keys)."""
+        if not isinstance(param, Parameter):
+            param = Parameter.from_file(param)
+        si = SimulationInfo(param)
+        kw = dict(box=si.L, capacity=n, cutoff=si.cutoff, margin=si.buffer_length, dt=si.time_step,
+                  precision=si.precision, thermostat=si.thermostat, temperature=si.aimed_temperature,
+                  gamma=si.heatbath_gamma, tau=si.heatbath_tau, seed=param.get_int("Seed", 1),
+                  langevin_half_drift_compat=si.langevin_half_drift_compat)
+        kw.update(overrides)
+        return cls(**kw)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.mdg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        native.check(rc, self._h)
+
+    # state ---------------------------------------------------------------
+    def set_state(self, q, p):
+        q4, p4 = _as4(q), _as4(p)
+        self.n = len(q4)
+        self._ck(self.lib.mdg_set_state(self._h, _dp(q4), _dp(p4), self.n))
+
+    def state(self):
+        q4 = np.zeros((self.n, 4))
+        p4 = np.zeros((self.n, 4))
+        self._ck(self.lib.mdg_get_state(self._h, _dp(q4), _dp(p4)))
+        return q4[:, :3], p4[:, :3]
+
+    # hot path ------------------------------------------------------------
+    def make_pairlist(self):
+        self._ck(self.lib.mdg_make_pairlist(self._h))
+
+    def calculate(self, nsteps=1):
+        self._ck(self.lib.mdg_calculate(self._h, int(nsteps)))
+
+    def forces(self):
+        f4 = np.zeros((self.n, 4))
+        self._ck(self.lib.mdg_forces(self._h, _dp(f4)))
+        return f4[:, :3]
+
+    def pairs(self):
+        cnt = ctypes.c_int64()
+        self._ck(self.lib.mdg_pairs(self._h, None, 0, ctypes.byref(cnt)))
+        rec = np.zeros((cnt.value, 3), dtype=np.int32)
+        self._ck(self.lib.mdg_pairs(self._h, rec.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cnt.value,
+                                    ctypes.byref(cnt)))
+        return rec
+
+    # observation (mdmanager.cc:390-429) ------------------------------------
+    def observe_raw(self):
+        out = np.zeros(3)
+        self._ck(self.lib.mdg_observe(self._h, _dp(out)))
+        return out
+
+    def observe(self):
+        """(T, P, E, KE/N, PE/N, virial/N) as MDManager reports them."""
+        ke, pe, vir = self.observe_raw()
+        n = float(self.n)
+        T = ke / n / 1.5
+        V = float(self.L[0] * self.L[1] * self.L[2])
+        P = (T - vir / n) * n / V
+        return np.array([T, P, ke / n + pe / n, ke / n, pe / n, vir / n])
+
+    def temperature(self):
+        return self.observe()[0]
+
+    def pressure(self):
+        return self.observe()[1]
+
+    def total_energy(self):
+        return self.observe()[2]
+
+    def kinetic_energy(self):
+        return self.observe()[3]
+
+    def potential_energy(self):
+        return self.observe()[4]
+
+    def get_total_particle_number(self):
+        return self.n
+
+    # control -------------------------------------------------------------
+    def set_seed(self, seed):
+        self._ck(self.lib.mdg_set_seed(self._h, int(seed)))
+
+    def set_thermostat(self, thermostat, temperature):
+        t = {"nve": native.NVE, "langevin": native.LANGEVIN, "nosehoover": native.NOSEHOOVER}[thermostat]
+        self._ck(self.lib.mdg_set_thermostat(self._h, t, float(temperature)))
+
+    def stats(self):
+        s = native.Stats()
+        self._ck(self.lib.mdg_get_stats(self._h, ctypes.byref(s)))
+        return {"steps": s.steps, "rebuilds": s.rebuilds, "list_capacity": s.list_capacity,
+                "max_neighbours": s.max_neighbours, "listed_pairs": s.listed_pairs, "cells": tuple(s.cells),
+                "particles": s.particles, "zeta": s.zeta, "elapsed_ms": s.elapsed_ms}

@@ -1,0 +1,169 @@
+"""GPU parity against the oracle (the C restatement pinned bitwise to the reference).
+
+Tolerances: pair set bit-exact; FP64 forces |dF_i| <= 1e-12 max(|F_i|, sum_j |f_ij|)
+and ||dF||/||F|| <= 1e-12; E/T/P traces over 100 steps relative 1e-10;
+mixed-precision RMS relative force error <= 1e-5.
+"""
+import numpy as np
+import pytest
+
+from oracle import port
+from tests.helpers import directed_pair_keys, liquid_like, pair_force_abs_sum
+
+pytestmark = pytest.mark.gpu
+
+RC, MARGIN = 2.5, 0.5
+
+
+def _gpu(L, n, **kw):
+    from mdacp_gb300.manager import MDManager
+    kw.setdefault("cutoff", RC)
+    kw.setdefault("margin", MARGIN)
+    return MDManager(L, capacity=n, **kw)
+
+
+@pytest.mark.parametrize("density,cells", [(0.5, 20), (0.8, 10), (0.5, 8)])
+def test_pair_set_bit_exact(density, cells):
+    q, p, L = liquid_like(density, cells, seed=cells)
+    n = len(q)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+    ref.make_pairlist()
+    rk = directed_pair_keys(ref.pairs(), n, half=True)
+    m = _gpu(L, n)
+    m.set_state(q, p)
+    m.make_pairlist()
+    gk = directed_pair_keys(m.pairs(), n, half=False)
+    assert len(gk) == len(rk)
+    assert np.array_equal(gk, rk)
+
+
+@pytest.mark.parametrize("density,cells", [(0.5, 20), (0.8, 10)])
+def test_forces_fp64(density, cells):
+    q, p, L = liquid_like(density, cells, seed=100 + cells)
+    n = len(q)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+    ref.make_pairlist()
+    fr = ref.forces()
+    scale = np.maximum(np.linalg.norm(fr, axis=1), pair_force_abs_sum(q, L, ref.pairs(), RC))
+    m = _gpu(L, n)
+    m.set_state(q, p)
+    f = m.forces()
+    df = np.linalg.norm(f - fr, axis=1)
+    assert np.all(df <= 1e-12 * scale), (df / scale).max()
+    assert np.linalg.norm(f - fr) <= 1e-12 * np.linalg.norm(fr)
+
+
+def test_observables_match_reference_expression():
+    q, p, L = liquid_like(0.5, 12, seed=5)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+    ref.make_pairlist()
+    m = _gpu(L, len(q))
+    m.set_state(q, p)
+    o, orf = m.observe_raw(), ref.observe_raw()
+    np.testing.assert_allclose(o, orf, rtol=1e-13)
+
+
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_nve_trace_100_steps(use_graphs):
+    q, p, L = liquid_like(0.5, 20, seed=9)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN, dt=0.001)
+    ref.make_pairlist()
+    m = _gpu(L, len(q), dt=0.001, use_graphs=use_graphs)
+    m.set_state(q, p)
+    m.make_pairlist()
+    rows, rrows = [m.observe()], [ref.observe()]
+    for _ in range(10):
+        m.calculate(10)
+        ref.calculate(10)
+        rows.append(m.observe())
+        rrows.append(ref.observe())
+    rows, rrows = np.array(rows), np.array(rrows)
+    np.testing.assert_allclose(rows, rrows, rtol=1e-10, atol=1e-12)
+    qg, pg = m.state()
+    qr, pr = ref.state()
+    dq = np.abs((qg - qr + L / 2) % L - L / 2).max()
+    assert dq < 1e-10 and np.abs(pg - pr).max() < 1e-10
+    assert m.stats()["steps"] == 100
+
+
+def test_mixed_force_error():
+    q, p, L = liquid_like(0.5, 20, seed=21)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+    ref.make_pairlist()
+    fr = ref.forces()
+    m = _gpu(L, len(q), precision="mixed")
+    m.set_state(q, p)
+    f = m.forces()
+    rel = np.linalg.norm(f - fr, axis=1) / np.linalg.norm(fr, axis=1)
+    rms = np.sqrt(np.mean(rel ** 2))
+    assert rms <= 1e-5, rms
+
+
+def test_mixed_trace_close():
+    q, p, L = liquid_like(0.5, 16, seed=23)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+    ref.make_pairlist()
+    m = _gpu(L, len(q), precision="mixed")
+    m.set_state(q, p)
+    m.calculate(100)
+    ref.calculate(100)
+    np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-5, atol=1e-6)
+
+
+def test_langevin_matches_oracle_stream():
+    q, p, L = liquid_like(0.5, 12, seed=31)
+    kw = dict(dt=0.005, thermostat="langevin", temperature=0.9, gamma=1.0, seed=12345)
+    m = _gpu(L, len(q), **kw)
+    m.set_state(q, p)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN, dt=0.005, thermostat=port.LANGEVIN, temperature=0.9,
+                      gamma=1.0, seed=12345)
+    ref.make_pairlist()
+    m.calculate(40)
+    ref.calculate(40)
+    qg, pg = m.state()
+    qr, pr = ref.state()
+    assert np.abs(pg - pr).max() < 1e-5
+    np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-5, atol=1e-6)
+
+
+def test_nosehoover_matches_oracle():
+    q, p, L = liquid_like(0.5, 12, seed=41, temperature=1.3)
+    m = _gpu(L, len(q), thermostat="nosehoover", temperature=1.0, tau=0.1)
+    m.set_state(q, p)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN, thermostat=port.NOSEHOOVER, temperature=1.0, tau=0.1)
+    ref.make_pairlist()
+    m.calculate(50)
+    ref.calculate(50)
+    np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-10, atol=1e-12)
+    assert abs(m.stats()["zeta"] - ref.zeta) < 1e-10
+
+
+def test_overflow_regrows_list():
+    q, p, L = liquid_like(0.8, 8, seed=51)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+    ref.make_pairlist()
+    fr = ref.forces()
+    m = _gpu(L, len(q), list_capacity=8)
+    m.set_state(q, p)
+    f = m.forces()
+    assert m.stats()["list_capacity"] > 8
+    assert np.linalg.norm(f - fr) <= 1e-12 * np.linalg.norm(fr)
+    m.calculate(30)
+    ref.calculate(30)
+    np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-10, atol=1e-12)
+
+
+def test_state_roundtrip_and_bad_state():
+    from mdacp_gb300 import native
+    q, p, L = liquid_like(0.5, 6, seed=61)
+    m = _gpu(L, len(q))
+    m.set_state(q, p)
+    qg, pg = m.state()
+    assert np.array_equal(qg, q) and np.array_equal(pg, p)
+    bad = q.copy()
+    bad[3, 1] = np.nan
+    m.set_state(bad, p)
+    with pytest.raises(native.MDGError, match="bad particle state"):
+        m.make_pairlist()
+    m.set_state(q, p)   # the handle stays usable
+    m.calculate(5)
