@@ -1,0 +1,319 @@
+#!/usr/bin/env python3
+"""Benchmark of the MDACP LJ hot path on GB300: atom-steps/s at 4M atoms, mixed vs FP64.
+
+Workload (the large NVE configuration): 100^3 FCC unit cells = 4,000,000 atoms,
+density 0.5 (L = 200), Maxwell velocities at T = 1 (seeded), rc = 2.5,
+margin 0.5, dt = 0.001, NVE drift-kick-drift.  One benchmark step is one MD
+step of the whole box: list rebuild when due, fused force/kick/drift kernel.
+Inputs are synthetic (seeded lattice + velocities); they are larger than L2
+(positions, momenta and the neighbour list total > 2 GB), so no flush is needed.
+
+value     mixed-form atom-steps/s over K steps, device time (CUDA events on the
+          library's stream), max over ranks, summed over ranks.
+e2e       the same through the public C ABI from host memory: pinned host state
+          uploaded with mdg_set_state, K calls of mdg_calculate(1), mdg_observe
+          every 100 steps (as Benchmark::Run observes), state read back with
+          mdg_get_state; wall clock.
+roofline  the fused step kernel (mixed): algorithmic bytes per launch
+          n * (pairs_per_atom * 20 B + 72 B) over its mean launch time from a
+          CUDA-event-bracketed pass of the same workload.
+--impl reference  the reference's CPU implementation on the host cores: the
+          reference binary built from its sources when present (oracle/_ref),
+          else the oracle's C restatement, with all host threads.
+
+Multi-GPU: independent replica boxes, one per rank (no collective on the data
+path); scaling is weak.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LJ atom-steps/s, 4M atoms: mixed vs FP64 on 1 GB300 @ rel force err<=1e-5"
+UNIT = "atom-steps/s"
+RC, MARGIN, DT, TEMP, DENSITY = 2.5, 0.5, 0.001, 1.0, 0.5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="mdg", choices=["mdg", "reference"])
+    ap.add_argument("--cells", type=int, default=100, help="FCC unit cells per side (100 -> 4M atoms)")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
+    return ap.parse_args()
+
+
+class Dist:
+    def __init__(self, n):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling during a timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def workload(cells, seed):
+    from mdacp_gb300 import lattice
+    q, L = lattice.fcc_cube(cells, DENSITY)
+    p = lattice.maxwell(len(q), TEMP, seed)
+    return q, p, L
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_atom(form):
+    """DRAM bytes per atom of one step-kernel launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)[form]["dram_bytes_per_atom"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def cpu_sample(q, p, L, budget_s, threads, prefer_reference=True):
+    """Times the reference CPU path on the same workload; returns (atom-steps/s, descr)."""
+    n = len(q)
+    from oracle import refrun
+    if prefer_reference and refrun.available(RC):
+        # the reference itself, timed like Benchmark::Run (list build outside,
+        # observation every ObserveLoop=100 steps inside); a 2-step probe sizes the run
+        def mups(steps):
+            out = refrun.run("bench", q, p, L, rc=RC, margin=MARGIN, dt=DT, steps=steps, observe_every=100,
+                             threads=threads, timeout=max(600, int(budget_s * 20)))
+            line = [x for x in out["stdout"].splitlines() if "[MUPS]" in x][-1]
+            return float(line.split("[SEC]")[1].split("[MUPS]")[0])
+        probe = mups(2)
+        steps = max(2, min(100, int(budget_s * probe * 1e6 / n)))
+        v = mups(steps) * 1e6
+        return v, "reference", "MDACP reference binary, %d steps of the full %d-atom box, %d threads" % (
+            steps, n, threads)
+    from oracle import port
+    s = port.System(q, p, L, rc=RC, margin=MARGIN, dt=DT, threads=threads)
+    s.make_pairlist()
+    t0 = time.perf_counter()
+    s.calculate(1)
+    one = time.perf_counter() - t0
+    steps = max(2, min(50, int(budget_s / max(one, 1e-6)) - 1))
+    t0 = time.perf_counter()
+    s.calculate(steps)
+    dt = time.perf_counter() - t0
+    s.close()
+    return n * steps / dt, "port", "oracle C restatement (half list, Newton-3), %d steps of the full %d-atom box, %d threads" % (
+        steps, n, threads)
+
+
+def run_reference(args):
+    d = Dist(args.gpus)
+    if d.rank != 0:
+        d.close()
+        return
+    q, p, L = workload(args.cells, 1)
+    threads = os.cpu_count() or 1
+    value, kind, descr = cpu_sample(q, p, L, args.cpu_seconds, threads)
+    n = len(q)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_block(args, n),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": descr},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    d.close()
+
+
+def config_block(args, n):
+    return {"workload": "LJ NVE %d atoms (%d^3 FCC), rho %.1f, rc %.1f, margin %.1f, dt %g, T %.1f" % (
+        n, args.cells, DENSITY, RC, MARGIN, DT, TEMP), "atoms": n, "density": DENSITY, "cutoff": RC,
+        "margin": MARGIN, "dt": DT, "precision": "mixed (value) / fp64 (fp64 block)",
+        "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas x%d" % args.gpus}
+
+
+def run_mine(args):
+    import numpy as np
+    from mdacp_gb300.manager import MDManager
+    d = Dist(args.gpus)
+    q, p, L = workload(args.cells, 1 + d.rank)
+    n = len(q)
+    K, W = args.steps, max(3, args.warmup)
+    res = {}
+    clk = Clocks(d.local)
+    clocks = None
+    for prec in ("mixed", "fp64"):
+        m = MDManager(L, capacity=n, cutoff=RC, margin=MARGIN, dt=DT, precision=prec, device=d.local)
+        m.set_state(q, p)
+        m.make_pairlist()
+        m.calculate(W)
+        e0 = m.observe()[2]
+        launches0 = m.stats()["kernel_launches"]
+        d.barrier()
+        if prec == "mixed":
+            clk.start()
+        m.calculate(K)
+        st = m.stats()
+        if prec == "mixed":
+            clocks = clk.stop()
+        d.barrier()
+        ms = d.max(st["elapsed_ms"])
+        e1 = m.observe()[2]
+        res[prec] = {"ms": ms, "launches": st["kernel_launches"] - launches0, "rebuilds": st["rebuilds"],
+                     "pairs_per_atom": st["listed_pairs"] / n, "drift": (e1 - e0) / (K * DT),
+                     "handle": m, "stats": st}
+    # force error of the mixed form against FP64 at the same (warmed-up) state
+    mf, md = res["mixed"]["handle"], res["fp64"]["handle"]
+    qs, ps = md.state()
+    mf.set_state(qs, ps)
+    f_mixed = mf.forces()
+    f_fp64 = md.forces()
+    rel = np.linalg.norm(f_mixed - f_fp64, axis=1) / np.maximum(np.linalg.norm(f_fp64, axis=1), 1e-300)
+    rms_err = float(np.sqrt(np.mean(rel ** 2)))
+    # roofline of the fused step kernel (mixed form)
+    kprof = max(50, min(K, 500))
+    mf.make_pairlist()
+    mf.calculate(W)
+    stp = mf.stats()
+    kernel_ms = mf.calculate_profiled(kprof) / kprof
+    ppa = stp["listed_pairs"] / n
+    alg_bytes = n * (ppa * 20.0 + 72.0)
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
+    tpa = ncu_traffic_per_atom("mixed")
+    roof = {"kernel": "k_step<NVE,mixed>", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": (tpa * n) if tpa else None, "algorithmic_bytes": alg_bytes,
+            "launch_ms": kernel_ms, "pairs_per_atom": ppa}
+    for prec in ("mixed", "fp64"):
+        res[prec]["handle"].close()
+    # end to end through the C ABI with host buffers
+    import torch
+    qh = torch.zeros((n, 4), dtype=torch.float64).pin_memory().numpy()
+    ph = torch.zeros((n, 4), dtype=torch.float64).pin_memory().numpy()
+    qh[:, :3] = q
+    ph[:, :3] = p
+    me = MDManager(L, capacity=n, cutoff=RC, margin=MARGIN, dt=DT, precision="mixed", device=d.local)
+    me.set_state(qh, ph)
+    me.calculate(W)
+    d.barrier()
+    t0 = time.perf_counter()
+    me.set_state(qh, ph)
+    nobs = 0
+    for k in range(K):
+        me.calculate(1)
+        if k % 100 == 0:
+            me.observe_raw()
+            nobs += 1
+    qo, po = me.state()
+    t_e2e = d.max(time.perf_counter() - t0)
+    me.close()
+    e2e_value = d.world * n * K / t_e2e
+    cpu = None
+    if d.rank == 0 and d.world == 1:
+        v, kind, descr = cpu_sample(q, p, L, args.cpu_seconds, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": kind, "sample": descr}
+    mixed, fp64 = res["mixed"], res["fp64"]
+    value = d.world * n * K / (mixed["ms"] * 1e-3)
+    v64 = d.world * n * K / (fp64["ms"] * 1e-3)
+    if d.rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world, "steps": K, "warmup": W,
+                "ms_per_step": mixed["ms"] / K, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 pair force / f64 accumulate-integrate", "data": "synthetic",
+                "config": config_block(args, n),
+                "fp64": {"value": v64, "unit": UNIT, "ms_per_step": fp64["ms"] / K,
+                         "energy_drift_per_atom_per_tau": fp64["drift"], "rebuilds": fp64["rebuilds"]},
+                "mixed_over_fp64": value / v64,
+                "mixed": {"rms_rel_force_err_vs_fp64": rms_err, "energy_drift_per_atom_per_tau": mixed["drift"],
+                          "rebuilds": mixed["rebuilds"], "pairs_per_atom": mixed["pairs_per_atom"]},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 32 / K,
+                        "d2h_bytes_per_step": (2 * n * 32 + 24 * nobs) / K},
+                "gpu_launches": mixed["launches"],
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+    d.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_mine(args)
+
+
+if __name__ == "__main__":
+    main()

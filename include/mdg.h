@@ -70,6 +70,7 @@ typedef struct mdg_stats {
   int32_t particles;
   double zeta;             /* Nose-Hoover friction (Variables::Zeta) */
   double elapsed_ms;       /* device time of the last mdg_calculate call */
+  int64_t kernel_launches; /* kernels this handle has enqueued (graph replays count each node) */
 } mdg_stats;
 
 typedef struct mdg_handle mdg_handle;
@@ -97,6 +98,10 @@ int mdg_get_state(mdg_handle *h, double *q4, double *p4);
 int mdg_make_pairlist(mdg_handle *h);
 /* Replaces nsteps calls of MDManager::Calculate (mdmanager.cc:116-148). */
 int mdg_calculate(mdg_handle *h, int32_t nsteps);
+/* mdg_calculate without graph replay, with a CUDA event pair on the handle's
+ * stream around every launch of the fused step kernel; *step_kernel_ms receives
+ * the summed device time of those launches (for roofline accounting). */
+int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms);
 /* Replaces KineticEnergyObserver, PotentialEnergyObserver and VirialObserver
  * (observer.cc:5-79) at the current positions: out[0] = sum p^2/2,
  * out[1] = sum of pair energies, out[2] = sum of pair virials / 3. */

@@ -40,6 +40,7 @@ struct mdg_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
   long long steps_host = 0;  // completed steps as last read from the device
+  long long launches = 0;    // kernels enqueued (counting every node of a graph replay)
 };
 
 namespace {
@@ -110,7 +111,11 @@ int setup_geometry(mdg_handle *h) {
   g.ncell = (int)ncell;
   g.sl2 = sl * sl;
   g.rc2 = p.cutoff * p.cutoff;
-  g.pre2 = (float)((sl + 1e-3) * (sl + 1e-3));
+  // Float r2 of home-cell-local positions is within ~1e-5 of the exact value
+  // (|local| <= w/2, three roundings per component); a 1e-4 band around SL^2
+  // goes to the exact double test.
+  g.acc_lo = (float)(sl * sl - 1e-4);
+  g.acc_hi = (float)(sl * sl + 1e-4);
   g.rc2f = (float)g.rc2;
   // Variables::Variables (variables.cc:16-28)
   const double s2 = 1.0 / (p.cutoff * p.cutoff);
@@ -192,6 +197,7 @@ int ensure_list(mdg_handle *h, bool force) {
   for (int attempt = 0; attempt < 16; attempt++) {
     if (force) mdg::launch_set_rebuild(h->d, h->stream);
     mdg::launch_rebuild(h->g, h->d, h->par, h->num_sms, h->stream, false, false);
+    h->launches += mdg::kRebuildKernels + (force ? 1 : 0);
     int rc = read_flags(h);
     if (rc) return rc;
     if (h->hflags->halt == 0) return MDG_OK;
@@ -203,10 +209,15 @@ int ensure_list(mdg_handle *h, bool force) {
   return fail(h, MDG_ERR_CAPACITY, "neighbour list could not be sized");
 }
 
-void enqueue_step(mdg_handle *h, int par) {
+int kernels_per_step(const mdg_handle *h) { return mdg::kRebuildKernels + mdg::step_kernels(h->prm.thermostat); }
+
+// Optional events around the step kernel (profiled runs only).
+void enqueue_step(mdg_handle *h, int par, cudaEvent_t before = nullptr, cudaEvent_t after = nullptr) {
   mdg::launch_rebuild(h->g, h->d, par, h->num_sms, h->stream, true, lang_on(h) != 0);
+  if (before) cudaEventRecord(before, h->stream);
   mdg::launch_step(h->g, h->d, par, h->prm.thermostat, h->prm.langevin_half_drift_compat, h->prm.precision,
                    h->stream);
+  if (after) cudaEventRecord(after, h->stream);
 }
 
 int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps) {
@@ -225,6 +236,7 @@ int enqueue_steps(mdg_handle *h, int nsteps) {
   if (!h->prm.use_graphs) {
     for (int k = 0; k < nsteps; k++) {
       enqueue_step(h, par);
+      h->launches += kernels_per_step(h);
       par ^= 1;
     }
     h->par = par;
@@ -238,6 +250,7 @@ int enqueue_steps(mdg_handle *h, int nsteps) {
     }
     while (left >= 2) {
       MDG_CK(cudaGraphLaunch(h->gx_pair[par], h->stream));
+      h->launches += 2 * kernels_per_step(h);
       left -= 2;
     }
   }
@@ -247,6 +260,7 @@ int enqueue_steps(mdg_handle *h, int nsteps) {
       if (rc) return rc;
     }
     MDG_CK(cudaGraphLaunch(h->gx_one[par], h->stream));
+    h->launches += kernels_per_step(h);
     par ^= 1;
   }
   h->par = par;
@@ -408,6 +422,7 @@ int mdg_set_state(mdg_handle *h, const double *q4, const double *p4, int32_t n) 
   MDG_CK(cudaMemcpyAsync(h->d.io4b, p4, (size_t)n * sizeof(double4_32a), cudaMemcpyHostToDevice, h->stream));
   h->g.n = n;
   mdg::launch_sort_in(h->g, h->d, h->d.io4, h->d.io4b, h->stream);
+  h->launches += 1;
   return set_state_common(h, n);
 }
 
@@ -425,6 +440,7 @@ int mdg_get_state(mdg_handle *h, double *q4, double *p4) {
   int rc = check_handle(h, true);
   if (rc) return rc;
   mdg::launch_unsort(h->g, h->d, q4 ? h->d.io4 : nullptr, p4 ? h->d.io4b : nullptr, h->stream);
+  h->launches += 1;
   const size_t bytes = (size_t)h->g.n * sizeof(double4_32a);
   if (q4) MDG_CK(cudaMemcpyAsync(q4, h->d.io4, bytes, cudaMemcpyDeviceToHost, h->stream));
   if (p4) MDG_CK(cudaMemcpyAsync(p4, h->d.io4b, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -453,6 +469,7 @@ int mdg_calculate(mdg_handle *h, int32_t nsteps) {
   if (nsteps == 0) return MDG_OK;
   if (h->prm.thermostat == MDG_NOSEHOOVER && h->nh_init) {
     mdg::launch_nh_init(h->g, h->d, h->stream);
+    h->launches += 2;
     h->nh_init = false;
   }
   MDG_CK(cudaEventRecord(h->ev0, h->stream));
@@ -485,6 +502,53 @@ int mdg_calculate(mdg_handle *h, int32_t nsteps) {
   return MDG_OK;
 }
 
+int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  if (nsteps < 0 || !step_kernel_ms) return fail(h, MDG_ERR_INVALID, "bad arguments");
+  *step_kernel_ms = 0.0;
+  if (h->prm.thermostat == MDG_NOSEHOOVER && h->nh_init) {
+    mdg::launch_nh_init(h->g, h->d, h->stream);
+    h->launches += 2;
+    h->nh_init = false;
+  }
+  constexpr int kChunk = 64;
+  cudaEvent_t ev[2 * kChunk];
+  for (int k = 0; k < 2 * kChunk; k++) MDG_CK(cudaEventCreate(&ev[k]));
+  long long done = 0;
+  double total = 0.0;
+  int status = MDG_OK;
+  for (int guard = 0; guard < 1000000 && done < nsteps && status == MDG_OK; guard++) {
+    const unsigned long long before = (unsigned long long)h->steps_host;
+    const int m = (int)((nsteps - done) < kChunk ? (nsteps - done) : kChunk);
+    for (int k = 0; k < m; k++) {
+      enqueue_step(h, h->par, ev[2 * k], ev[2 * k + 1]);
+      h->launches += kernels_per_step(h);
+      h->par ^= 1;
+    }
+    status = read_flags(h);
+    if (status) break;
+    for (int k = 0; k < m; k++) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]) == cudaSuccess) total += ms;
+    }
+    long long completed = (long long)(h->hflags->steps - before);
+    if (h->hflags->halt == 0) {
+      done += completed;
+      h->steps_host = (long long)h->hflags->steps;
+    } else if (h->hflags->halt == mdg::kHaltOverflow) {
+      done += completed - 1;
+      status = recover_overflow(h, true);
+      h->steps_host = (long long)h->hflags->steps - 1;
+    } else {
+      status = halt_error(h);
+    }
+  }
+  for (int k = 0; k < 2 * kChunk; k++) cudaEventDestroy(ev[k]);
+  *step_kernel_ms = total;
+  return status;
+}
+
 int mdg_observe(mdg_handle *h, double out[3]) {
   int rc = check_handle(h, true);
   if (rc) return rc;
@@ -492,6 +556,7 @@ int mdg_observe(mdg_handle *h, double out[3]) {
   rc = ensure_list(h, false);
   if (rc) return rc;
   mdg::launch_observe(h->g, h->d, h->dobs, h->stream);
+  h->launches += 2;
   MDG_CK(cudaMemcpyAsync(h->hobs, h->dobs, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   out[0] = h->hobs[0];
@@ -507,6 +572,7 @@ int mdg_forces(mdg_handle *h, double *f4) {
   rc = ensure_list(h, false);
   if (rc) return rc;
   mdg::launch_forces(h->g, h->d, h->prm.precision, h->par, h->stream);
+  h->launches += h->prm.precision == MDG_MIXED ? 2 : 1;
   MDG_CK(cudaMemcpyAsync(f4, h->d.io4, (size_t)h->g.n * sizeof(double4_32a), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   return MDG_OK;
@@ -583,6 +649,7 @@ int mdg_get_stats(mdg_handle *h, mdg_stats *s) {
   for (int k = 0; k < 3; k++) s->cells[k] = h->g.nc[k];
   s->particles = h->has_state ? h->g.n : 0;
   s->elapsed_ms = h->last_ms;
+  s->kernel_launches = h->launches;
   return MDG_OK;
 }
 

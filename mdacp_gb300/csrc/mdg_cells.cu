@@ -195,7 +195,12 @@ __global__ void k_finalize(Geom g, Dev d, int q_mid_dst) {
     d.cell[k] = c;
     d.inv[id] = k;
     d.q_build[k] = q;
-    d.qf[k] = make_float4((float)q.x, (float)q.y, (float)q.z, 0.0f);
+    {
+      const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+      d.qf[k] = make_float4((float)(q.x - ((double)cx + 0.5) * (double)g.w32[0]),
+                            (float)(q.y - ((double)cy + 0.5) * (double)g.w32[1]),
+                            (float)(q.z - ((double)cz + 0.5) * (double)g.w32[2]), 0.0f);
+    }
     double4_32a m = q;
     m.x = __dadd_rn(q.x, __dmul_rn(p.x, g.dt2));
     m.y = __dadd_rn(q.y, __dmul_rn(p.y, g.dt2));

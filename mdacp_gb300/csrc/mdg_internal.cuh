@@ -63,7 +63,7 @@ struct Geom {
   int stride;         // ELL row stride (allocated particle capacity)
   int list_cap;       // entries per row
   double sl2, rc2;    // (rc+margin)^2, rc^2
-  float pre2;         // FP32 prefilter threshold (rc+margin+1e-3)^2
+  float acc_lo, acc_hi;  // float r2 below acc_lo: inside SL; above acc_hi: outside; between: exact test
   float rc2f;
   double c0, c2, c2x8;
   double dt, dt2;
@@ -92,6 +92,10 @@ struct Dev {
   double4_32a *io4;         // caller-order staging for get/set/forces
   double4_32a *io4b;
 };
+
+// kernels enqueued by one launch_rebuild and one launch_step call
+constexpr int kRebuildKernels = 11;
+inline int step_kernels(int thermostat) { return thermostat == MDG_NOSEHOOVER ? 2 : 1; }
 
 // host-side launchers (stream-ordered; none synchronises)
 void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cudaStream_t s, bool count_step,

@@ -11,8 +11,10 @@
 // Acceptance is decided exactly as the reference decides it: the image
 // position is formed first, q_j +- L (mdunit.cc:167), then the difference and
 // r2 = dx*dx + dy*dy + dz*dz with every operation rounded separately
-// (meshlist.cc:262-266), accepted when r2 <= SL^2.  A float prefilter with a
-// 1e-3 slack skips candidates that are clearly outside.
+// (meshlist.cc:262-266), accepted when r2 <= SL^2.  Candidates are first
+// measured in float from home-cell-local positions, whose r2 is within 1e-5
+// of the exact value; only those within 1e-4 of SL^2 take the double test,
+// so the result is the exact set at float cost.
 #include "mdg_internal.cuh"
 
 namespace mdg {
@@ -28,30 +30,39 @@ __global__ void __launch_bounds__(kListThreads) k_build_list(Geom g, Dev d) {
   int mx = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
     int cnt = 0;
-    const double4_32a qi = d.q_end[i];
     const float4 fi = d.qf[i];
     const int c = d.cell[i];
     const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
-    const float Lf0 = (float)g.L[0], Lf1 = (float)g.L[1], Lf2 = (float)g.L[2];
     for (int oz = -1; oz <= 1; oz++) {
       int nz = cz + oz, sz = 0;
       if (nz < 0) { nz += g.nc[2]; sz = -1; } else if (nz >= g.nc[2]) { nz -= g.nc[2]; sz = 1; }
+      // offset of the partner cell's centre: oz*w + sz*(L - nc*w)
+      const float offz = (float)oz * g.w32[2] + (float)sz * g.dl32[2];
       for (int oy = -1; oy <= 1; oy++) {
         int ny = cy + oy, sy = 0;
         if (ny < 0) { ny += g.nc[1]; sy = -1; } else if (ny >= g.nc[1]) { ny -= g.nc[1]; sy = 1; }
+        const float offy = (float)oy * g.w32[1] + (float)sy * g.dl32[1];
         for (int ox = -1; ox <= 1; ox++) {
           int nx = cx + ox, sx = 0;
           if (nx < 0) { nx += g.nc[0]; sx = -1; } else if (nx >= g.nc[0]) { nx -= g.nc[0]; sx = 1; }
+          const float offx = (float)ox * g.w32[0] + (float)sx * g.dl32[0];
           const int cc = (nz * g.nc[1] + ny) * g.nc[0] + nx;
           const int a = d.cell_start[cc], b = d.cell_start[cc + 1];
-          const float fx = fi.x - (float)sx * Lf0, fy = fi.y - (float)sy * Lf1, fz = fi.z - (float)sz * Lf2;
+          const float fx = offx - fi.x, fy = offy - fi.y, fz = offz - fi.z;
           const uint32_t code = (uint32_t)((ox + 1) | ((oy + 1) << 2) | ((oz + 1) << 4)) << kJBits;
           const bool self_cell = (sx | sy | sz) == 0;
           for (int j = a; j < b; j++) {
             const float4 fj = d.qf[j];
-            const float ex = fx - fj.x, ey = fy - fj.y, ez = fz - fj.z;
-            if (ex * ex + ey * ey + ez * ez > g.pre2) continue;
+            const float ex = fj.x + fx, ey = fj.y + fy, ez = fj.z + fz;
+            const float r2f = ex * ex + ey * ey + ez * ez;
+            if (r2f > g.acc_hi) continue;
             if (self_cell && j == i) continue;
+            if (r2f < g.acc_lo) {
+              if (cnt < g.list_cap) d.nl[(size_t)cnt * g.stride + i] = (uint32_t)j | code;
+              cnt++;
+              continue;
+            }
+            const double4_32a qi = d.q_end[i];
             const double4_32a qj = d.q_end[j];
             const double xj = sx ? __dadd_rn(qj.x, sx > 0 ? g.L[0] : -g.L[0]) : qj.x;
             const double yj = sy ? __dadd_rn(qj.y, sy > 0 ? g.L[1] : -g.L[1]) : qj.y;

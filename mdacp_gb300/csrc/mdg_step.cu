@@ -105,18 +105,20 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
   const float mx0 = -g.w32[0] - (cp.cx == 0 ? g.dl32[0] : 0.0f), px0 = g.w32[0] + (cp.cx == g.nc[0] - 1 ? g.dl32[0] : 0.0f);
   const float mx1 = -g.w32[1] - (cp.cy == 0 ? g.dl32[1] : 0.0f), px1 = g.w32[1] + (cp.cy == g.nc[1] - 1 ? g.dl32[1] : 0.0f);
   const float mx2 = -g.w32[2] - (cp.cz == 0 ? g.dl32[2] : 0.0f), px2 = g.w32[2] + (cp.cz == g.nc[2] - 1 ? g.dl32[2] : 0.0f);
+  // offset of the partner's cell centre minus i's own local position, per stencil step
+  const float mxl = mx0 - li.x, pxl = px0 - li.x, zxl = -li.x;
+  const float myl = mx1 - li.y, pyl = px1 - li.y, zyl = -li.y;
+  const float mzl = mx2 - li.z, pzl = px2 - li.z, zzl = -li.z;
   const int cnt = d.ncount[i];
   const uint32_t *row = d.nl + i;
+  const size_t stride = (size_t)g.stride;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
   const float rc2 = g.rc2f, c2x8 = g.c2x8f;
-  for (int k = 0; k < cnt; k++) {
-    const uint32_t e = __ldg(row + (size_t)k * g.stride);
-    const float4 lj = __ldg(loc + (e & kJMask));
+  auto pair = [&](uint32_t e, const float4 &lj) {
     const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
-    const float offx = ox == 0 ? mx0 : (ox == 2 ? px0 : 0.0f);
-    const float offy = oy == 0 ? mx1 : (oy == 2 ? px1 : 0.0f);
-    const float offz = oz == 0 ? mx2 : (oz == 2 ? px2 : 0.0f);
-    const float dx = (lj.x - li.x) + offx, dy = (lj.y - li.y) + offy, dz = (lj.z - li.z) + offz;
+    const float dx = lj.x + (ox == 0 ? mxl : (ox == 2 ? pxl : zxl));
+    const float dy = lj.y + (oy == 0 ? myl : (oy == 2 ? pyl : zyl));
+    const float dz = lj.z + (oz == 0 ? mzl : (oz == 2 ? pzl : zzl));
     const float r2 = dx * dx + dy * dy + dz * dz;
     if (r2 <= rc2) {
       float inv;
@@ -127,6 +129,23 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
       two_sum_acc(sy, cy, df * dy);
       two_sum_acc(sz, cz, df * dz);
     }
+  };
+  int k = 0;
+  // four rows' worth of independent index and position loads in flight per thread
+#pragma unroll 1
+  for (; k + 4 <= cnt; k += 4) {
+    uint32_t e[4];
+    float4 l[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) e[u] = __ldg(row + (size_t)(k + u) * stride);
+#pragma unroll
+    for (int u = 0; u < 4; u++) l[u] = __ldg(loc + (e[u] & kJMask));
+#pragma unroll
+    for (int u = 0; u < 4; u++) pair(e[u], l[u]);
+  }
+  for (; k < cnt; k++) {
+    const uint32_t e = __ldg(row + (size_t)k * stride);
+    pair(e, __ldg(loc + (e & kJMask)));
   }
   return make_double3((double)sx + (double)cx, (double)sy + (double)cy, (double)sz + (double)cz);
 }
@@ -208,18 +227,21 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
     q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, g.dt2));
     const double4_32a qb = d.q_build[i];
     const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
-    if (ux * ux + uy * uy + uz * uz > g.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
-      d.flags->rebuild = 1;
+    if (MIXED) {
+      // displacement since the build in float: the expiry test and the new
+      // home-cell-local position (qf holds the local position at the build)
+      const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
+      if (fx * fx + fy * fy + fz * fz > (float)g.half_margin2 || !(fx == fx && fy == fy && fz == fz))
+        d.flags->rebuild = 1;
+      const float4 lb = d.qf[i];
+      d.loc[par ^ 1][i] = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
+    } else {
+      if (ux * ux + uy * uy + uz * uz > g.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
+        d.flags->rebuild = 1;
+    }
     d.p[i] = p;
     d.q_end[i] = qe;
     qn[i] = q1;
-    if (MIXED) {
-      const int c = d.cell[i];
-      const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
-      d.loc[par ^ 1][i] = make_float4((float)(q1.x - ((double)cx + 0.5) * (double)g.w32[0]),
-                             (float)(q1.y - ((double)cy + 0.5) * (double)g.w32[1]),
-                             (float)(q1.z - ((double)cz + 0.5) * (double)g.w32[2]), 0.0f);
-    }
     if (THERMO == MDG_NOSEHOOVER)
       ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
   }

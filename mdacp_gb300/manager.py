@@ -97,6 +97,12 @@ class MDManager:
     def calculate(self, nsteps=1):
         self._ck(self.lib.mdg_calculate(self._h, int(nsteps)))
 
+    def calculate_profiled(self, nsteps):
+        """Steps without graph replay; returns the summed device ms of the fused step kernel."""
+        ms = ctypes.c_double()
+        self._ck(self.lib.mdg_calculate_profiled(self._h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
     def forces(self):
         f4 = np.zeros((self.n, 4))
         self._ck(self.lib.mdg_forces(self._h, _dp(f4)))
@@ -156,4 +162,5 @@ class MDManager:
         self._ck(self.lib.mdg_get_stats(self._h, ctypes.byref(s)))
         return {"steps": s.steps, "rebuilds": s.rebuilds, "list_capacity": s.list_capacity,
                 "max_neighbours": s.max_neighbours, "listed_pairs": s.listed_pairs, "cells": tuple(s.cells),
-                "particles": s.particles, "zeta": s.zeta, "elapsed_ms": s.elapsed_ms}
+                "particles": s.particles, "zeta": s.zeta, "elapsed_ms": s.elapsed_ms,
+                "kernel_launches": s.kernel_launches}

@@ -29,7 +29,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int64), ("rebuilds", ctypes.c_int64), ("list_capacity", ctypes.c_int32),
                 ("max_neighbours", ctypes.c_int32), ("listed_pairs", ctypes.c_int64),
                 ("cells", ctypes.c_int32 * 3), ("particles", ctypes.c_int32), ("zeta", ctypes.c_double),
-                ("elapsed_ms", ctypes.c_double)]
+                ("elapsed_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64)]
 
 
 # Every exported symbol of include/mdg.h, with (restype, argtypes).
@@ -45,6 +45,7 @@ SIGNATURES = {
     "mdg_get_state": (ctypes.c_int, [_P, _D, _D]),
     "mdg_make_pairlist": (ctypes.c_int, [_P]),
     "mdg_calculate": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "mdg_calculate_profiled": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
     "mdg_observe": (ctypes.c_int, [_P, _D]),
     "mdg_forces": (ctypes.c_int, [_P, _D]),
     "mdg_pairs": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,

@@ -1,0 +1,39 @@
+"""Runs one LJ workload through the C ABI for profiling (e.g. under ncu).
+
+    python -m mdacp_gb300.profile_run --cells 63 --precision mixed --steps 8 [--no-graphs]
+
+cells^3 FCC unit cells at density 0.5 (cells=100 -> 4,000,000 atoms, cells=63 ->
+1,000,188 atoms), Maxwell velocities at T=1, rc 2.5, margin 0.5, dt 0.001:
+one list build, then `steps` NVE steps.
+"""
+import argparse
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cells", type=int, default=63)
+    ap.add_argument("--density", type=float, default=0.5)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--no-graphs", action="store_true")
+    a = ap.parse_args()
+    from mdacp_gb300 import lattice
+    from mdacp_gb300.manager import MDManager
+    q, L = lattice.fcc_cube(a.cells, a.density)
+    p = lattice.maxwell(len(q), 1.0, 1)
+    m = MDManager(L, capacity=len(q), cutoff=2.5, margin=0.5, dt=0.001, precision=a.precision,
+                  use_graphs=not a.no_graphs)
+    m.set_state(q, p)
+    m.make_pairlist()
+    m.calculate(a.steps)
+    st = m.stats()
+    print("atoms %d steps %d ms/step %.4f pairs/atom %.2f rebuilds %d" % (
+        len(q), a.steps, st["elapsed_ms"] / max(a.steps, 1), st["listed_pairs"] / len(q), st["rebuilds"]))
+
+
+if __name__ == "__main__":
+    main()

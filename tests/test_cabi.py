@@ -1,0 +1,66 @@
+"""The C-ABI library: builds for sm_103a, loads, and exports every entry point of include/mdg.h.
+
+No compute calls here (no GPU on the CPU runner)."""
+import ctypes
+import os
+import re
+import shutil
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(mdg_\w+)\s*\(", text, re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mdacp_gb300 import build, native
+    if not os.path.exists(native.LIB_PATH):
+        if not shutil.which("nvcc") and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+            pytest.skip("nvcc not available")
+        build.build()
+    return ctypes.CDLL(native.LIB_PATH)
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert "mdg_create" in names and "mdg_calculate" in names and len(names) >= 15
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in _declared():
+        assert hasattr(lib, name), name
+
+
+def test_binding_covers_header():
+    from mdacp_gb300 import native
+    assert set(_declared()) <= set(native.SIGNATURES)
+
+
+def test_version_and_defaults_without_gpu(lib):
+    from mdacp_gb300 import native
+    L = native.load()
+    assert b"sm_103a" in L.mdg_version()
+    p = native.Params()
+    L.mdg_params_default(ctypes.byref(p))
+    assert p.cutoff == 3.0 and abs(p.margin - 0.3) < 1e-15 and p.dt == 0.001 and p.langevin_half_drift_compat == 1
+
+
+def test_invalid_parameters_rejected_before_device_use(lib):
+    from mdacp_gb300 import native
+    L = native.load()
+    p = native.Params()
+    L.mdg_params_default(ctypes.byref(p))
+    p.capacity = -5
+    h = ctypes.c_void_p()
+    assert L.mdg_create(ctypes.byref(p), ctypes.byref(h)) == 1
+    assert not h.value
+    assert L.mdg_destroy(None) == 0
