@@ -128,6 +128,31 @@ int mdg_get_stats(mdg_handle *h, mdg_stats *s);
 int mdg_set_state_device(mdg_handle *h, const double *q4_dev, const double *p4_dev, int32_t n);
 int mdg_get_state_device(mdg_handle *h, double *q4_dev, double *p4_dev);
 
+/* Observers without any allocation (this entry point has no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc -- applications whose
+ * device memory is owned by their own pool, code running in a host callback
+ * or a stream-ordered section that must not allocate or synchronise, or a
+ * caller that holds its particles on the device and has no handle (creating a
+ * handle allocates the whole pair-list machinery).
+ *
+ * q4_dev, p4_dev: caller-owned device arrays [n][4] (positions in any image;
+ * they are wrapped into the box here); out3_dev: caller-owned device buffer of
+ * 3 doubles that receives the sums of mdg_observe: sum p^2/2, the pair energy
+ * and the pair virial / 3, over every image pair within `cutoff` of the
+ * smoothly truncated LJ potential.  Work is enqueued on `stream` (a
+ * cudaStream_t; NULL = legacy default stream) and not synchronised.
+ *
+ * Working memory is one fixed static device array of about 11.3 MB per GPU,
+ * held until the process exits: at most 1,048,576 particles and 262,144 cells
+ * of width >= cutoff (box side / cutoff, rounded down, per axis); larger
+ * inputs return MDG_ERR_CAPACITY with a message on stderr.  The first call on
+ * each device looks up that array's device address (cudaGetSymbolAddress), so
+ * make the first call on a device outside any stream capture.  Every call
+ * reuses the same array: calls that overlap on the GPU (other streams, other
+ * host threads) race and give wrong results; serialise them. */
+int mdg_observe_noalloc(const double *q4_dev, const double *p4_dev, int32_t n, const double box[3], double cutoff,
+                        double *out3_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,7 @@ SIGNATURES = {
     "mdg_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
     "mdg_set_state_device": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32]),
     "mdg_get_state_device": (ctypes.c_int, [_P, _P, _P]),
+    "mdg_observe_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int32, _D, ctypes.c_double, _P, _P]),
 }
 
 _lib = None
