@@ -72,6 +72,27 @@ def build(force=False, verbose=False, extra_flags=()):
     return LIB
 
 
+HOST = os.path.join(HERE, "host")
+HOST_BIN = os.path.join(HERE, "mdg_mdacp")
+
+
+def build_host(force=False):
+    """Links the C++ host front-end (mdg_mdacp) against libmdg.so."""
+    srcs = [os.path.join(HOST, f) for f in ("mdg_host.cpp", "mdg_mdacp.cpp")]
+    deps = srcs + [os.path.join(HOST, "mdg_host.hpp"), os.path.join(ROOT, "include", "mdg.h"), LIB]
+    if not force and not _stale(HOST_BIN, deps):
+        return HOST_BIN
+    cxx = shutil.which("g++") or "g++"
+    tmp = HOST_BIN + ".tmp%d" % os.getpid()
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"), *srcs, "-L", HERE, "-lmdg",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("host build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, HOST_BIN)
+    return HOST_BIN
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
                 extra_flags=["-Xptxas", "-v"] if "-v" in sys.argv else ()))

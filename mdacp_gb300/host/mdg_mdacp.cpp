@@ -1,0 +1,134 @@
+// mdg_mdacp: runs MDACP's Benchmark and Langevin projects (benchmark.cc:12-52,
+// langevin.cc:9-32) on one GB300 through the C ABI.  Usage: mdg_mdacp [input.cfg]
+// (the reference reads input.cfg when no file is given, mdmanager.cc:18-23).
+//
+// Output lines keep the reference's layout: "time T P E #observe" every
+// ObserveLoop steps and "# N = n sec [SEC] mups [MUPS]" at the end.  Both
+// projects build the lattice with ConfigurationMaker's sites (with the 1e-7
+// offset) and give every particle the fixed-speed isotropic velocity of
+// Variables::SetInitialVelocity seeded with the unit id 0.  Extra key:
+// InitialStateFile=<path> writes the initial state (int64 n, n x {q, p}).
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <string>
+
+#include "mdg_host.hpp"
+
+namespace {
+
+double now() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+int lattice_count(const mdghost::Parameter &param) {
+  const mdghost::SimulationInfo si(param);
+  const double s = 1.0 / pow(param.GetDoubleDef("Density", 0.5) * 0.25, 1.0 / 3.0);
+  return 4 * (int)(si.L[0] / s) * (int)(si.L[1] / s) * (int)(si.L[2] / s);
+}
+
+void observe_line(mdghost::MDManager &m, bool tag) {
+  const double T = m.Temperature(), P = m.Pressure(), E = m.TotalEnergy();
+  printf("%.15g %.15g %.15g %.15g%s\n", m.GetSimulationTime(), T, P, E, tag ? " #observe" : "");
+}
+
+void setup(const mdghost::Parameter &param, mdghost::MDManager &m) {
+  mdghost::MakeFCC(param, m);
+  m.SetInitialVelocity(param.GetDoubleDef("InitialVelocity", 1.0), 0);
+  if (param.Contains("InitialStateFile")) m.SaveStateRaw(param.GetStringDef("InitialStateFile", ""));
+}
+
+void run_benchmark(const mdghost::Parameter &param) {
+  const int n = lattice_count(param);
+  mdghost::MDManager m(param, n > 0 ? n : 1);
+  setup(param, m);
+  const int T_LOOP = param.GetIntegerDef("ThermalizeLoop", 150);
+  const int LOOP = param.GetIntegerDef("TotalLoop", 1000);
+  const int OBSERVE_LOOP = param.GetIntegerDef("ObserveLoop", 100);
+  printf("# Number of Particles = %lu\n", m.GetTotalParticleNumber());
+  m.MakePairList();
+  if (T_LOOP > 0) m.Calculate(T_LOOP);
+  const double start = now();
+  for (int i = 0; i < LOOP;) {
+    // steps up to and including the next observation point run as one call
+    int next = i + 1;
+    if (i % OBSERVE_LOOP != 0) next = ((i / OBSERVE_LOOP) + 1) * OBSERVE_LOOP + 1;
+    if (next > LOOP) next = LOOP;
+    m.Calculate(next - i);
+    if ((next - 1) % OBSERVE_LOOP == 0) observe_line(m, true);
+    i = next;
+  }
+  const double sec = now() - start;
+  const unsigned long pn = m.GetTotalParticleNumber();
+  printf("# N = %lu %g [SEC] %g [MUPS]\n", pn, sec, (double)LOOP * (double)pn / sec / 1.0e6);
+}
+
+void run_langevin(const mdghost::Parameter &param) {
+  const int n = lattice_count(param);
+  mdghost::MDManager m(param, n > 0 ? n : 1);
+  setup(param, m);
+  const int LOOP = param.GetIntegerDef("TotalLoop", 1000);
+  const int OBSERVE_LOOP = param.GetIntegerDef("ObserveLoop", 100);
+  m.SetSeed(param.GetIntegerDef("Seed", 1));
+  m.SetControlTemperature(true);
+  printf("# Number of Particles = %lu\n", m.GetTotalParticleNumber());
+  m.MakePairList();
+  for (int i = 0; i < LOOP; i++) {
+    m.Calculate();
+    if (i % OBSERVE_LOOP == 0) observe_line(m, false);
+  }
+}
+
+}  // namespace
+
+// mdg_mdacp --print-config file.cfg: the parsed simulation settings, no GPU use.
+int print_config(const std::string &path) {
+  mdghost::Parameter param;
+  if (!param.LoadFromFile(path)) return 1;
+  try {
+    const mdghost::SimulationInfo si(param);
+    printf("L %.17g %.17g %.17g\n", si.L[0], si.L[1], si.L[2]);
+    printf("TimeStep %.17g\nAimedTemperature %.17g\nHeatbathTau %.17g\nHeatbathGamma %.17g\n", si.TimeStep,
+           si.AimedTemperature, si.HeatbathTau, si.HeatbathGamma);
+    printf("ControlTemperature %d\nHeatbathType %d\nCutoffLength %.17g\nBufferLength %.17g\n",
+           si.ControlTemperature ? 1 : 0, si.HeatbathType, si.CutoffLength, si.BufferLength);
+    printf("Precision %d\nLangevinHalfDriftCompat %d\nMode %s\nlattice %d\n", si.Precision,
+           si.LangevinHalfDriftCompat ? 1 : 0, param.GetStringDef("Mode", "").c_str(), lattice_count(param));
+  } catch (const std::exception &e) {
+    printf("error %s\n", e.what());
+    return 2;
+  }
+  return 0;
+}
+
+int main(int argc, char **argv) {
+  setvbuf(stdout, nullptr, _IOLBF, 0);
+  if (argc > 2 && std::string(argv[1]) == "--print-config") return print_config(argv[2]);
+  printf("# %s\n", mdg_version());
+  const std::string input = argc > 1 ? argv[1] : "input.cfg";
+  mdghost::Parameter param;
+  if (!param.LoadFromFile(input)) {
+    printf("Could not open input file %s\n", input.c_str());
+    printf("Program is aborted.\n");
+    return 1;
+  }
+  if (!param.Contains("Mode")) {
+    printf("Mode is not defined in inputfile.\n");
+    return 1;
+  }
+  const std::string mode = param.GetStringDef("Mode", "");
+  printf("# Mode = %s\n", mode.c_str());
+  try {
+    if (mode == "Benchmark") run_benchmark(param);
+    else if (mode == "Langevin") run_langevin(param);
+    else {
+      printf("Mode %s is not found.\n", mode.c_str());
+      return 1;
+    }
+  } catch (const std::exception &e) {
+    printf("# Error: %s\n", e.what());
+    return 2;
+  }
+  return 0;
+}

@@ -1,0 +1,83 @@
+"""The C++ host front-end (mdacp_gb300/host): builds, parses .cfg like the reference,
+and (GPU) runs MDACP's Benchmark project with results matching the oracle."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from mdacp_gb300 import build
+from mdacp_gb300.config import Parameter, SimulationInfo
+
+
+@pytest.fixture(scope="module")
+def host_bin():
+    try:
+        build.build()
+        return build.build_host()
+    except RuntimeError as e:
+        pytest.skip("toolchain unavailable: %s" % e)
+
+
+def _cfg(tmp_path, text):
+    p = tmp_path / "in.cfg"
+    p.write_text(text)
+    return str(p)
+
+
+def test_print_config_matches_python_semantics(host_bin, tmp_path):
+    text = ("Mode=Benchmark\nSystemSize=16\nSystemSizeZ=18.5\nTimeStep=0.002\nTimeStep=9\nDensity=0.5\n"
+            "ControlTemperature=Yes\nHeatbathType=Langevin\nCutoffLength=2.5\nBufferLength=0.5\nPrecision=mixed\n"
+            "#AimedTemperature=3\nHeatbathGamma=0.7x\n")
+    out = subprocess.run([host_bin, "--print-config", _cfg(tmp_path, text)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+    kv = dict(line.split(" ", 1) for line in out.stdout.strip().splitlines())
+    si = SimulationInfo(Parameter(text))
+    assert [float(x) for x in kv["L"].split()] == si.L
+    assert float(kv["TimeStep"]) == si.time_step == 0.002
+    assert float(kv["AimedTemperature"]) == si.aimed_temperature == 1.0
+    assert float(kv["HeatbathGamma"]) == si.heatbath_gamma == 0.7
+    assert kv["ControlTemperature"] == "1" and kv["HeatbathType"] == "1" and kv["Precision"] == "1"
+    assert float(kv["CutoffLength"]) == 2.5 and float(kv["BufferLength"]) == 0.5
+    assert int(kv["lattice"]) == 4 * 8 * 8 * 9
+
+
+def test_bad_heatbath_rejected(host_bin, tmp_path):
+    out = subprocess.run([host_bin, "--print-config", _cfg(tmp_path, "HeatbathType=Foo\n")], capture_output=True,
+                         text=True)
+    assert out.returncode == 2 and "Unknown Heatbath" in out.stdout
+
+
+@pytest.mark.gpu
+def test_benchmark_project_matches_oracle(host_bin, tmp_path):
+    from oracle import port
+    init = str(tmp_path / "init.bin")
+    text = ("Mode=Benchmark\nSystemSize=16\nDensity=0.5\nInitialVelocity=1.7320508\nThermalizeLoop=0\n"
+            "TotalLoop=200\nObserveLoop=50\nTimeStep=0.001\nCutoffLength=2.5\nBufferLength=0.5\n"
+            "InitialStateFile=%s\n" % init)
+    out = subprocess.run([host_bin, _cfg(tmp_path, text)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    rows = np.array([[float(x) for x in l.split()[:4]] for l in out.stdout.splitlines() if l.endswith("#observe")])
+    assert re.search(r"# N = 2048 .* \[MUPS\]", out.stdout)
+    raw = np.fromfile(init, dtype="<f8", offset=8).reshape(-1, 6)
+    s = port.System(raw[:, :3], raw[:, 3:], 16.0, rc=2.5, margin=0.5, dt=0.001)
+    s.make_pairlist()
+    ref, done = [], 0
+    for c in (1, 51, 101, 151):
+        s.calculate(c - done)
+        done = c
+        T, P, E = s.observe()[:3]
+        ref.append([c * 0.001, T, P, E])
+    np.testing.assert_allclose(rows, np.array(ref), rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_langevin_project_runs(host_bin, tmp_path):
+    text = ("Mode=Langevin\nSystemSize=16\nDensity=0.5\nInitialVelocity=1.8\nTimeStep=0.005\nTotalLoop=2000\n"
+            "ObserveLoop=100\nAimedTemperature=0.9\nHeatbathType=Langevin\nHeatbathGamma=1.0\nSeed=12345\n"
+            "CutoffLength=2.5\nBufferLength=0.5\n")
+    out = subprocess.run([host_bin, _cfg(tmp_path, text)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    T = np.array([float(l.split()[1]) for l in out.stdout.splitlines() if l and l[0].isdigit()])
+    assert len(T) == 20 and abs(T[10:].mean() - 0.9) < 0.08
