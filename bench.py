@@ -234,6 +234,7 @@ def run_mine(args):
         e1 = m.observe()[2]
         res[prec] = {"ms": ms, "launches": st["kernel_launches"] - launches0, "rebuilds": st["rebuilds"],
                      "pairs_per_atom": st["listed_pairs"] / n, "drift": (e1 - e0) / (K * DT),
+                     "inner_pairs_per_atom": st["inner_pairs"] / n, "prunes": st["prunes"],
                      "handle": m, "stats": st}
     # force error of the mixed form against FP64 at the same (warmed-up) state
     mf, md = res["mixed"]["handle"], res["fp64"]["handle"]
@@ -247,9 +248,12 @@ def run_mine(args):
     kprof = max(50, min(K, 500))
     mf.make_pairlist()
     mf.calculate(W)
-    stp = mf.stats()
+    s0 = mf.stats()
     kernel_ms = mf.calculate_profiled(kprof) / kprof
-    ppa = stp["listed_pairs"] / n
+    s1 = mf.stats()
+    # pairs the kernel walks: the inner list (mean over the prunes of the pass
+    # is not exposed; the inner list at the end of the pass is used)
+    ppa = s1["inner_pairs"] / n
     alg_bytes = n * (ppa * 20.0 + 72.0)
     peak, peak_kind = peaks()
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
@@ -257,7 +261,8 @@ def run_mine(args):
     roof = {"kernel": "k_step<NVE,mixed>", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": (tpa * n) if tpa else None, "algorithmic_bytes": alg_bytes,
-            "launch_ms": kernel_ms, "pairs_per_atom": ppa}
+            "launch_ms": kernel_ms, "pairs_per_atom": ppa, "listed_pairs_per_atom": s1["listed_pairs"] / n,
+            "prunes_in_pass": s1["prunes"] - s0["prunes"], "rebuilds_in_pass": s1["rebuilds"] - s0["rebuilds"]}
     for prec in ("mixed", "fp64"):
         res[prec]["handle"].close()
     # end to end through the C ABI with host buffers
@@ -298,7 +303,8 @@ def run_mine(args):
                          "energy_drift_per_atom_per_tau": fp64["drift"], "rebuilds": fp64["rebuilds"]},
                 "mixed_over_fp64": value / v64,
                 "mixed": {"rms_rel_force_err_vs_fp64": rms_err, "energy_drift_per_atom_per_tau": mixed["drift"],
-                          "rebuilds": mixed["rebuilds"], "pairs_per_atom": mixed["pairs_per_atom"]},
+                          "rebuilds": mixed["rebuilds"], "pairs_per_atom": mixed["pairs_per_atom"],
+                          "inner_pairs_per_atom": mixed["inner_pairs_per_atom"], "prunes": mixed["prunes"]},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 32 / K,
                         "d2h_bytes_per_step": (2 * n * 32 + 24 * nobs) / K},
                 "gpu_launches": mixed["launches"],

@@ -58,6 +58,10 @@ typedef struct mdg_params {
   int32_t device;          /* CUDA device ordinal */
   int32_t use_graphs;      /* 1 = replay steps as CUDA graphs */
   int32_t reserved;
+  double prune_buffer;     /* inner-list buffer: the force kernels walk the pairs within
+                              cutoff + prune_buffer, re-selected from the list whenever a
+                              particle moved prune_buffer/2 (default -1 = automatic,
+                              min(100 dt, margin); 0 keeps every listed pair) */
 } mdg_params;
 
 typedef struct mdg_stats {
@@ -71,6 +75,8 @@ typedef struct mdg_stats {
   double zeta;             /* Nose-Hoover friction (Variables::Zeta) */
   double elapsed_ms;       /* device time of the last mdg_calculate call */
   int64_t kernel_launches; /* kernels this handle has enqueued (graph replays count each node) */
+  int64_t inner_pairs;     /* directed pairs in the inner list at the last prune */
+  int64_t prunes;          /* inner-list selections since the last mdg_set_state */
 } mdg_stats;
 
 typedef struct mdg_handle mdg_handle;
@@ -127,6 +133,96 @@ int mdg_get_stats(mdg_handle *h, mdg_stats *s);
  * buffers, [n][4] doubles, caller's order). */
 int mdg_set_state_device(mdg_handle *h, const double *q4_dev, const double *p4_dev, int32_t n);
 int mdg_get_state_device(mdg_handle *h, double *q4_dev, double *p4_dev);
+
+/* ------------------------------------------------------------------------
+ * Batched replicas (no reference counterpart; a pattern on top of the
+ * drop-in): nbox independent periodic boxes of uneven size and density, each
+ * an NVE drift-kick-drift run with its own cell list and Verlet list, all
+ * advanced by one persistent kernel per step (replayed from a CUDA graph).
+ * Particles are concatenated box after box, [sum n][4] doubles; every box is
+ * returned in the order it was given. */
+typedef struct mdg_batch_params {
+  int32_t precision;      /* mdg_precision */
+  int32_t device;
+  double cutoff;          /* rc */
+  double margin;          /* list margin */
+  double dt;
+  int32_t list_capacity;  /* neighbour slots per particle; 0 = from the densest box */
+  int32_t use_graphs;
+} mdg_batch_params;
+
+typedef struct mdg_batch_stats {
+  int64_t steps;              /* steps every box has advanced */
+  int64_t rebuilds;           /* list builds summed over boxes */
+  int64_t particles;
+  int32_t boxes;
+  int32_t list_capacity;
+  int32_t threads;            /* CTA size of the persistent kernel */
+  int32_t lanes_per_particle; /* lanes sharing one particle's row */
+  int32_t ctas_per_sm;
+  int32_t reserved;
+  double elapsed_ms;          /* device time of the last mdg_batch_calculate */
+  int64_t kernel_launches;
+} mdg_batch_stats;
+
+typedef struct mdg_batch mdg_batch;
+
+void mdg_batch_params_default(mdg_batch_params *p);
+/* box_lengths: nbox x 3 box sides; each side must exceed 2 (cutoff + margin). */
+int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_per_box, const double *box_lengths,
+                     mdg_batch **out);
+int mdg_batch_destroy(mdg_batch *b);
+const char *mdg_batch_last_error(const mdg_batch *b);
+int mdg_batch_set_state(mdg_batch *b, const double *q4, const double *p4);
+int mdg_batch_get_state(mdg_batch *b, double *q4, double *p4);
+int mdg_batch_calculate(mdg_batch *b, int32_t nsteps);
+/* out: nbox x 3 observer sums (as mdg_observe) at the current positions. */
+int mdg_batch_observe(mdg_batch *b, double *out);
+/* Autotuner: times trial_steps for every (threads per CTA, lanes per particle,
+ * CTAs per SM) shape from a copy of the current state, keeps the fastest, and
+ * restores the state. */
+int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t *lanes_per_particle,
+                   int32_t *ctas_per_sm);
+int mdg_batch_set_shape(mdg_batch *b, int32_t threads, int32_t lanes_per_particle, int32_t ctas_per_sm);
+int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s);
+
+/* ------------------------------------------------------------------------
+ * Adjoint (no reference counterpart; a pattern on top of the drop-in):
+ * gradients of a trajectory-averaged observable of an NVE drift-kick-drift
+ * run with respect to epsilon, sigma and the initial state, by the discrete
+ * adjoint (reverse steps with a Hessian-vector product over the same pair
+ * list), checkpointing every checkpoint_every steps and recomputing each
+ * segment in the backward pass.  V(r) = epsilon phi(r / sigma) with the
+ * reference's smoothly truncated phi; the cut-off is cutoff * sigma.  The pair
+ * list (all pairs within cutoff * sigma + margin at the initial positions) is
+ * kept for the whole horizon; a particle moving more than margin / 2 is an
+ * error (MDG_ERR_STATE).  FP64 throughout. */
+enum mdg_objective { MDG_OBJ_POTENTIAL = 0, MDG_OBJ_PRESSURE = 1 };
+
+typedef struct mdg_adjoint_params {
+  double box[3];
+  double cutoff;           /* in units of sigma */
+  double margin;           /* absolute list margin for the whole horizon */
+  double dt;
+  double epsilon, sigma;
+  int32_t steps;           /* horizon */
+  int32_t checkpoint_every;
+  int32_t objective;       /* MDG_OBJ_POTENTIAL: mean of U/N over steps 1..steps;
+                              MDG_OBJ_PRESSURE: mean of (2 KE - sum f r^2) / (3 V) */
+  int32_t device;
+} mdg_adjoint_params;
+
+typedef struct mdg_adjoint mdg_adjoint;
+
+void mdg_adjoint_params_default(mdg_adjoint_params *p);
+int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out);
+int mdg_adjoint_destroy(mdg_adjoint *a);
+const char *mdg_adjoint_last_error(const mdg_adjoint *a);
+/* Runs the horizon from host state q4, p4 ([n][4]); *J receives the objective. */
+int mdg_adjoint_forward(mdg_adjoint *a, const double *q4, const double *p4, double *J);
+/* Gradients of the last forward's objective: dJ/dq0 and dJ/dp0 as host [n][4]
+ * (either may be NULL), dJ/depsilon, dJ/dsigma. */
+int mdg_adjoint_backward(mdg_adjoint *a, double *dq0, double *dp0, double *depsilon, double *dsigma);
 
 /* Observers without any allocation (this entry point has no counterpart in the
  * reference).  For callers that cannot call cudaMalloc -- applications whose

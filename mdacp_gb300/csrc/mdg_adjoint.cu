@@ -1,0 +1,549 @@
+// Adjoint of an NVE trajectory: gradients of a trajectory-averaged observable
+// with respect to the LJ parameters (epsilon, sigma) and the initial state.
+//
+// No reference counterpart (a pattern on top of the drop-in).  The potential
+// is the reference's smoothly truncated LJ (variables.cc:16-28) written with
+// explicit parameters, V(r) = eps * phi(r / sigma),
+//   phi(x) = 4 (x^-12 - x^-6 + C2 x^2 + C0) for x <= xc,
+// the cut-off scaling with sigma (xc = cutoff in sigma units).  The step is
+// the reference's drift-kick-drift (mdmanager.cc:151-157):
+//   qh = q + p dt/2;  p' = p + F(qh) dt;  q' = qh + p' dt/2.
+// Objectives J = (1/Ns) sum_{n=1..Ns} j(q_n, p_n) with j = U/N (mean
+// potential energy per particle, MDManager::PotentialEnergy) or
+// j = P = (2 KE - G) / (3 V), G = sum_pairs f(r) r^2 (MDManager::Pressure).
+//
+// Discrete adjoint (exact gradient of the discrete trajectory): walking the
+// steps backwards, with a_q, a_p the adjoints of (q_n, p_n):
+//   a_p += dt/2 a_q;  a_qh = a_q - dt H(qh) a_p;  g_theta += dt a_p . dF/dtheta(qh);
+//   a_q = a_qh;  a_p += dt/2 a_qh;  then the objective terms of the earlier state.
+// H v is the Hessian-vector product over the same pair list.  States are
+// checkpointed every K steps in the forward pass; the backward pass recomputes
+// each segment from its checkpoint (storing its K half-step positions and
+// states) and then reverses it.  The pair list (every pair within
+// cutoff*sigma + margin at q0, minimum image) is fixed over the horizon; the
+// forward pass verifies that no particle moves more than margin/2.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mdg_internal.cuh"
+
+namespace mdg {
+namespace adj {
+
+constexpr int kT = 128;
+
+struct P {
+  double L[3];
+  double eps, sig, dt, dt2;
+  double xc2;      // (cutoff in sigma units)^2
+  double c0, c2;   // correction constants of phi
+  double sl2;      // list radius^2 (absolute)
+  double half_margin2;
+  double volume;
+  int n, cap, objective, pad;
+};
+
+struct D {
+  double4_32a *q, *p, *qh, *F, *aq, *ap, *aqh, *tmp, *q0;
+  double4_32a *ckq, *ckp;    // checkpoints
+  double4_32a *segq, *segp, *segqh;  // recomputed segment
+  int *nbr, *cnt;            // fixed list, row-major [n][cap]
+  double *part;              // block partials
+  double *acc;               // running sums: J, g_eps, g_sig
+  int *flag;
+};
+
+__device__ __forceinline__ void min_image(const P &c, double &dx, double &dy, double &dz) {
+  dx -= c.L[0] * rint(dx / c.L[0]);
+  dy -= c.L[1] * rint(dy / c.L[1]);
+  dz -= c.L[2] * rint(dz / c.L[2]);
+}
+
+// Per pair at distance r (d = q_j - q_i): the reduced quantities.
+struct PairTerms {
+  double f;      // V'(r)/r: force on i is f d
+  double fpr;    // f'(r)/r
+  double phi;    // V(r)
+  double fs;     // d f / d sigma
+  double dphis;  // d V / d sigma
+  double g;      // f r^2
+  double gpr;    // g'(r)/r
+  double gs;     // d g / d sigma
+};
+
+__device__ __forceinline__ bool pair_terms(const P &c, double r2, PairTerms &t) {
+  const double s2 = c.sig * c.sig;
+  const double x2 = r2 / s2;
+  if (x2 > c.xc2) return false;
+  const double ix2 = 1.0 / x2, ix6 = ix2 * ix2 * ix2, ix8 = ix6 * ix2, ix12 = ix6 * ix6, ix14 = ix12 * ix2;
+  const double ix10 = ix8 * ix2, ix16 = ix14 * ix2;
+  // psi(x) = phi'(x)/x, chi(x) = x^2 psi(x)
+  const double psi = -48.0 * ix14 + 24.0 * ix8 + 8.0 * c.c2;
+  const double dpsi_x = 672.0 * ix16 - 192.0 * ix10;      // psi'(x)/x
+  const double phi = 4.0 * (ix12 - ix6 + c.c2 * x2 + c.c0);
+  const double xdphi = 4.0 * (-12.0 * ix12 + 6.0 * ix6 + 2.0 * c.c2 * x2);  // x phi'(x)
+  const double chi = x2 * psi;                               // -48 x^-12 + 24 x^-6 + 8 C2 x^2
+  const double xdchi = 576.0 * ix12 - 144.0 * ix6 + 16.0 * c.c2 * x2;  // x chi'(x)
+  const double e = c.eps, s = c.sig;
+  t.f = e / s2 * psi;
+  t.fpr = e / (s2 * s2) * dpsi_x;
+  t.phi = e * phi;
+  t.fs = -e / (s2 * s) * (2.0 * psi + x2 * dpsi_x);
+  t.dphis = -e / s * xdphi;
+  t.g = e * chi;
+  t.gpr = e / s2 * (xdchi / x2);
+  t.gs = -e / s * xdchi;
+  return true;
+}
+
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+  __syncthreads();
+  return t;
+}
+
+__global__ void k_build(P c, D d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  const double4_32a qi = d.q[i];
+  int m = 0;
+  for (int j = 0; j < c.n; j++) {
+    if (j == i) continue;
+    const double4_32a qj = d.q[j];
+    double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+    min_image(c, dx, dy, dz);
+    if (dx * dx + dy * dy + dz * dz <= c.sl2) {
+      if (m < c.cap) d.nbr[(size_t)i * c.cap + m] = j;
+      m++;
+    }
+  }
+  d.cnt[i] = m < c.cap ? m : c.cap;
+  if (m > c.cap) atomicMax(d.flag, m);
+}
+
+__global__ void k_force(P c, D d, const double4_32a *q, double4_32a *F) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  const double4_32a qi = q[i];
+  double fx = 0, fy = 0, fz = 0;
+  for (int k = 0; k < d.cnt[i]; k++) {
+    const double4_32a qj = q[d.nbr[(size_t)i * c.cap + k]];
+    double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+    min_image(c, dx, dy, dz);
+    PairTerms t;
+    if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
+    fx += t.f * dx;
+    fy += t.f * dy;
+    fz += t.f * dz;
+  }
+  F[i] = make_double4_32a(fx, fy, fz, 0.0);
+}
+
+// qh = q + p dt/2 (also records the displacement check against q0)
+__global__ void k_drift(P c, D d, const double4_32a *q, const double4_32a *p, double4_32a *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  double4_32a a = q[i];
+  const double4_32a b = p[i];
+  a.x += b.x * c.dt2;
+  a.y += b.y * c.dt2;
+  a.z += b.z * c.dt2;
+  out[i] = a;
+  const double4_32a z = d.q0[i];
+  const double ux = a.x - z.x, uy = a.y - z.y, uz = a.z - z.z;
+  if (ux * ux + uy * uy + uz * uz > c.half_margin2) atomicMax(d.flag + 1, 1);
+}
+
+// p += F dt; q = qh + p dt/2
+__global__ void k_kick_drift(P c, const double4_32a *qh, const double4_32a *F, double4_32a *q, double4_32a *p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  double4_32a b = p[i];
+  const double4_32a f = F[i];
+  b.x += f.x * c.dt;
+  b.y += f.y * c.dt;
+  b.z += f.z * c.dt;
+  p[i] = b;
+  double4_32a a = qh[i];
+  a.x += b.x * c.dt2;
+  a.y += b.y * c.dt2;
+  a.z += b.z * c.dt2;
+  q[i] = a;
+}
+
+// Objective j at (q, p) into partials (value, d/deps, d/dsigma); with grad,
+// also adds w * dj/dq to aq and w * dj/dp to ap (w = 1/Ns).
+__global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p, int grad, double w) {
+  __shared__ double sh[32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double val = 0, ge = 0, gs = 0;
+  if (i < c.n) {
+    const double4_32a qi = q[i], pi = p[i];
+    double gx = 0, gy = 0, gz = 0, u = 0, us = 0, G = 0, Gs = 0;
+    for (int k = 0; k < d.cnt[i]; k++) {
+      const double4_32a qj = q[d.nbr[(size_t)i * c.cap + k]];
+      double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+      min_image(c, dx, dy, dz);
+      PairTerms t;
+      if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
+      if (c.objective == 0) {
+        u += 0.5 * t.phi;
+        us += 0.5 * t.dphis;
+        gx -= t.f * dx;  // dU/dq_i = -F_i
+        gy -= t.f * dy;
+        gz -= t.f * dz;
+      } else {
+        G += 0.5 * t.g;
+        Gs += 0.5 * t.gs;
+        gx += t.gpr * dx;  // dG/dq_i = -sum g'(r) d/r;  dP/dq_i = -(1/3V) dG/dq_i
+        gy += t.gpr * dy;
+        gz += t.gpr * dz;
+      }
+    }
+    const double ke = 0.5 * (pi.x * pi.x + pi.y * pi.y + pi.z * pi.z);
+    if (c.objective == 0) {
+      const double inv_n = 1.0 / (double)c.n;
+      val = u * inv_n;
+      ge = u / c.eps * inv_n;
+      gs = us * inv_n;
+      if (grad) {
+        double4_32a a = d.aq[i];
+        a.x += w * gx * inv_n;
+        a.y += w * gy * inv_n;
+        a.z += w * gz * inv_n;
+        d.aq[i] = a;
+      }
+    } else {
+      const double inv3v = 1.0 / (3.0 * c.volume);
+      val = (2.0 * ke - G) * inv3v;
+      ge = -G / c.eps * inv3v;
+      gs = -Gs * inv3v;
+      if (grad) {
+        double4_32a a = d.aq[i], b = d.ap[i];
+        a.x += w * gx * inv3v;
+        a.y += w * gy * inv3v;
+        a.z += w * gz * inv3v;
+        b.x += w * 2.0 * pi.x * inv3v;
+        b.y += w * 2.0 * pi.y * inv3v;
+        b.z += w * 2.0 * pi.z * inv3v;
+        d.aq[i] = a;
+        d.ap[i] = b;
+      }
+    }
+  }
+  const double a = block_sum(val, sh), b = block_sum(ge, sh), e = block_sum(gs, sh);
+  if (threadIdx.x == 0) {
+    d.part[3 * blockIdx.x + 0] = a;
+    d.part[3 * blockIdx.x + 1] = b;
+    d.part[3 * blockIdx.x + 2] = e;
+  }
+}
+
+// acc[0..2] += w * (sum of partials), fixed order.
+__global__ void k_accumulate(D d, int nparts, double w) {
+  __shared__ double sh[32];
+  double a = 0, b = 0, e = 0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+    a += d.part[3 * k];
+    b += d.part[3 * k + 1];
+    e += d.part[3 * k + 2];
+  }
+  const double ta = block_sum(a, sh), tb = block_sum(b, sh), te = block_sum(e, sh);
+  if (threadIdx.x == 0) {
+    d.acc[0] += w * ta;
+    d.acc[1] += w * tb;
+    d.acc[2] += w * te;
+  }
+}
+
+// Reverse of one step at half-step positions qh.  In: aq, ap adjoints of
+// (q_{n}, p_{n}).  Out: aq, ap adjoints of (q_{n-1}, p_{n-1}); parameter terms
+// dt * ap . dF/dtheta into partials (slots 1, 2).
+__global__ void k_reverse(P c, D d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < c.n) {
+    double4_32a a = d.aq[i], b = d.ap[i];
+    // drift q_n = qh + dt/2 p_n : a_p += dt/2 a_q  (done per particle, a_q unchanged)
+    b.x += c.dt2 * a.x;
+    b.y += c.dt2 * a.y;
+    b.z += c.dt2 * a.z;
+    d.tmp[i] = b;  // adjoint of p after the kick, needed by the neighbours' H v
+    d.aqh[i] = a;
+  }
+}
+
+__global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
+  __shared__ double sh[32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double te = 0, ts = 0;
+  if (i < c.n) {
+    const double4_32a qi = qh[i], vi = d.tmp[i];
+    double hx = 0, hy = 0, hz = 0, fx = 0, fy = 0, fz = 0, sx = 0, sy = 0, sz = 0;
+    for (int k = 0; k < d.cnt[i]; k++) {
+      const int j = d.nbr[(size_t)i * c.cap + k];
+      const double4_32a qj = qh[j], vj = d.tmp[j];
+      double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+      min_image(c, dx, dy, dz);
+      PairTerms t;
+      if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
+      const double wx = vi.x - vj.x, wy = vi.y - vj.y, wz = vi.z - vj.z;
+      const double dw = dx * wx + dy * wy + dz * wz;
+      // (H v)_i = sum_j f (v_i - v_j) + (f'/r) d (d . (v_i - v_j))
+      hx += t.f * wx + t.fpr * dx * dw;
+      hy += t.f * wy + t.fpr * dy * dw;
+      hz += t.f * wz + t.fpr * dz * dw;
+      fx += t.f * dx;
+      fy += t.f * dy;
+      fz += t.f * dz;
+      sx += t.fs * dx;
+      sy += t.fs * dy;
+      sz += t.fs * dz;
+    }
+    const double4_32a b = d.tmp[i];
+    // parameter terms: dt * a_p . dF_i/deps (= F_i/eps), dt * a_p . dF_i/dsigma
+    te = c.dt * (b.x * fx + b.y * fy + b.z * fz) / c.eps;
+    ts = c.dt * (b.x * sx + b.y * sy + b.z * sz);
+    // kick: a_qh = a_q - dt H a_p ; then drift qh = q + dt/2 p : a_p += dt/2 a_qh
+    double4_32a a = d.aqh[i];
+    a.x -= c.dt * hx;
+    a.y -= c.dt * hy;
+    a.z -= c.dt * hz;
+    double4_32a pb = b;
+    pb.x += c.dt2 * a.x;
+    pb.y += c.dt2 * a.y;
+    pb.z += c.dt2 * a.z;
+    d.aq[i] = a;
+    d.ap[i] = pb;
+  }
+  const double A = block_sum(0.0, sh), B = block_sum(te, sh), E = block_sum(ts, sh);
+  if (threadIdx.x == 0) {
+    d.part[3 * blockIdx.x + 0] = A;
+    d.part[3 * blockIdx.x + 1] = B;
+    d.part[3 * blockIdx.x + 2] = E;
+  }
+}
+
+}  // namespace adj
+}  // namespace mdg
+
+using namespace mdg::adj;
+
+struct mdg_adjoint {
+  mdg_adjoint_params prm;
+  std::string err;
+  P c;
+  D d;
+  cudaStream_t s = nullptr;
+  int grid = 1;
+  int nck = 0;
+  bool forward_done = false;
+};
+
+namespace {
+
+int afail(mdg_adjoint *a, int code, const std::string &m) {
+  if (a) a->err = m;
+  return code;
+}
+
+#define MDG_ACK(call)                                                                                    \
+  do {                                                                                                   \
+    cudaError_t e_ = (call);                                                                             \
+    if (e_ != cudaSuccess) return afail(a, MDG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+cudaError_t aalloc(T **p, size_t n) {
+  *p = nullptr;
+  return cudaMalloc((void **)p, (n ? n : 1) * sizeof(T));
+}
+
+// One forward step from (q, p): qh_out, then (q, p) updated in place.
+void fwd_step(mdg_adjoint *a, double4_32a *q, double4_32a *p, double4_32a *qh) {
+  k_drift<<<a->grid, kT, 0, a->s>>>(a->c, a->d, q, p, qh);
+  k_force<<<a->grid, kT, 0, a->s>>>(a->c, a->d, qh, a->d.F);
+  k_kick_drift<<<a->grid, kT, 0, a->s>>>(a->c, qh, a->d.F, q, p);
+}
+
+}  // namespace
+
+extern "C" {
+
+void mdg_adjoint_params_default(mdg_adjoint_params *p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->cutoff = 2.5;
+  p->margin = 2.0;
+  p->dt = 0.002;
+  p->epsilon = 1.0;
+  p->sigma = 1.0;
+  p->steps = 200;
+  p->checkpoint_every = 20;
+  p->objective = MDG_OBJ_POTENTIAL;
+}
+
+int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out) {
+  if (!p || !out || n <= 1 || p->steps <= 0 || p->checkpoint_every <= 0 || !(p->dt > 0) || !(p->epsilon > 0) ||
+      !(p->sigma > 0) || (p->objective != MDG_OBJ_POTENTIAL && p->objective != MDG_OBJ_PRESSURE))
+    return MDG_ERR_INVALID;
+  *out = nullptr;
+  const double sl = p->cutoff * p->sigma + p->margin;
+  for (int k = 0; k < 3; k++)
+    if (!(p->box[k] > 2.0 * sl)) return MDG_ERR_INVALID;
+  mdg_adjoint *a = new mdg_adjoint();
+  a->prm = *p;
+  memset(&a->d, 0, sizeof(a->d));
+  P &c = a->c;
+  for (int k = 0; k < 3; k++) c.L[k] = p->box[k];
+  c.eps = p->epsilon;
+  c.sig = p->sigma;
+  c.dt = p->dt;
+  c.dt2 = 0.5 * p->dt;
+  c.xc2 = p->cutoff * p->cutoff;
+  const double s2 = 1.0 / c.xc2, s6 = s2 * s2 * s2, s8 = s6 * s2, s12 = s6 * s6, s14 = s12 * s2;
+  c.c2 = 6.0 * s14 - 3.0 * s8;  // variables.cc:16-28 in sigma units
+  c.c0 = -s12 + s6 - c.c2 / s2;
+  c.sl2 = sl * sl;
+  c.half_margin2 = 0.25 * p->margin * p->margin;
+  c.volume = p->box[0] * p->box[1] * p->box[2];
+  c.n = n;
+  c.objective = p->objective;
+  const double rho = n / c.volume;
+  c.cap = ((int)(rho * 4.18879020478639 * sl * sl * sl * 1.5 + 32) + 7) & ~7;
+  a->grid = (n + kT - 1) / kT;
+  a->nck = p->steps / p->checkpoint_every + 1;
+  const size_t N = (size_t)n, K = (size_t)p->checkpoint_every;
+  D &d = a->d;
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->s, cudaStreamNonBlocking);
+  double4_32a **vecs[] = {&d.q, &d.p, &d.qh, &d.F, &d.aq, &d.ap, &d.aqh, &d.tmp, &d.q0};
+  for (auto v : vecs)
+    if (e == cudaSuccess) e = aalloc(v, N);
+  if (e == cudaSuccess) e = aalloc(&d.ckq, N * a->nck);
+  if (e == cudaSuccess) e = aalloc(&d.ckp, N * a->nck);
+  if (e == cudaSuccess) e = aalloc(&d.segq, N * (K + 1));
+  if (e == cudaSuccess) e = aalloc(&d.segp, N * (K + 1));
+  if (e == cudaSuccess) e = aalloc(&d.segqh, N * (K + 1));
+  if (e == cudaSuccess) e = aalloc(&d.nbr, N * (size_t)c.cap);
+  if (e == cudaSuccess) e = aalloc(&d.cnt, N);
+  if (e == cudaSuccess) e = aalloc(&d.part, 3 * (size_t)a->grid);
+  if (e == cudaSuccess) e = aalloc(&d.acc, 3);
+  if (e == cudaSuccess) e = aalloc(&d.flag, 2);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "mdg_adjoint_create: %s\n", cudaGetErrorString(e));
+    mdg_adjoint_destroy(a);
+    return MDG_ERR_CUDA;
+  }
+  *out = a;
+  return MDG_OK;
+}
+
+int mdg_adjoint_destroy(mdg_adjoint *a) {
+  if (!a) return MDG_OK;
+  cudaSetDevice(a->prm.device);
+  if (a->s) cudaStreamSynchronize(a->s);
+  D &d = a->d;
+  void *ptrs[] = {d.q, d.p, d.qh, d.F, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
+                  d.nbr, d.cnt, d.part, d.acc, d.flag};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (a->s) cudaStreamDestroy(a->s);
+  delete a;
+  return MDG_OK;
+}
+
+const char *mdg_adjoint_last_error(const mdg_adjoint *a) { return a ? a->err.c_str() : "null adjoint"; }
+
+int mdg_adjoint_forward(mdg_adjoint *a, const double *q4, const double *p4, double *J) {
+  if (!a || !q4 || !p4 || !J) return MDG_ERR_INVALID;
+  MDG_ACK(cudaSetDevice(a->prm.device));
+  const size_t N = (size_t)a->c.n, bytes = N * 32;
+  D &d = a->d;
+  MDG_ACK(cudaMemcpyAsync(d.q, q4, bytes, cudaMemcpyHostToDevice, a->s));
+  MDG_ACK(cudaMemcpyAsync(d.p, p4, bytes, cudaMemcpyHostToDevice, a->s));
+  MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+  MDG_ACK(cudaMemsetAsync(d.flag, 0, 2 * sizeof(int), a->s));
+  MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
+  k_build<<<a->grid, kT, 0, a->s>>>(a->c, d);
+  int flag[2] = {0, 0};
+  MDG_ACK(cudaMemcpyAsync(flag, d.flag, sizeof flag, cudaMemcpyDeviceToHost, a->s));
+  MDG_ACK(cudaStreamSynchronize(a->s));
+  if (flag[0]) return afail(a, MDG_ERR_CAPACITY, "adjoint pair list capacity exceeded");
+  const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
+  const double w = 1.0 / Ns;
+  MDG_ACK(cudaMemcpyAsync(d.ckq, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+  MDG_ACK(cudaMemcpyAsync(d.ckp, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
+  for (int n = 1; n <= Ns; n++) {
+    fwd_step(a, d.q, d.p, d.qh);
+    k_objective<<<a->grid, kT, 0, a->s>>>(a->c, d, d.q, d.p, 0, w);
+    k_accumulate<<<1, 1024, 0, a->s>>>(d, a->grid, w);
+    if (n % K == 0) {
+      MDG_ACK(cudaMemcpyAsync(d.ckq + N * (n / K), d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+      MDG_ACK(cudaMemcpyAsync(d.ckp + N * (n / K), d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
+    }
+  }
+  double acc[3];
+  MDG_ACK(cudaMemcpyAsync(acc, d.acc, sizeof acc, cudaMemcpyDeviceToHost, a->s));
+  MDG_ACK(cudaMemcpyAsync(flag, d.flag, sizeof flag, cudaMemcpyDeviceToHost, a->s));
+  MDG_ACK(cudaStreamSynchronize(a->s));
+  if (flag[1]) return afail(a, MDG_ERR_STATE, "a particle moved more than margin/2 over the horizon; raise margin");
+  *J = acc[0];
+  a->forward_done = true;
+  return MDG_OK;
+}
+
+int mdg_adjoint_backward(mdg_adjoint *a, double *dq0, double *dp0, double *deps, double *dsigma) {
+  if (!a) return MDG_ERR_INVALID;
+  if (!a->forward_done) return afail(a, MDG_ERR_NOT_READY, "run mdg_adjoint_forward first");
+  MDG_ACK(cudaSetDevice(a->prm.device));
+  const size_t N = (size_t)a->c.n, bytes = N * 32;
+  D &d = a->d;
+  const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
+  const double w = 1.0 / Ns;
+  MDG_ACK(cudaMemsetAsync(d.aq, 0, bytes, a->s));
+  MDG_ACK(cudaMemsetAsync(d.ap, 0, bytes, a->s));
+  MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
+  for (int seg_end = Ns; seg_end > 0;) {
+    const int seg_start = ((seg_end - 1) / K) * K;
+    const int len = seg_end - seg_start;
+    // recompute the segment from its checkpoint: states 0..len, half steps 1..len
+    MDG_ACK(cudaMemcpyAsync(d.segq, d.ckq + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
+    MDG_ACK(cudaMemcpyAsync(d.segp, d.ckp + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
+    for (int k = 1; k <= len; k++) {
+      MDG_ACK(cudaMemcpyAsync(d.segq + N * k, d.segq + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
+      MDG_ACK(cudaMemcpyAsync(d.segp + N * k, d.segp + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
+      fwd_step(a, d.segq + N * k, d.segp + N * k, d.segqh + N * k);
+    }
+    for (int k = len; k >= 1; k--) {
+      // objective terms of state (seg_start + k)
+      k_objective<<<a->grid, kT, 0, a->s>>>(a->c, d, d.segq + N * k, d.segp + N * k, 1, w);
+      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->grid, w);
+      // reverse the step that produced it
+      k_reverse<<<a->grid, kT, 0, a->s>>>(a->c, d);
+      k_reverse_hvp<<<a->grid, kT, 0, a->s>>>(a->c, d, d.segqh + N * k);
+      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->grid, 1.0);
+    }
+    seg_end = seg_start;
+  }
+  double acc[3];
+  MDG_ACK(cudaMemcpyAsync(acc, d.acc, sizeof acc, cudaMemcpyDeviceToHost, a->s));
+  if (dq0) MDG_ACK(cudaMemcpyAsync(dq0, d.aq, bytes, cudaMemcpyDeviceToHost, a->s));
+  if (dp0) MDG_ACK(cudaMemcpyAsync(dp0, d.ap, bytes, cudaMemcpyDeviceToHost, a->s));
+  MDG_ACK(cudaStreamSynchronize(a->s));
+  // acc[1], acc[2]: objective parameter terms (weighted) plus the kick terms
+  if (deps) *deps = acc[1];
+  if (dsigma) *dsigma = acc[2];
+  return MDG_OK;
+}
+
+}  // extern "C"

@@ -78,7 +78,7 @@ void dfree_all(mdg_handle *h) {
   mdg::Dev &d = h->d;
   void *ptrs[] = {d.q_end, d.q_mid[0], d.q_mid[1], d.p, d.q_build, d.t_q, d.t_p, d.qf, d.loc[0], d.loc[1], d.id,
                   d.inv, d.cell, d.t_id, d.t_cell, d.order, d.cell_count, d.cell_fill, d.cell_start, d.block_sums,
-                  d.nl, d.ncount, d.partials, d.flags, d.io4, d.io4b, h->dobs};
+                  d.nl, d.ncount, d.pl, d.pcount, d.loc_p, d.partials, d.flags, d.io4, d.io4b, h->dobs};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   memset(&h->d, 0, sizeof(h->d));
@@ -127,6 +127,16 @@ int setup_geometry(mdg_handle *h) {
   g.dt = p.dt;
   g.dt2 = p.dt * 0.5;
   g.half_margin2 = 0.25 * p.margin * p.margin;
+  // negative: automatic, 100 time steps of travel (0.1 at dt = 0.001) capped by the margin
+  const double buffer = p.prune_buffer < 0.0 ? std::fmin(100.0 * p.dt, p.margin) : p.prune_buffer;
+  if (buffer > 0.0) {
+    const double rb = p.cutoff + buffer;
+    g.prune_thr2 = (float)(rb * rb + 1e-4);  // float r2 of local positions is within ~1e-5
+    g.half_prune2 = (float)(0.25 * buffer * buffer * (1.0 - 1e-4));
+  } else {
+    g.prune_thr2 = 3.0e38f;   // keep every listed pair, select only after a rebuild
+    g.half_prune2 = 3.0e38f;
+  }
   g.gamma = p.gamma;
   g.temperature = p.temperature;
   g.tau = p.tau;
@@ -146,8 +156,10 @@ int estimate_list_cap(const mdg_handle *h, int n) {
 
 int alloc_list(mdg_handle *h, int list_cap) {
   if (h->d.nl) cudaFree(h->d.nl);
-  h->d.nl = nullptr;
+  if (h->d.pl) cudaFree(h->d.pl);
+  h->d.nl = h->d.pl = nullptr;
   MDG_CK(dalloc(&h->d.nl, (size_t)list_cap * (size_t)h->cap));
+  MDG_CK(dalloc(&h->d.pl, (size_t)list_cap * (size_t)h->cap));
   h->g.list_cap = list_cap;
   drop_graphs(h);
   return MDG_OK;
@@ -297,6 +309,7 @@ void mdg_params_default(mdg_params *p) {
   p->tau = 0.1;          // HeatbathTau default
   p->seed = 1;
   p->use_graphs = 1;
+  p->prune_buffer = -1.0;  // automatic
 }
 
 int mdg_create(const mdg_params *p, mdg_handle **out) {
@@ -335,8 +348,10 @@ int mdg_create(const mdg_params *p, mdg_handle **out) {
   if (e == cudaSuccess) e = dalloc(&d.t_q, cap);
   if (e == cudaSuccess) e = dalloc(&d.t_p, cap);
   if (e == cudaSuccess) e = dalloc(&d.qf, cap);
-  if (e == cudaSuccess && p->precision == MDG_MIXED) e = dalloc(&d.loc[0], cap);
-  if (e == cudaSuccess && p->precision == MDG_MIXED) e = dalloc(&d.loc[1], cap);
+  if (e == cudaSuccess) e = dalloc(&d.loc[0], cap);
+  if (e == cudaSuccess) e = dalloc(&d.loc[1], cap);
+  if (e == cudaSuccess) e = dalloc(&d.loc_p, cap);
+  if (e == cudaSuccess) e = dalloc(&d.pcount, cap);
   if (e == cudaSuccess) e = dalloc(&d.id, cap);
   if (e == cudaSuccess) e = dalloc(&d.inv, cap);
   if (e == cudaSuccess) e = dalloc(&d.cell, cap);
@@ -644,6 +659,8 @@ int mdg_get_stats(mdg_handle *h, mdg_stats *s) {
     s->max_neighbours = h->hflags->max_count;
     s->listed_pairs = (int64_t)h->hflags->pairs;
     s->zeta = h->hflags->zeta;
+    s->inner_pairs = (int64_t)h->hflags->inner_pairs;
+    s->prunes = (int64_t)h->hflags->prunes;
   }
   s->list_capacity = h->g.list_cap;
   for (int k = 0; k < 3; k++) s->cells[k] = h->g.nc[k];

@@ -1,2 +1,982 @@
-// Batched replica boxes (filled in with the persistent replica kernel).
+// Batched replicas: many independent periodic LJ boxes of uneven size,
+// density and temperature advanced together, one persistent kernel per step.
+//
+// No reference counterpart (a new pattern on top of the drop-in): each box is
+// what one MDACP run does (NVE drift-kick-drift, cell list + Verlet list with a
+// margin, the same smoothly truncated potential), but a thousand of them share
+// the GPU.  Design:
+//   * the grid is a few CTAs per SM; each CTA owns a fixed list of boxes
+//     assigned longest-first to the least-loaded CTA (host, deterministic);
+//   * a CTA advances each of its boxes by one step: when the box's own
+//     displacement test fired it first rebuilds the box's cell list and pair
+//     list in place (counting sort with the cell counters in shared memory,
+//     stable by particle index, same float-first exact acceptance test as the
+//     single-box path), then runs the fused force/kick/drift over the box;
+//   * lanes-per-particle (1, 2 or 4 lanes share one particle's row and reduce
+//     with shuffles), threads per CTA and CTAs per SM are chosen by the
+//     autotuner (mdg_batch_tune);
+//   * a box whose row overflows stops (its step counter does not advance) while
+//     the others continue; the host regrows the rows and runs catch-up steps
+//     that advance only the boxes behind the goal.  No kernel waits on another.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
 #include "mdg_internal.cuh"
+
+namespace mdg {
+namespace batch {
+
+constexpr int kMaxCellsPerBox = 4096;  // cell counters and starts live in shared memory
+constexpr int kErrOverflow = 1, kErrBadState = 2;
+
+struct BoxDesc {
+  double L[3];
+  double inv_w[3];
+  float w32[3];
+  float dl32[3];
+  int nc[3];
+  int ncell;
+  int n;
+  int atom_off;
+  long long list_off;  // first entry of the box in the list pool (n * cap entries)
+  int cell_off;        // first cell start of the box (ncell + 1 entries)
+  int pad;
+};
+
+struct Params {
+  double sl2, rc2, c2x8, dt, dt2, half_margin2;
+  float acc_lo, acc_hi, rc2f, c2x8f;
+  int list_cap;
+  int nbox;
+};
+
+struct Dev {
+  BoxDesc *boxes;
+  int *cta_start, *cta_boxes;
+  double4_32a *q_end, *q_mid[2], *p, *q_build, *t_q, *t_p;
+  float4 *qf, *loc[2];
+  int *id, *cell, *t_id, *t_cell, *order, *cell_start;
+  uint32_t *nl;
+  int *ncount;
+  int *box_rebuild, *box_err, *box_need;
+  long long *box_steps, *box_rebuilds, *goal;
+  double *partials;  // per box: KE, PE, virial
+};
+
+__device__ __forceinline__ double rcp_hh3(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double e = fma(-x, y, 1.0);
+  return fma(y, fma(e, e, e), y);
+}
+
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x) {
+  const float t = s + x;
+  const float bp = t - s;
+  c += (s - (t - bp)) + (x - bp);
+  s = t;
+}
+
+__device__ __forceinline__ void cell_xyz(const BoxDesc &b, int c, int &cx, int &cy, int &cz) {
+  cx = c % b.nc[0];
+  const int t = c / b.nc[0];
+  cy = t % b.nc[1];
+  cz = t / b.nc[1];
+}
+
+// Exclusive scan over cnt[0..m) in shared memory by the whole CTA; writes the
+// starts to out[0..m] (out[m] = total) and zeroes cnt.
+__device__ void cta_scan(int *cnt, int *out, int m) {
+  __shared__ int warp_tot[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int base = 0; base < m; base += blockDim.x) {
+    const int c = base + threadIdx.x;
+    const int v = c < m ? cnt[c] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int t = lane < nw ? warp_tot[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      if (lane < nw) warp_tot[lane] = t;
+    }
+    __syncthreads();
+    if (c < m) {
+      out[c] = carry + (wid ? warp_tot[wid - 1] : 0) + x - v;
+      cnt[c] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warp_tot[nw - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[m] = carry;
+  __syncthreads();
+}
+
+// Rebuild of one box by the whole CTA: wrap (one +-L per component), bin,
+// stable reorder by (cell, particle index), mid-step positions, pair list.
+template <int MIXED>
+__device__ void rebuild_box(const Params &P, const Dev &d, const BoxDesc &b, int bi, int par, int *s_cnt,
+                            int *s_start, int *s_err) {
+  const int n = b.n, o = b.atom_off;
+  for (int c = threadIdx.x; c < b.ncell; c += blockDim.x) s_cnt[c] = 0;
+  if (threadIdx.x == 0) *s_err = 0;
+  __syncthreads();
+  for (int a = threadIdx.x; a < n; a += blockDim.x) {
+    double4_32a q = d.q_end[o + a];
+    double x[3] = {q.x, q.y, q.z};
+    int ci[3];
+    bool bad = false;
+    for (int k = 0; k < 3; k++) {
+      double v = x[k];
+      if (v < 0.0) v += b.L[k];
+      else if (v > b.L[k]) v -= b.L[k];
+      if (!(v >= 0.0 && v <= b.L[k])) bad = true;
+      x[k] = v;
+      int c = bad ? 0 : (int)(v * b.inv_w[k]);
+      ci[k] = c < 0 ? 0 : (c >= b.nc[k] ? b.nc[k] - 1 : c);
+    }
+    if (bad) *s_err = kErrBadState;
+    q.x = x[0]; q.y = x[1]; q.z = x[2];
+    d.q_end[o + a] = q;
+    const int cc = (ci[2] * b.nc[1] + ci[1]) * b.nc[0] + ci[0];
+    d.cell[o + a] = cc;
+    atomicAdd(&s_cnt[cc], 1);
+  }
+  __syncthreads();
+  if (*s_err) {
+    if (threadIdx.x == 0) d.box_err[bi] = kErrBadState;
+    __syncthreads();
+    return;
+  }
+  cta_scan(s_cnt, s_start, b.ncell);
+  for (int a = threadIdx.x; a < n; a += blockDim.x) {
+    const int c = d.cell[o + a];
+    d.order[o + s_start[c] + atomicAdd(&s_cnt[c], 1)] = a;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < b.ncell; c += blockDim.x) {
+    const int lo = s_start[c], hi = s_start[c + 1];
+    d.cell_start[b.cell_off + c] = lo;
+    for (int k = lo + 1; k < hi; k++) {
+      const int v = d.order[o + k], key = d.id[o + v];
+      int m = k - 1;
+      while (m >= lo && d.id[o + d.order[o + m]] > key) {
+        d.order[o + m + 1] = d.order[o + m];
+        m--;
+      }
+      d.order[o + m + 1] = v;
+    }
+  }
+  if (threadIdx.x == 0) d.cell_start[b.cell_off + b.ncell] = n;
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int src = o + d.order[o + k];
+    d.t_q[o + k] = d.q_end[src];
+    d.t_p[o + k] = d.p[src];
+    d.t_id[o + k] = d.id[src];
+    d.t_cell[o + k] = d.cell[src];
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double4_32a q = d.t_q[o + k], p = d.t_p[o + k];
+    const int c = d.t_cell[o + k];
+    d.q_end[o + k] = q;
+    d.p[o + k] = p;
+    d.id[o + k] = d.t_id[o + k];
+    d.cell[o + k] = c;
+    d.q_build[o + k] = q;
+    int cx, cy, cz;
+    cell_xyz(b, c, cx, cy, cz);
+    const double ox = ((double)cx + 0.5) * (double)b.w32[0], oy = ((double)cy + 0.5) * (double)b.w32[1],
+                 oz = ((double)cz + 0.5) * (double)b.w32[2];
+    d.qf[o + k] = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), 0.0f);
+    double4_32a m = q;
+    m.x = __dadd_rn(q.x, __dmul_rn(p.x, P.dt2));
+    m.y = __dadd_rn(q.y, __dmul_rn(p.y, P.dt2));
+    m.z = __dadd_rn(q.z, __dmul_rn(p.z, P.dt2));
+    d.q_mid[par][o + k] = m;
+    d.loc[par][o + k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), 0.0f);
+  }
+  __syncthreads();
+  int need = 0;
+  for (int a = threadIdx.x; a < n; a += blockDim.x) {
+    const float4 fi = d.qf[o + a];
+    int cx, cy, cz;
+    cell_xyz(b, d.cell[o + a], cx, cy, cz);
+    int cnt = 0;
+    for (int oz = -1; oz <= 1; oz++) {
+      int nz = cz + oz, sz = 0;
+      if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
+      const float offz = (float)oz * b.w32[2] + (float)sz * b.dl32[2];
+      for (int oy = -1; oy <= 1; oy++) {
+        int ny = cy + oy, sy = 0;
+        if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
+        const float offy = (float)oy * b.w32[1] + (float)sy * b.dl32[1];
+        for (int ox = -1; ox <= 1; ox++) {
+          int nx = cx + ox, sx = 0;
+          if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
+          const float offx = (float)ox * b.w32[0] + (float)sx * b.dl32[0];
+          const int cc = (nz * b.nc[1] + ny) * b.nc[0] + nx;
+          const int lo = s_start[cc], hi = s_start[cc + 1];
+          const uint32_t code = (uint32_t)((ox + 1) | ((oy + 1) << 2) | ((oz + 1) << 4)) << kJBits;
+          const bool self_cell = (sx | sy | sz) == 0;
+          const float fx = offx - fi.x, fy = offy - fi.y, fz = offz - fi.z;
+          for (int j = lo; j < hi; j++) {
+            const float4 fj = d.qf[o + j];
+            const float ex = fj.x + fx, ey = fj.y + fy, ez = fj.z + fz;
+            const float r2f = ex * ex + ey * ey + ez * ez;
+            if (r2f > P.acc_hi) continue;
+            if (self_cell && j == a) continue;
+            bool take = r2f < P.acc_lo;
+            if (!take) {
+              const double4_32a qi = d.q_end[o + a], qj = d.q_end[o + j];
+              const double xj = sx ? __dadd_rn(qj.x, sx > 0 ? b.L[0] : -b.L[0]) : qj.x;
+              const double yj = sy ? __dadd_rn(qj.y, sy > 0 ? b.L[1] : -b.L[1]) : qj.y;
+              const double zj = sz ? __dadd_rn(qj.z, sz > 0 ? b.L[2] : -b.L[2]) : qj.z;
+              const double dx = __dsub_rn(qi.x, xj), dy = __dsub_rn(qi.y, yj), dz = __dsub_rn(qi.z, zj);
+              const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+              take = r2 <= P.sl2;
+            }
+            if (take) {
+              if (cnt < P.list_cap) d.nl[b.list_off + (long long)cnt * n + a] = (uint32_t)j | code;
+              cnt++;
+            }
+          }
+        }
+      }
+    }
+    d.ncount[o + a] = cnt < P.list_cap ? cnt : P.list_cap;
+    need = max(need, cnt);
+  }
+  if (need > P.list_cap) {
+    atomicMax(&d.box_need[bi], need);
+    *s_err = kErrOverflow;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (*s_err) {
+      d.box_err[bi] = kErrOverflow;
+    } else {
+      d.box_rebuild[bi] = 0;
+      d.box_rebuilds[bi] += 1;
+    }
+  }
+  __syncthreads();
+}
+
+// Force on local particle a of box b from its row, lanes l = 0..LPI-1 of a group
+// taking every LPI-th entry; returns the group sum on every lane.
+template <int MIXED, int LPI>
+__device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, const BoxDesc &b, int a, int lane, int par) {
+  const int o = b.atom_off, n = b.n;
+  int cx, cy, cz;
+  cell_xyz(b, d.cell[o + a], cx, cy, cz);
+  const int cnt = d.ncount[o + a];
+  const uint32_t *row = d.nl + b.list_off + a;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (MIXED) {
+    const float4 li = d.loc[par][o + a];
+    const float mx0 = -b.w32[0] - (cx == 0 ? b.dl32[0] : 0.0f) - li.x, px0 = b.w32[0] + (cx == b.nc[0] - 1 ? b.dl32[0] : 0.0f) - li.x;
+    const float mx1 = -b.w32[1] - (cy == 0 ? b.dl32[1] : 0.0f) - li.y, px1 = b.w32[1] + (cy == b.nc[1] - 1 ? b.dl32[1] : 0.0f) - li.y;
+    const float mx2 = -b.w32[2] - (cz == 0 ? b.dl32[2] : 0.0f) - li.z, px2 = b.w32[2] + (cz == b.nc[2] - 1 ? b.dl32[2] : 0.0f) - li.z;
+    float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
+    for (int k = lane; k < cnt; k += LPI) {
+      const uint32_t e = __ldg(row + (long long)k * n);
+      const float4 lj = __ldg(d.loc[par] + o + (e & kJMask));
+      const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+      const float dx = lj.x + (ox == 0 ? mx0 : (ox == 2 ? px0 : -li.x));
+      const float dy = lj.y + (oy == 0 ? mx1 : (oy == 2 ? px1 : -li.y));
+      const float dz = lj.z + (oz == 0 ? mx2 : (oz == 2 ? px2 : -li.z));
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 <= P.rc2f) {
+        float inv;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+        const float i6 = inv * inv * inv;
+        const float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + P.c2x8f;
+        two_sum_acc(sx, ex, df * dx);
+        two_sum_acc(sy, ey, df * dy);
+        two_sum_acc(sz, ez, df * dz);
+      }
+    }
+    fx = (double)sx + (double)ex;
+    fy = (double)sy + (double)ey;
+    fz = (double)sz + (double)ez;
+  } else {
+    const double4_32a qi = d.q_mid[par][o + a];
+    const bool edge = cx == 0 || cy == 0 || cz == 0 || cx == b.nc[0] - 1 || cy == b.nc[1] - 1 || cz == b.nc[2] - 1;
+    for (int k = lane; k < cnt; k += LPI) {
+      const uint32_t e = __ldg(row + (long long)k * n);
+      double4_32a qj = ldg4(d.q_mid[par] + o + (e & kJMask));
+      if (edge) {
+        const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+        if (ox == 0 && cx == 0) qj.x -= b.L[0]; else if (ox == 2 && cx == b.nc[0] - 1) qj.x += b.L[0];
+        if (oy == 0 && cy == 0) qj.y -= b.L[1]; else if (oy == 2 && cy == b.nc[1] - 1) qj.y += b.L[1];
+        if (oz == 0 && cz == 0) qj.z -= b.L[2]; else if (oz == 2 && cz == b.nc[2] - 1) qj.z += b.L[2];
+      }
+      const double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 <= P.rc2) {
+        const double inv = rcp_hh3(r2);
+        const double i6 = inv * inv * inv;
+        const double df = (i6 * inv) * fma(-48.0, i6, 24.0) + P.c2x8;
+        fx = fma(df, dx, fx);
+        fy = fma(df, dy, fy);
+        fz = fma(df, dz, fz);
+      }
+    }
+  }
+  if (LPI > 1) {
+#pragma unroll
+    for (int off = LPI / 2; off > 0; off >>= 1) {
+      fx += __shfl_xor_sync(0xffffffffu, fx, off, LPI);
+      fy += __shfl_xor_sync(0xffffffffu, fy, off, LPI);
+      fz += __shfl_xor_sync(0xffffffffu, fz, off, LPI);
+    }
+  }
+  return make_double3(fx, fy, fz);
+}
+
+template <int MIXED, int LPI>
+__global__ void k_batch_step(Params P, Dev d, int par) {
+  __shared__ int s_cnt[kMaxCellsPerBox];
+  __shared__ int s_start[kMaxCellsPerBox + 1];
+  __shared__ int s_flag[2];
+  const long long goal = *d.goal;
+  for (int t = d.cta_start[blockIdx.x]; t < d.cta_start[blockIdx.x + 1]; t++) {
+    const int bi = d.cta_boxes[t];
+    if (threadIdx.x == 0) {
+      s_flag[0] = (d.box_err[bi] == 0 && d.box_steps[bi] < goal) ? 1 : 0;
+      s_flag[1] = d.box_rebuild[bi];
+    }
+    __syncthreads();
+    const int go = s_flag[0], rb = s_flag[1];
+    __syncthreads();
+    if (!go) continue;
+    const BoxDesc b = d.boxes[bi];
+    if (rb) {
+      rebuild_box<MIXED>(P, d, b, bi, par, s_cnt, s_start, &s_flag[0]);
+      if (threadIdx.x == 0) s_flag[1] = d.box_err[bi];
+      __syncthreads();
+      const int err = s_flag[1];
+      __syncthreads();
+      if (err) continue;
+    }
+    const int o = b.atom_off, n = b.n;
+    const int groups = blockDim.x / LPI, lane = threadIdx.x % LPI;
+    bool rebuild = false;
+    // all lanes of a group stay together: loop bound rounded to whole groups
+    for (int a0 = threadIdx.x / LPI; a0 < ((n + groups - 1) / groups) * groups; a0 += groups) {
+      const int a = a0 < n ? a0 : n - 1;
+      const double3 F = box_force<MIXED, LPI>(P, d, b, a, lane, par);
+      if (lane != 0 || a0 >= n) continue;
+      double4_32a p = d.p[o + a];
+      p.x += F.x * P.dt;
+      p.y += F.y * P.dt;
+      p.z += F.z * P.dt;
+      const double4_32a q0 = d.q_mid[par][o + a];
+      double4_32a qe = q0, q1 = q0;
+      qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, P.dt2));
+      qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, P.dt2));
+      qe.z = __dadd_rn(q0.z, __dmul_rn(p.z, P.dt2));
+      q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, P.dt2));
+      q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, P.dt2));
+      q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, P.dt2));
+      const double4_32a qb = d.q_build[o + a];
+      const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
+      if (ux * ux + uy * uy + uz * uz > P.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
+        rebuild = true;
+      const float4 lb = d.qf[o + a];
+      d.loc[par ^ 1][o + a] = make_float4(lb.x + (float)ux, lb.y + (float)uy, lb.z + (float)uz, 0.0f);
+      d.p[o + a] = p;
+      d.q_end[o + a] = qe;
+      d.q_mid[par ^ 1][o + a] = q1;
+    }
+    const int any = __syncthreads_or(rebuild ? 1 : 0);
+    if (threadIdx.x == 0) {
+      if (any) d.box_rebuild[bi] = 1;
+      d.box_steps[bi] += 1;
+    }
+  }
+}
+
+// Per-box observer sums at q_end (observer.cc:5-79 expressions, pairs 1/2 each).
+__global__ void k_batch_observe(Params P, Dev d) {
+  __shared__ double sh[3][32];
+  const int bi = blockIdx.x;
+  const BoxDesc b = d.boxes[bi];
+  const int o = b.atom_off, n = b.n;
+  double ke = 0.0, pe = 0.0, vir = 0.0;
+  for (int a = threadIdx.x; a < n; a += blockDim.x) {
+    const double4_32a p = d.p[o + a];
+    ke += 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+    const double4_32a qi = d.q_end[o + a];
+    int cx, cy, cz;
+    cell_xyz(b, d.cell[o + a], cx, cy, cz);
+    const int cnt = d.ncount[o + a];
+    for (int k = 0; k < cnt; k++) {
+      const uint32_t e = d.nl[b.list_off + (long long)k * n + a];
+      double4_32a qj = d.q_end[o + (e & kJMask)];
+      const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+      if (ox == 0 && cx == 0) qj.x -= b.L[0]; else if (ox == 2 && cx == b.nc[0] - 1) qj.x += b.L[0];
+      if (oy == 0 && cy == 0) qj.y -= b.L[1]; else if (oy == 2 && cy == b.nc[1] - 1) qj.y += b.L[1];
+      if (oz == 0 && cz == 0) qj.z -= b.L[2]; else if (oz == 2 && cz == b.nc[2] - 1) qj.z += b.L[2];
+      const double dx = __dsub_rn(qi.x, qj.x), dy = __dsub_rn(qi.y, qj.y), dz = __dsub_rn(qi.z, qj.z);
+      const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+      if (r2 > P.rc2) continue;
+      const double r4 = __dmul_rn(r2, r2), r6 = __dmul_rn(r4, r2), r8 = __dmul_rn(r6, r2), r10 = __dmul_rn(r8, r2),
+                   r12 = __dmul_rn(r10, r2);
+      const double c2 = P.c2x8 / 8.0;
+      const double c0 = -1.0 / (P.rc2 * P.rc2 * P.rc2 * P.rc2 * P.rc2 * P.rc2) + 1.0 / (P.rc2 * P.rc2 * P.rc2) -
+                        c2 * P.rc2;
+      pe += 0.5 * (4.0 * (1.0 / r12 - 1.0 / r6 + __dmul_rn(c2, r2) + c0));
+      vir += 0.5 * ((__dsub_rn(__dmul_rn(24.0, r6), 48.0) / (__dmul_rn(__dmul_rn(r6, r6), r2)) + P.c2x8) * r2);
+    }
+  }
+  double v[3] = {ke, pe, vir};
+  for (int k = 0; k < 3; k++)
+    for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 3; k++) sh[k][threadIdx.x >> 5] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[3] = {0, 0, 0};
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++)
+      for (int k = 0; k < 3; k++) t[k] += sh[k][w];
+    d.partials[3 * bi + 0] = t[0];
+    d.partials[3 * bi + 1] = t[1];
+    d.partials[3 * bi + 2] = t[2] / 3.0;
+  }
+}
+
+__global__ void k_batch_unsort(Dev d, int total, double4_32a *qo, double4_32a *po, const int *box_of_slot) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= total) return;
+  const int bi = box_of_slot[s];
+  const int dst = d.boxes[bi].atom_off + d.id[s];
+  if (qo) qo[dst] = d.q_end[s];
+  if (po) po[dst] = d.p[s];
+}
+
+}  // namespace batch
+}  // namespace mdg
+
+// ---------------------------------------------------------------- C ABI
+using namespace mdg::batch;
+
+struct mdg_batch {
+  mdg_batch_params prm;
+  std::string err;
+  int nbox = 0, total = 0, num_sms = 0;
+  int threads = 256, lpi = 1, ctas_per_sm = 2;
+  cudaStream_t stream = nullptr;
+  Params P;
+  Dev d;
+  std::vector<BoxDesc> boxes;
+  std::vector<int> box_of_slot;
+  int *d_box_of_slot = nullptr;
+  int par = 0;
+  long long steps = 0;  // goal reached by every box
+  cudaGraphExec_t gx[2] = {nullptr, nullptr};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  long long launches = 0;
+  int grid = 0;
+};
+
+namespace {
+
+int bfail(mdg_batch *b, int code, const std::string &m) {
+  if (b) b->err = m;
+  return code;
+}
+
+#define MDG_BCK(call)                                                                               \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) return bfail(b, MDG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+void drop_batch_graphs(mdg_batch *b) {
+  for (int k = 0; k < 2; k++)
+    if (b->gx[k]) {
+      cudaGraphExecDestroy(b->gx[k]);
+      b->gx[k] = nullptr;
+    }
+}
+
+template <class T>
+cudaError_t balloc(T **p, size_t count) {
+  *p = nullptr;
+  return cudaMalloc((void **)p, (count ? count : 1) * sizeof(T));
+}
+
+// Longest-first assignment of boxes to grid CTAs (work ~ n * list capacity).
+int assign(mdg_batch *b) {
+  const int G = b->num_sms * b->ctas_per_sm;
+  std::vector<int> idx(b->nbox);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return b->boxes[x].n > b->boxes[y].n; });
+  std::vector<long long> load(G, 0);
+  std::vector<std::vector<int>> own(G);
+  for (int k : idx) {
+    int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    own[best].push_back(k);
+    load[best] += b->boxes[k].n;
+  }
+  std::vector<int> start(G + 1, 0), flat;
+  for (int g = 0; g < G; g++) {
+    start[g + 1] = start[g] + (int)own[g].size();
+    flat.insert(flat.end(), own[g].begin(), own[g].end());
+  }
+  if (b->d.cta_start) cudaFree(b->d.cta_start);
+  if (b->d.cta_boxes) cudaFree(b->d.cta_boxes);
+  MDG_BCK(balloc(&b->d.cta_start, G + 1));
+  MDG_BCK(balloc(&b->d.cta_boxes, b->nbox));
+  MDG_BCK(cudaMemcpy(b->d.cta_start, start.data(), (G + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  MDG_BCK(cudaMemcpy(b->d.cta_boxes, flat.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice));
+  b->grid = G;
+  drop_batch_graphs(b);
+  return MDG_OK;
+}
+
+// (Re)allocates the list pool for capacity `cap` and uploads box descriptors.
+int alloc_batch_list(mdg_batch *b, int cap) {
+  long long off = 0;
+  for (auto &bx : b->boxes) {
+    bx.list_off = off;
+    off += (long long)bx.n * cap;
+  }
+  if (b->d.nl) cudaFree(b->d.nl);
+  MDG_BCK(balloc(&b->d.nl, (size_t)off));
+  b->P.list_cap = cap;
+  MDG_BCK(cudaMemcpy(b->d.boxes, b->boxes.data(), b->nbox * sizeof(BoxDesc), cudaMemcpyHostToDevice));
+  std::vector<int> ones(b->nbox, 1);
+  MDG_BCK(cudaMemcpy(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice));
+  drop_batch_graphs(b);
+  return MDG_OK;
+}
+
+void launch_batch_step(mdg_batch *b, int par) {
+  const int T = b->threads;
+  const bool mixed = b->prm.precision == MDG_MIXED;
+#define MDG_BSTEP(M, L) k_batch_step<M, L><<<b->grid, T, 0, b->stream>>>(b->P, b->d, par)
+  if (mixed) {
+    if (b->lpi == 4) MDG_BSTEP(1, 4); else if (b->lpi == 2) MDG_BSTEP(1, 2); else MDG_BSTEP(1, 1);
+  } else {
+    if (b->lpi == 4) MDG_BSTEP(0, 4); else if (b->lpi == 2) MDG_BSTEP(0, 2); else MDG_BSTEP(0, 1);
+  }
+#undef MDG_BSTEP
+  b->launches += 1;
+}
+
+int run_steps(mdg_batch *b, int nsteps) {
+  if (!b->prm.use_graphs) {
+    for (int k = 0; k < nsteps; k++) {
+      launch_batch_step(b, b->par);
+      b->par ^= 1;
+    }
+    return cudaGetLastError() == cudaSuccess ? MDG_OK : bfail(b, MDG_ERR_CUDA, "launch failed");
+  }
+  int left = nsteps;
+  while (left > 0) {
+    const int par = b->par;
+    if (left >= 2) {
+      if (!b->gx[par]) {
+        cudaGraph_t g = nullptr;
+        MDG_BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        const long long l0 = b->launches;
+        launch_batch_step(b, par);
+        launch_batch_step(b, par ^ 1);
+        b->launches = l0;
+        MDG_BCK(cudaStreamEndCapture(b->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&b->gx[par], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bfail(b, MDG_ERR_CUDA, cudaGetErrorString(e));
+      }
+      MDG_BCK(cudaGraphLaunch(b->gx[par], b->stream));
+      b->launches += 2;
+      left -= 2;
+    } else {
+      launch_batch_step(b, par);
+      b->par ^= 1;
+      left -= 1;
+    }
+  }
+  return MDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mdg_batch_params_default(mdg_batch_params *p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->precision = MDG_FP64;
+  p->cutoff = 2.5;
+  p->margin = 0.4;
+  p->dt = 0.002;
+  p->list_capacity = 0;
+  p->use_graphs = 1;
+}
+
+int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_per_box, const double *box_lengths,
+                     mdg_batch **out) {
+  if (!p || !out || nbox <= 0 || !n_per_box || !box_lengths) return MDG_ERR_INVALID;
+  *out = nullptr;
+  mdg_batch *b = new mdg_batch();
+  b->prm = *p;
+  b->nbox = nbox;
+  memset(&b->d, 0, sizeof(b->d));
+  const double sl = p->cutoff + p->margin;
+  long long total = 0, cells = 0;
+  double max_rho = 0.0;
+  for (int k = 0; k < nbox; k++) {
+    BoxDesc bx;
+    memset(&bx, 0, sizeof bx);
+    bx.n = n_per_box[k];
+    if (bx.n <= 0) {
+      delete b;
+      return MDG_ERR_INVALID;
+    }
+    long long nc_tot = 1;
+    for (int a = 0; a < 3; a++) {
+      const double L = box_lengths[3 * k + a];
+      int nc = (int)(L / sl);
+      while (nc > 0 && L / (double)nc < sl * (1.0 + 1e-12)) nc--;
+      if (nc < 2 || !(L > 2.0 * sl)) {
+        delete b;
+        return MDG_ERR_INVALID;
+      }
+      const double w = L / (double)nc;
+      bx.L[a] = L;
+      bx.nc[a] = nc;
+      bx.inv_w[a] = 1.0 / w;
+      bx.w32[a] = (float)w;
+      bx.dl32[a] = (float)(L - (double)nc * (double)bx.w32[a]);
+      nc_tot *= nc;
+    }
+    if (nc_tot > kMaxCellsPerBox) {
+      delete b;
+      return MDG_ERR_CAPACITY;
+    }
+    bx.ncell = (int)nc_tot;
+    bx.atom_off = (int)total;
+    bx.cell_off = (int)cells;
+    total += bx.n;
+    cells += nc_tot + 1;
+    max_rho = std::max(max_rho, bx.n / (bx.L[0] * bx.L[1] * bx.L[2]));
+    b->boxes.push_back(bx);
+  }
+  if (total > (1LL << 30)) {
+    delete b;
+    return MDG_ERR_CAPACITY;
+  }
+  b->total = (int)total;
+  for (int k = 0; k < nbox; k++)
+    for (int a = 0; a < b->boxes[k].n; a++) b->box_of_slot.push_back(k);
+  Params &P = b->P;
+  P.sl2 = sl * sl;
+  P.rc2 = p->cutoff * p->cutoff;
+  const double s2 = 1.0 / P.rc2, s6 = s2 * s2 * s2, s8 = s6 * s2, s12 = s6 * s6, s14 = s12 * s2;
+  P.c2x8 = (6.0 * s14 - 3.0 * s8) * 8.0;
+  (void)s12;
+  P.c2x8f = (float)P.c2x8;
+  P.rc2f = (float)P.rc2;
+  P.acc_lo = (float)(sl * sl - 1e-4);
+  P.acc_hi = (float)(sl * sl + 1e-4);
+  P.dt = p->dt;
+  P.dt2 = p->dt * 0.5;
+  P.half_margin2 = 0.25 * p->margin * p->margin;
+  P.nbox = nbox;
+  int cap = p->list_capacity > 0 ? p->list_capacity : (int)(max_rho * 4.18879020478639 * sl * sl * sl * 1.5 + 24);
+  cap = (cap + 7) & ~7;
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, p->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+  Dev &d = b->d;
+  const size_t n = (size_t)total;
+  if (e == cudaSuccess) e = balloc(&d.boxes, nbox);
+  if (e == cudaSuccess) e = balloc(&d.q_end, n);
+  if (e == cudaSuccess) e = balloc(&d.q_mid[0], n);
+  if (e == cudaSuccess) e = balloc(&d.q_mid[1], n);
+  if (e == cudaSuccess) e = balloc(&d.p, n);
+  if (e == cudaSuccess) e = balloc(&d.q_build, n);
+  if (e == cudaSuccess) e = balloc(&d.t_q, n);
+  if (e == cudaSuccess) e = balloc(&d.t_p, n);
+  if (e == cudaSuccess) e = balloc(&d.qf, n);
+  if (e == cudaSuccess) e = balloc(&d.loc[0], n);
+  if (e == cudaSuccess) e = balloc(&d.loc[1], n);
+  if (e == cudaSuccess) e = balloc(&d.id, n);
+  if (e == cudaSuccess) e = balloc(&d.cell, n);
+  if (e == cudaSuccess) e = balloc(&d.t_id, n);
+  if (e == cudaSuccess) e = balloc(&d.t_cell, n);
+  if (e == cudaSuccess) e = balloc(&d.order, n);
+  if (e == cudaSuccess) e = balloc(&d.ncount, n);
+  if (e == cudaSuccess) e = balloc(&d.cell_start, (size_t)cells);
+  if (e == cudaSuccess) e = balloc(&d.box_rebuild, nbox);
+  if (e == cudaSuccess) e = balloc(&d.box_err, nbox);
+  if (e == cudaSuccess) e = balloc(&d.box_need, nbox);
+  if (e == cudaSuccess) e = balloc(&d.box_steps, nbox);
+  if (e == cudaSuccess) e = balloc(&d.box_rebuilds, nbox);
+  if (e == cudaSuccess) e = balloc(&d.goal, 1);
+  if (e == cudaSuccess) e = balloc(&d.partials, 3 * (size_t)nbox);
+  if (e == cudaSuccess) e = balloc(&b->d_box_of_slot, n);
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_box_of_slot, b->box_of_slot.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "mdg_batch_create: %s\n", cudaGetErrorString(e));
+    mdg_batch_destroy(b);
+    return MDG_ERR_CUDA;
+  }
+  if (alloc_batch_list(b, cap) != MDG_OK || assign(b) != MDG_OK) {
+    fprintf(stderr, "mdg_batch_create: %s\n", b->err.c_str());
+    mdg_batch_destroy(b);
+    return MDG_ERR_CUDA;
+  }
+  *out = b;
+  return MDG_OK;
+}
+
+int mdg_batch_destroy(mdg_batch *b) {
+  if (!b) return MDG_OK;
+  cudaSetDevice(b->prm.device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_batch_graphs(b);
+  Dev &d = b->d;
+  void *ptrs[] = {d.boxes, d.cta_start, d.cta_boxes, d.q_end, d.q_mid[0], d.q_mid[1], d.p, d.q_build, d.t_q, d.t_p,
+                  d.qf, d.loc[0], d.loc[1], d.id, d.cell, d.t_id, d.t_cell, d.order, d.cell_start, d.nl, d.ncount,
+                  d.box_rebuild, d.box_err, d.box_need, d.box_steps, d.box_rebuilds, d.goal, d.partials,
+                  b->d_box_of_slot};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return MDG_OK;
+}
+
+const char *mdg_batch_last_error(const mdg_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int mdg_batch_set_state(mdg_batch *b, const double *q4, const double *p4) {
+  if (!b || !q4 || !p4) return MDG_ERR_INVALID;
+  cudaSetDevice(b->prm.device);
+  const size_t bytes = (size_t)b->total * 32;
+  MDG_BCK(cudaMemcpyAsync(b->d.q_end, q4, bytes, cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.p, p4, bytes, cudaMemcpyHostToDevice, b->stream));
+  std::vector<int> ids(b->total);
+  for (int k = 0; k < b->nbox; k++)
+    for (int a = 0; a < b->boxes[k].n; a++) ids[b->boxes[k].atom_off + a] = a;
+  MDG_BCK(cudaMemcpyAsync(b->d.id, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  std::vector<int> ones(b->nbox, 1), zeros(b->nbox, 0);
+  std::vector<long long> lz(b->nbox, 0);
+  MDG_BCK(cudaMemcpyAsync(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.box_err, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.box_need, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.box_steps, lz.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.box_rebuilds, lz.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaStreamSynchronize(b->stream));
+  b->steps = 0;
+  b->par = 0;
+  drop_batch_graphs(b);
+  return MDG_OK;
+}
+
+int mdg_batch_get_state(mdg_batch *b, double *q4, double *p4) {
+  if (!b) return MDG_ERR_INVALID;
+  cudaSetDevice(b->prm.device);
+  double4_32a *tq = b->d.t_q, *tp = b->d.t_p;  // staging (free outside rebuilds)
+  k_batch_unsort<<<(b->total + 255) / 256, 256, 0, b->stream>>>(b->d, b->total, q4 ? tq : nullptr,
+                                                                 p4 ? tp : nullptr, b->d_box_of_slot);
+  const size_t bytes = (size_t)b->total * 32;
+  if (q4) MDG_BCK(cudaMemcpyAsync(q4, tq, bytes, cudaMemcpyDeviceToHost, b->stream));
+  if (p4) MDG_BCK(cudaMemcpyAsync(p4, tp, bytes, cudaMemcpyDeviceToHost, b->stream));
+  MDG_BCK(cudaStreamSynchronize(b->stream));
+  return MDG_OK;
+}
+
+int mdg_batch_calculate(mdg_batch *b, int32_t nsteps) {
+  if (!b || nsteps < 0) return MDG_ERR_INVALID;
+  cudaSetDevice(b->prm.device);
+  if (nsteps == 0) return MDG_OK;
+  const long long goal = b->steps + nsteps;
+  MDG_BCK(cudaMemcpyAsync(b->d.goal, &goal, sizeof goal, cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaEventRecord(b->ev0, b->stream));
+  int rc = run_steps(b, nsteps);
+  if (rc) return rc;
+  for (int round = 0; round < 32; round++) {
+    std::vector<int> err(b->nbox), need(b->nbox);
+    std::vector<long long> st(b->nbox);
+    MDG_BCK(cudaMemcpyAsync(err.data(), b->d.box_err, b->nbox * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    MDG_BCK(cudaMemcpyAsync(need.data(), b->d.box_need, b->nbox * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    MDG_BCK(cudaMemcpyAsync(st.data(), b->d.box_steps, b->nbox * sizeof(long long), cudaMemcpyDeviceToHost, b->stream));
+    MDG_BCK(cudaStreamSynchronize(b->stream));
+    long long behind = 0;
+    int maxneed = 0;
+    for (int k = 0; k < b->nbox; k++) {
+      if (err[k] == kErrBadState) return bfail(b, MDG_ERR_STATE, "box " + std::to_string(k) + ": bad coordinate");
+      behind = std::max(behind, goal - st[k]);
+      if (err[k] == kErrOverflow) maxneed = std::max(maxneed, need[k]);
+    }
+    if (behind == 0) break;
+    if (maxneed > 0) {
+      int cap = ((int)(maxneed * 1.25) + 15) & ~7;
+      rc = alloc_batch_list(b, cap);  // every box rebuilds its list at the new capacity
+      if (rc) return rc;
+      std::vector<int> zeros(b->nbox, 0);
+      MDG_BCK(cudaMemcpyAsync(b->d.box_err, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+      MDG_BCK(cudaMemcpyAsync(b->d.box_need, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    }
+    // catch-up: only boxes behind the goal advance
+    for (long long k = 0; k < behind; k++) {
+      launch_batch_step(b, b->par);
+      b->par ^= 1;
+    }
+    drop_batch_graphs(b);
+    b->par = 0;  // parity is re-established by the rebuild of every box
+    std::vector<int> ones(b->nbox, 1);
+    MDG_BCK(cudaMemcpyAsync(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  }
+  MDG_BCK(cudaEventRecord(b->ev1, b->stream));
+  MDG_BCK(cudaEventSynchronize(b->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+  b->last_ms = ms;
+  b->steps = goal;
+  return MDG_OK;
+}
+
+int mdg_batch_observe(mdg_batch *b, double *out) {
+  if (!b || !out) return MDG_ERR_INVALID;
+  cudaSetDevice(b->prm.device);
+  k_batch_observe<<<b->nbox, 256, 0, b->stream>>>(b->P, b->d);
+  MDG_BCK(cudaMemcpyAsync(out, b->d.partials, 3 * (size_t)b->nbox * sizeof(double), cudaMemcpyDeviceToHost,
+                          b->stream));
+  MDG_BCK(cudaStreamSynchronize(b->stream));
+  return MDG_OK;
+}
+
+int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t *lanes_per_particle,
+                   int32_t *ctas_per_sm) {
+  if (!b || trial_steps <= 0) return MDG_ERR_INVALID;
+  cudaSetDevice(b->prm.device);
+  // work on a copy of the state and restore it afterwards
+  const size_t n = (size_t)b->total;
+  double4_32a *sq = nullptr, *sp = nullptr;
+  int *sid = nullptr;
+  MDG_BCK(balloc(&sq, n));
+  MDG_BCK(balloc(&sp, n));
+  MDG_BCK(balloc(&sid, n));
+  MDG_BCK(cudaMemcpyAsync(sq, b->d.q_end, n * 32, cudaMemcpyDeviceToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(sp, b->d.p, n * 32, cudaMemcpyDeviceToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(sid, b->d.id, n * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
+  std::vector<long long> st0(b->nbox);
+  MDG_BCK(cudaMemcpy(st0.data(), b->d.box_steps, b->nbox * sizeof(long long), cudaMemcpyDeviceToHost));
+  const long long steps0 = b->steps;
+  const int T0 = b->threads, L0 = b->lpi, C0 = b->ctas_per_sm;
+  double best = 1e300;
+  int bt = T0, bl = L0, bc = C0;
+  const int Ts[] = {128, 256, 512}, Ls[] = {1, 2, 4}, Cs[] = {1, 2, 4};
+  for (int T : Ts)
+    for (int Lp : Ls)
+      for (int C : Cs) {
+        if (T * C > 2048) continue;
+        b->threads = T;
+        b->lpi = Lp;
+        b->ctas_per_sm = C;
+        int rc = assign(b);
+        if (rc) return rc;
+        // every trial starts from the saved state with fresh lists
+        MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
+        MDG_BCK(cudaMemcpyAsync(b->d.p, sp, n * 32, cudaMemcpyDeviceToDevice, b->stream));
+        MDG_BCK(cudaMemcpyAsync(b->d.id, sid, n * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
+        std::vector<int> ones(b->nbox, 1);
+        MDG_BCK(cudaMemcpyAsync(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+        MDG_BCK(cudaMemcpyAsync(b->d.box_steps, st0.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+        b->steps = steps0;
+        b->par = 0;
+        rc = mdg_batch_calculate(b, 2);  // builds lists
+        if (rc) return rc;
+        rc = mdg_batch_calculate(b, trial_steps);
+        if (rc) return rc;
+        if (b->last_ms < best) {
+          best = b->last_ms;
+          bt = T;
+          bl = Lp;
+          bc = C;
+        }
+      }
+  b->threads = bt;
+  b->lpi = bl;
+  b->ctas_per_sm = bc;
+  int rc = assign(b);
+  if (rc) return rc;
+  MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.p, sp, n * 32, cudaMemcpyDeviceToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.id, sid, n * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
+  std::vector<int> ones(b->nbox, 1);
+  MDG_BCK(cudaMemcpyAsync(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.box_steps, st0.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaStreamSynchronize(b->stream));
+  b->steps = steps0;
+  b->par = 0;
+  cudaFree(sq);
+  cudaFree(sp);
+  cudaFree(sid);
+  if (threads) *threads = bt;
+  if (lanes_per_particle) *lanes_per_particle = bl;
+  if (ctas_per_sm) *ctas_per_sm = bc;
+  return MDG_OK;
+}
+
+int mdg_batch_set_shape(mdg_batch *b, int32_t threads, int32_t lanes_per_particle, int32_t ctas_per_sm) {
+  if (!b || (threads != 128 && threads != 256 && threads != 512 && threads != 1024) ||
+      (lanes_per_particle != 1 && lanes_per_particle != 2 && lanes_per_particle != 4) || ctas_per_sm < 1 ||
+      threads * ctas_per_sm > 2048)
+    return MDG_ERR_INVALID;
+  b->threads = threads;
+  b->lpi = lanes_per_particle;
+  b->ctas_per_sm = ctas_per_sm;
+  return assign(b);
+}
+
+int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s) {
+  if (!b || !s) return MDG_ERR_INVALID;
+  memset(s, 0, sizeof(*s));
+  std::vector<long long> rb(b->nbox);
+  MDG_BCK(cudaMemcpy(rb.data(), b->d.box_rebuilds, b->nbox * sizeof(long long), cudaMemcpyDeviceToHost));
+  s->steps = b->steps;
+  for (long long v : rb) s->rebuilds += v;
+  s->particles = b->total;
+  s->boxes = b->nbox;
+  s->list_capacity = b->P.list_cap;
+  s->threads = b->threads;
+  s->lanes_per_particle = b->lpi;
+  s->ctas_per_sm = b->ctas_per_sm;
+  s->elapsed_ms = b->last_ms;
+  s->kernel_launches = b->launches;
+  return MDG_OK;
+}
+
+}  // extern "C"

@@ -61,6 +61,14 @@ __global__ void k_wrap_bin(Geom g, Dev d, int count_step, int lang_step) {
   if (count_step && blockIdx.x == 0 && threadIdx.x == 0 && f->halt == 0) {
     f->steps += 1;
     if (lang_step) f->lang += 1;
+    // inner-list re-selection requested by the last step (or by a rebuild
+    // outside a step) happens in this step's kernel
+    f->prune_now = f->prune_next;
+    f->prune_next = 0;
+    if (f->prune_now) {
+      f->prunes += 1;
+      f->inner_pairs = 0;
+    }
   }
   if (rebuild_off(f)) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
@@ -223,7 +231,7 @@ __global__ void k_set_rebuild(DevFlags *f) {
 }  // namespace
 
 // Declared in mdg_list.cu.
-void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s);
+void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s, bool in_step);
 
 void launch_set_rebuild(const Dev &d, cudaStream_t s) { k_set_rebuild<<<1, 1, 0, s>>>(d.flags); }
 
@@ -245,7 +253,7 @@ void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cud
   k_cell_sort<<<cgrid, threads, 0, s>>>(g, d);
   k_reorder<<<grid, threads, 0, s>>>(g, d);
   k_finalize<<<grid, threads, 0, s>>>(g, d, q_mid_dst);
-  launch_build_list(g, d, num_sms, s);
+  launch_build_list(g, d, num_sms, s, count_step);
 }
 
 }  // namespace mdg

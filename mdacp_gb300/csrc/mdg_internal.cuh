@@ -51,6 +51,10 @@ struct DevFlags {
   double zeta_a;                // zeta after the first update of the coming step
   double exp1;                  // exp(-dt/2 * zeta_a)
   double t_cur;                 // temperature of the current momenta
+  int prune_now;                // this step's kernel re-selects the inner list (set by the prelude)
+  int prune_next;               // a particle left its prune buffer: re-select at the next step
+  unsigned long long prunes;    // completed prunes
+  unsigned long long inner_pairs;  // directed pairs in the inner list at the last prune
 };
 
 struct Geom {
@@ -75,6 +79,9 @@ struct Geom {
   float w32[3];       // cell widths rounded to float
   float dl32[3];      // L - nc * w32
   float c2x8f;
+  // inner (pruned) list: pairs within rc + prune_buffer at the last prune
+  float prune_thr2;   // (rc + buffer)^2 + float slack
+  float half_prune2;  // (buffer / 2)^2, displacement that forces a re-prune
 };
 
 struct Dev {
@@ -86,6 +93,9 @@ struct Dev {
   int *cell_count, *cell_fill, *cell_start, *block_sums;
   uint32_t *nl;
   int *ncount;
+  uint32_t *pl;         // inner list, same layout and capacity as nl
+  int *pcount;
+  float4 *loc_p;        // home-cell-local position at the last prune
   double *partials;     // reduction scratch
   int nblocks_red;
   DevFlags *flags;

@@ -105,10 +105,19 @@ __global__ void __launch_bounds__(kListThreads) k_build_list(Geom g, Dev d) {
   }
 }
 
-__global__ void k_rebuild_done(DevFlags *f) {
+// A new outer list always gets a fresh inner list: in this step's kernel
+// when the rebuild ran inside a step, otherwise in the next step's.
+__global__ void k_rebuild_done(DevFlags *f, int in_step) {
   if (f->halt == 0 && f->rebuild) {
     f->rebuild = 0;
     f->rebuilds += 1;
+    if (!in_step) {
+      f->prune_next = 1;
+    } else if (!f->prune_now) {
+      f->prune_now = 1;
+      f->prunes += 1;
+      f->inner_pairs = 0;
+    }
   }
 }
 
@@ -121,12 +130,12 @@ __global__ void k_list_prepare(DevFlags *f) {
 
 }  // namespace
 
-void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s) {
+void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s, bool in_step) {
   k_list_prepare<<<1, 1, 0, s>>>(d.flags);
   int grid = (g.n + kListThreads - 1) / kListThreads;
   if (grid > num_sms * 16) grid = num_sms * 16;
   k_build_list<<<grid > 0 ? grid : 1, kListThreads, 0, s>>>(g, d);
-  k_rebuild_done<<<1, 1, 0, s>>>(d.flags);
+  k_rebuild_done<<<1, 1, 0, s>>>(d.flags, in_step ? 1 : 0);
 }
 
 }  // namespace mdg

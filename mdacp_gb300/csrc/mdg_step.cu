@@ -72,11 +72,20 @@ __device__ __forceinline__ void apply_image(const Geom &g, const CellPos &cp, ui
 
 // Sum over the row of slot i of f(r) (q_j - q_i), f(r) = 24 r^-8 - 48 r^-14 + 8 C2,
 // the force on i (fcalculator.cc:263-277 without the dt factor).
-__device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const double4_32a *__restrict__ pos, int i) {
+// `list`/`counts` is the inner (pruned) list in an ordinary step and the outer
+// list for a stand-alone force evaluation.  With PRUNE the outer list is
+// walked and every entry within the prune radius is copied to the inner row
+// of slot i (d.pl); *kept receives the new row length.
+template <bool PRUNE>
+__device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const double4_32a *__restrict__ pos, int i,
+                                              const uint32_t *__restrict__ list, const int *__restrict__ counts,
+                                              int *kept) {
   const double4_32a qi = pos[i];
   const CellPos cp = cell_pos(g, d.cell[i]);
-  const int cnt = d.ncount[i];
-  const uint32_t *row = d.nl + i;
+  const int cnt = counts[i];
+  const uint32_t *row = list + i;
+  const double thr = (double)g.prune_thr2;
+  int m = 0;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int k = 0; k < cnt; k++) {
     const uint32_t e = __ldg(row + (size_t)k * g.stride);
@@ -84,6 +93,7 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
     if (cp.edge) apply_image(g, cp, e, qj);
     const double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
     const double r2 = dx * dx + dy * dy + dz * dz;
+    if (PRUNE && r2 <= thr) d.pl[(size_t)(m++) * g.stride + i] = e;
     if (r2 <= g.rc2) {
       const double inv = rcp_hh3(r2);
       const double i6 = inv * inv * inv;
@@ -93,13 +103,17 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
       fz = fma(df, dz, fz);
     }
   }
+  if (PRUNE) *kept = m;
   return make_double3(fx, fy, fz);
 }
 
 // Mixed form of force_fp64 on home-cell-local float positions.  The offset
 // between the home cells of i and j is ox*w + s*(L - nc*w) per axis, s the
 // periodic wrap of the stencil step.
-__device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i) {
+template <bool PRUNE>
+__device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
+                                               const uint32_t *__restrict__ list, const int *__restrict__ counts,
+                                               int *kept) {
   const float4 li = loc[i];
   const CellPos cp = cell_pos(g, d.cell[i]);
   const float mx0 = -g.w32[0] - (cp.cx == 0 ? g.dl32[0] : 0.0f), px0 = g.w32[0] + (cp.cx == g.nc[0] - 1 ? g.dl32[0] : 0.0f);
@@ -109,17 +123,19 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
   const float mxl = mx0 - li.x, pxl = px0 - li.x, zxl = -li.x;
   const float myl = mx1 - li.y, pyl = px1 - li.y, zyl = -li.y;
   const float mzl = mx2 - li.z, pzl = px2 - li.z, zzl = -li.z;
-  const int cnt = d.ncount[i];
-  const uint32_t *row = d.nl + i;
+  const int cnt = counts[i];
+  const uint32_t *row = list + i;
   const size_t stride = (size_t)g.stride;
   float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-  const float rc2 = g.rc2f, c2x8 = g.c2x8f;
+  const float rc2 = g.rc2f, c2x8 = g.c2x8f, thr = g.prune_thr2;
+  int m = 0;
   auto pair = [&](uint32_t e, const float4 &lj) {
     const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
     const float dx = lj.x + (ox == 0 ? mxl : (ox == 2 ? pxl : zxl));
     const float dy = lj.y + (oy == 0 ? myl : (oy == 2 ? pyl : zyl));
     const float dz = lj.z + (oz == 0 ? mzl : (oz == 2 ? pzl : zzl));
     const float r2 = dx * dx + dy * dy + dz * dz;
+    if (PRUNE && r2 <= thr) d.pl[(size_t)(m++) * stride + i] = e;
     if (r2 <= rc2) {
       float inv;
       asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
@@ -147,6 +163,7 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
     const uint32_t e = __ldg(row + (size_t)k * stride);
     pair(e, __ldg(loc + (e & kJMask)));
   }
+  if (PRUNE) *kept = m;
   return make_double3((double)sx + (double)cx, (double)sy + (double)cy, (double)sz + (double)cz);
 }
 
@@ -196,8 +213,17 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
   const double4_32a *qm = d.q_mid[par];
   double4_32a *qn = d.q_mid[par ^ 1];
   double ke = 0.0;
+  // inner-list re-selection: the same for the whole grid this step
+  const bool prune = f->prune_now != 0;
+  int kept = 0;
   if (active) {
-    const double3 F = MIXED ? force_mixed(g, d, d.loc[par], i) : force_fp64(g, d, qm, i);
+    double3 F;
+    if (prune)
+      F = MIXED ? force_mixed<true>(g, d, d.loc[par], i, d.nl, d.ncount, &kept)
+                : force_fp64<true>(g, d, qm, i, d.nl, d.ncount, &kept);
+    else
+      F = MIXED ? force_mixed<false>(g, d, d.loc[par], i, d.pl, d.pcount, nullptr)
+                : force_fp64<false>(g, d, qm, i, d.pl, d.pcount, nullptr);
     double4_32a p = d.p[i];
     if (THERMO == MDG_NOSEHOOVER) {
       const double e1 = f->exp1;
@@ -227,18 +253,31 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
     q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, g.dt2));
     const double4_32a qb = d.q_build[i];
     const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
+    // displacement since the build in float: the new home-cell-local position
+    // (qf holds the local position at the build) and the inner-list test
+    const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
+    const float4 lb = d.qf[i];
+    const float4 ln = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
+    d.loc[par ^ 1][i] = ln;
     if (MIXED) {
-      // displacement since the build in float: the expiry test and the new
-      // home-cell-local position (qf holds the local position at the build)
-      const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
       if (fx * fx + fy * fy + fz * fz > (float)g.half_margin2 || !(fx == fx && fy == fy && fz == fz))
         d.flags->rebuild = 1;
-      const float4 lb = d.qf[i];
-      d.loc[par ^ 1][i] = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
     } else {
       if (ux * ux + uy * uy + uz * uz > g.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
         d.flags->rebuild = 1;
     }
+    // prune reference: the positions of this force evaluation when the
+    // inner list was re-selected now, else those of the last selection
+    float4 lp;
+    if (prune) {
+      lp = d.loc[par][i];
+      d.loc_p[i] = lp;
+      d.pcount[i] = kept;
+    } else {
+      lp = d.loc_p[i];
+    }
+    const float vx = ln.x - lp.x, vy = ln.y - lp.y, vz = ln.z - lp.z;
+    if (vx * vx + vy * vy + vz * vz > g.half_prune2) d.flags->prune_next = 1;
     d.p[i] = p;
     d.q_end[i] = qe;
     qn[i] = q1;
@@ -249,6 +288,12 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
     __shared__ double sh[kStepThreads / 32];
     const double t = block_sum(ke, sh);
     if (threadIdx.x == 0) d.partials[blockIdx.x] = t;
+  }
+  if (prune) {  // inner-list size for the statistics (uniform branch)
+    unsigned long long v = (unsigned long long)kept;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(&d.flags->inner_pairs, v);
   }
 }
 
@@ -345,7 +390,8 @@ template <int MIXED>
 __global__ void __launch_bounds__(kStepThreads) k_forces(Geom g, Dev d, const float4 *loc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n) return;
-  const double3 F = MIXED ? force_mixed(g, d, loc, i) : force_fp64(g, d, d.q_end, i);
+  const double3 F = MIXED ? force_mixed<false>(g, d, loc, i, d.nl, d.ncount, nullptr)
+                          : force_fp64<false>(g, d, d.q_end, i, d.nl, d.ncount, nullptr);
   d.io4[d.id[i]] = make_double4_32a(F.x, F.y, F.z, 0.0);
 }
 

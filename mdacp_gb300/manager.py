@@ -28,7 +28,7 @@ def _as4(x):
 class MDManager:
     def __init__(self, box, capacity=None, cutoff=3.0, margin=0.3, dt=0.001, precision="fp64",
                  thermostat="nve", temperature=1.0, gamma=0.1, tau=0.1, seed=1, langevin_half_drift_compat=True,
-                 list_capacity=0, device=0, use_graphs=True, n=None):
+                 list_capacity=0, device=0, use_graphs=True, n=None, prune_buffer=None):
         self.lib = native.load()
         prm = native.Params()
         self.lib.mdg_params_default(ctypes.byref(prm))
@@ -44,6 +44,8 @@ class MDManager:
         prm.list_capacity = int(list_capacity)
         prm.device = int(device)
         prm.use_graphs = 1 if use_graphs else 0
+        if prune_buffer is not None:
+            prm.prune_buffer = float(prune_buffer)
         self.params = prm
         self.L = np.array(prm.box[:])
         h = ctypes.c_void_p()
@@ -163,4 +165,4 @@ class MDManager:
         return {"steps": s.steps, "rebuilds": s.rebuilds, "list_capacity": s.list_capacity,
                 "max_neighbours": s.max_neighbours, "listed_pairs": s.listed_pairs, "cells": tuple(s.cells),
                 "particles": s.particles, "zeta": s.zeta, "elapsed_ms": s.elapsed_ms,
-                "kernel_launches": s.kernel_launches}
+                "kernel_launches": s.kernel_launches, "inner_pairs": s.inner_pairs, "prunes": s.prunes}

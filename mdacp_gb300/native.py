@@ -22,14 +22,15 @@ class Params(ctypes.Structure):
                 ("thermostat", ctypes.c_int32), ("langevin_half_drift_compat", ctypes.c_int32),
                 ("temperature", ctypes.c_double), ("gamma", ctypes.c_double), ("tau", ctypes.c_double),
                 ("seed", ctypes.c_uint64), ("list_capacity", ctypes.c_int32), ("device", ctypes.c_int32),
-                ("use_graphs", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("use_graphs", ctypes.c_int32), ("reserved", ctypes.c_int32), ("prune_buffer", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int64), ("rebuilds", ctypes.c_int64), ("list_capacity", ctypes.c_int32),
                 ("max_neighbours", ctypes.c_int32), ("listed_pairs", ctypes.c_int64),
                 ("cells", ctypes.c_int32 * 3), ("particles", ctypes.c_int32), ("zeta", ctypes.c_double),
-                ("elapsed_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64)]
+                ("elapsed_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
+                ("inner_pairs", ctypes.c_int64), ("prunes", ctypes.c_int64)]
 
 
 # Every exported symbol of include/mdg.h, with (restype, argtypes).

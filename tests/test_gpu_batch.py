@@ -1,0 +1,89 @@
+"""Batched replicas: every box of a batch against the oracle run on that box alone.
+
+Boxes of uneven size (500..2000 atoms here), density 0.3..0.9 (so some boxes
+have only two cells per side) and temperature 0.7..1.5, rc 2.5, margin 0.4,
+dt 0.002.  FP64: per-box observables rtol 1e-10 after 100 steps; mixed: within
+1e-5 of FP64; overflow regrowth; autotuner leaves the state unchanged.
+"""
+import numpy as np
+import pytest
+
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+
+RC, MARGIN, DT = 2.5, 0.4, 0.002
+
+
+def _boxes(nbox=12, seed=3):
+    """nbox drawn boxes plus one 500-atom box at density 0.9 (L = 8.2: two cells per side)."""
+    from mdacp_gb300.batch import make_replicas
+    return make_replicas(nbox, seed=seed, n_range=(500, 2000)) + make_replicas(
+        1, seed=seed + 1000, n_range=(500, 500), rho_range=(0.9, 0.9))
+
+
+def _oracle_obs(boxes, steps):
+    out = []
+    for q, p, L in boxes:
+        s = port.System(q, p, L, rc=RC, margin=MARGIN, dt=DT)
+        s.make_pairlist()
+        s.calculate(steps)
+        out.append(s.observe_raw())
+    return np.array(out)
+
+
+def test_batch_fp64_matches_oracle_per_box():
+    from mdacp_gb300.batch import Batch
+    boxes = _boxes()
+    assert any(L[0] < 3 * (RC + MARGIN) for _, _, L in boxes)   # two cells per side occurs
+    b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT)
+    b.calculate(100)
+    np.testing.assert_allclose(b.observe_raw(), _oracle_obs(boxes, 100), rtol=1e-10, atol=1e-10)
+    st = b.stats()
+    assert st["steps"] == 100 and st["rebuilds"] >= len(boxes)
+
+
+def test_batch_mixed_close_to_fp64():
+    from mdacp_gb300.batch import Batch
+    boxes = _boxes(8, seed=5)
+    a = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision="fp64")
+    m = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision="mixed")
+    a.calculate(50)
+    m.calculate(50)
+    np.testing.assert_allclose(m.observe_raw(), a.observe_raw(), rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("shape", [(128, 1, 4), (256, 2, 2), (512, 4, 1)])
+def test_batch_shapes_agree(shape):
+    from mdacp_gb300.batch import Batch
+    boxes = _boxes(6, seed=7)
+    b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT)
+    b.set_shape(*shape)
+    b.calculate(60)
+    np.testing.assert_allclose(b.observe_raw(), _oracle_obs(boxes, 60), rtol=1e-10, atol=1e-10)
+
+
+def test_batch_overflow_regrows_and_catches_up():
+    from mdacp_gb300.batch import Batch
+    boxes = _boxes(6, seed=9)
+    b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, list_capacity=8)
+    b.calculate(40)
+    assert b.stats()["list_capacity"] > 8
+    np.testing.assert_allclose(b.observe_raw(), _oracle_obs(boxes, 40), rtol=1e-10, atol=1e-10)
+
+
+def test_autotuner_restores_state():
+    from mdacp_gb300.batch import Batch
+    boxes = _boxes(6, seed=11)
+    b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT)
+    b.calculate(10)
+    before = [x.copy() for pair in b.state() for x in pair]
+    t, lanes, c = b.tune(trial_steps=4)
+    assert t in (128, 256, 512) and lanes in (1, 2, 4) and c in (1, 2, 4)
+    after = [x for pair in b.state() for x in pair]
+    for u, v in zip(before, after):
+        assert np.array_equal(u, v)
+    b.calculate(30)
+    np.testing.assert_allclose(b.observe_raw(), _oracle_obs([(q, p, L) for (q, p), (_, _, L) in
+                                                             zip([(x, y) for x, y in zip(before[0::2], before[1::2])],
+                                                                 boxes)], 30), rtol=1e-10, atol=1e-10)

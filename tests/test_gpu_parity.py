@@ -63,12 +63,14 @@ def test_observables_match_reference_expression():
     np.testing.assert_allclose(o, orf, rtol=1e-13)
 
 
-@pytest.mark.parametrize("use_graphs", [True, False])
-def test_nve_trace_100_steps(use_graphs):
+@pytest.mark.parametrize("use_graphs,prune", [(True, None), (False, None), (True, 0.0), (True, 0.02)])
+def test_nve_trace_100_steps(use_graphs, prune):
+    """prune: inner-list buffer (None = default 0.1; 0 = walk every listed pair;
+    0.02 = re-select every few steps)."""
     q, p, L = liquid_like(0.5, 20, seed=9)
     ref = port.System(q, p, L, rc=RC, margin=MARGIN, dt=0.001)
     ref.make_pairlist()
-    m = _gpu(L, len(q), dt=0.001, use_graphs=use_graphs)
+    m = _gpu(L, len(q), dt=0.001, use_graphs=use_graphs, prune_buffer=prune)
     m.set_state(q, p)
     m.make_pairlist()
     rows, rrows = [m.observe()], [ref.observe()]
@@ -83,7 +85,10 @@ def test_nve_trace_100_steps(use_graphs):
     qr, pr = ref.state()
     dq = np.abs((qg - qr + L / 2) % L - L / 2).max()
     assert dq < 1e-10 and np.abs(pg - pr).max() < 1e-10
-    assert m.stats()["steps"] == 100
+    st = m.stats()
+    assert st["steps"] == 100
+    if prune == 0.02:
+        assert st["prunes"] > st["rebuilds"] and st["inner_pairs"] < st["listed_pairs"]
 
 
 def test_mixed_force_error():
