@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--impl", default="mdg", choices=["mdg", "reference"])
     ap.add_argument("--cells", type=int, default=100, help="FCC unit cells per side (100 -> 4M atoms)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--workload", default="nve4m", choices=["nve4m", "langevin16m", "batch1024", "adjoint4k"],
+                    help="nve4m: the headline (4M atoms NVE); langevin16m: 160^3 FCC Langevin NVT; "
+                         "batch1024: 1024 replica boxes; adjoint4k: 4000-atom trajectory gradient")
     return ap.parse_args()
 
 
@@ -313,8 +316,112 @@ def run_mine(args):
     d.close()
 
 
+def base_line(metric, value, n_gpus, K, W, ms, config, dtype):
+    return {"metric": metric, "value": value, "unit": UNIT, "n_gpus": n_gpus, "steps": K, "warmup": W,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic", "config": config}
+
+
+def run_langevin16m(args):
+    """Langevin NVT, 160^3 FCC = 16,384,000 atoms, density 0.5, T 0.9, gamma 1, dt 0.005."""
+    from mdacp_gb300.manager import MDManager
+    cells = 160 if args.cells == 100 else args.cells
+    from mdacp_gb300 import lattice
+    q, L = lattice.fcc_cube(cells, DENSITY)
+    p = lattice.maxwell(len(q), 1.0, 1)
+    n = len(q)
+    K, W = args.steps if args.steps != 1000 else 200, max(3, args.warmup)
+    res = {}
+    clk = Clocks(0)
+    clocks = None
+    for prec in ("mixed", "fp64"):
+        m = MDManager(L, capacity=n, cutoff=RC, margin=MARGIN, dt=0.005, precision=prec, thermostat="langevin",
+                      temperature=0.9, gamma=1.0, seed=12345)
+        m.set_state(q, p)
+        m.make_pairlist()
+        m.calculate(W)
+        if prec == "mixed":
+            clk.start()
+        m.calculate(K)
+        st = m.stats()
+        if prec == "mixed":
+            clocks = clk.stop()
+        res[prec] = {"ms": st["elapsed_ms"], "rebuilds": st["rebuilds"], "prunes": st["prunes"],
+                     "T_end": float(m.observe()[0]), "pairs_per_atom": st["listed_pairs"] / n}
+        m.close()
+    cfg = {"workload": "Langevin NVT %d atoms (%d^3 FCC), rho 0.5, T 0.9, gamma 1.0, dt 0.005, rc 2.5, margin 0.5"
+           % (n, cells), "atoms": n, "l2": "inputs larger than L2 (no flush)"}
+    v = n * K / (res["mixed"]["ms"] * 1e-3)
+    line = base_line("LJ atom-steps/s, 16.4M atoms Langevin NVT: mixed vs FP64 on 1 GB300", v, 1, K, W,
+                     res["mixed"]["ms"] / K, cfg, "f32 pair force / f64 accumulate-integrate")
+    line.update({"fp64": {"value": n * K / (res["fp64"]["ms"] * 1e-3), "ms_per_step": res["fp64"]["ms"] / K,
+                          "rebuilds": res["fp64"]["rebuilds"], "T_end": res["fp64"]["T_end"]},
+                 "mixed": res["mixed"], "clocks": clocks})
+    print(json.dumps(line), flush=True)
+
+
+def run_batch1024(args):
+    """1024 replica boxes: N ~ U[500, 8000], density ~ U[0.3, 0.9], T ~ U[0.7, 1.5], rc 2.5, margin 0.4, dt 0.002."""
+    from mdacp_gb300.batch import Batch, make_replicas
+    boxes = make_replicas(1024, seed=1)
+    n = sum(len(b[0]) for b in boxes)
+    K, W = args.steps if args.steps != 1000 else 500, max(3, args.warmup)
+    res = {}
+    for prec in ("mixed", "fp64"):
+        b = Batch(boxes, cutoff=2.5, margin=0.4, dt=0.002, precision=prec)
+        shape = b.tune(trial_steps=10)
+        b.calculate(W)
+        b.calculate(K)
+        st = b.stats()
+        res[prec] = {"ms": st["elapsed_ms"], "shape": {"threads": shape[0], "lanes_per_particle": shape[1],
+                                                        "ctas_per_sm": shape[2]},
+                     "rebuilds": st["rebuilds"], "launches_per_step": 1}
+        b.close()
+    cfg = {"workload": "1024 replica boxes, %d atoms total, N~U[500,8000], rho~U[0.3,0.9], T~U[0.7,1.5], "
+                       "rc 2.5, margin 0.4, dt 0.002" % n, "atoms": n, "boxes": 1024}
+    v = n * K / (res["mixed"]["ms"] * 1e-3)
+    line = base_line("LJ atom-steps/s, 1024 batched replicas: mixed vs FP64 on 1 GB300", v, 1, K, W,
+                     res["mixed"]["ms"] / K, cfg, "f32 pair force / f64 accumulate-integrate")
+    line.update({"fp64": {"value": n * K / (res["fp64"]["ms"] * 1e-3), "ms_per_step": res["fp64"]["ms"] / K,
+                          "shape": res["fp64"]["shape"]}, "mixed": res["mixed"]})
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint4k(args):
+    """Gradient of mean PE and of mean pressure, 4000 atoms at density 0.8, 200 steps, checkpoint every 20."""
+    from mdacp_gb300 import lattice
+    from mdacp_gb300.adjoint import Adjoint
+    q, L = lattice.fcc_cube(10, 0.8)
+    p = lattice.maxwell(len(q), 1.0, 1)
+    n = len(q)
+    out = {}
+    for obj in ("pe", "pressure"):
+        a = Adjoint(L, n, steps=200, checkpoint_every=20, dt=0.002, margin=2.0, objective=obj)
+        a.forward(q, p)
+        a.backward()
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            a.forward(q, p)
+            a.backward()
+        dt = (time.perf_counter() - t0) / reps
+        out[obj] = {"ms_per_gradient": dt * 1e3}
+        a.close()
+    # one gradient = 200 forward steps + 200 recomputed steps + 200 reverse steps
+    v = n * 200 / (out["pe"]["ms_per_gradient"] * 1e-3)
+    cfg = {"workload": "adjoint, 4000 atoms (10^3 FCC), rho 0.8, T 1, dt 0.002, 200 steps, checkpoint every 20",
+           "atoms": n}
+    line = base_line("LJ adjoint: trajectory atom-steps/s per gradient (forward+backward), 4000 atoms", v, 1, 200,
+                     1, out["pe"]["ms_per_gradient"] / 200, cfg, "f64")
+    line.update({"gradients": out})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.impl == "mdg" and args.workload != "nve4m":
+        {"langevin16m": run_langevin16m, "batch1024": run_batch1024, "adjoint4k": run_adjoint4k}[args.workload](args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
