@@ -208,7 +208,7 @@ int halt_error(mdg_handle *h) {
 int ensure_list(mdg_handle *h, bool force) {
   for (int attempt = 0; attempt < 16; attempt++) {
     if (force) mdg::launch_set_rebuild(h->d, h->stream);
-    mdg::launch_rebuild(h->g, h->d, h->par, h->num_sms, h->stream, false, false);
+    mdg::launch_rebuild(h->g, h->d, h->par, h->num_sms, h->stream, false, false, false);
     h->launches += mdg::kRebuildKernels + (force ? 1 : 0);
     int rc = read_flags(h);
     if (rc) return rc;
@@ -223,24 +223,96 @@ int ensure_list(mdg_handle *h, bool force) {
 
 int kernels_per_step(const mdg_handle *h) { return mdg::kRebuildKernels + mdg::step_kernels(h->prm.thermostat); }
 
-// Optional events around the step kernel (profiled runs only).
-void enqueue_step(mdg_handle *h, int par, cudaEvent_t before = nullptr, cudaEvent_t after = nullptr) {
-  mdg::launch_rebuild(h->g, h->d, par, h->num_sms, h->stream, true, lang_on(h) != 0);
+// One step as plain launches: the rebuild sequence (no-ops unless due) and
+// the step kernel deciding its variant on the device (pmode 0), or both
+// variants in turn with optional events around them (pmode 3, profiled runs).
+void enqueue_step(mdg_handle *h, int par, int pmode = 0, cudaEvent_t before = nullptr, cudaEvent_t after = nullptr) {
+  mdg::launch_rebuild(h->g, h->d, par, h->num_sms, h->stream, true, lang_on(h) != 0, true);
   if (before) cudaEventRecord(before, h->stream);
   mdg::launch_step(h->g, h->d, par, h->prm.thermostat, h->prm.langevin_half_drift_compat, h->prm.precision,
-                   h->stream);
+                   h->stream, pmode);
   if (after) cudaEventRecord(after, h->stream);
 }
 
-int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps) {
-  cudaGraph_t graph = nullptr;
-  MDG_CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  for (int k = 0; k < nsteps; k++) enqueue_step(h, par ^ (k & 1));
-  MDG_CK(cudaStreamEndCapture(h->stream, &graph));
-  cudaError_t e = cudaGraphInstantiate(out, graph, 0);
-  cudaGraphDestroy(graph);
-  if (e != cudaSuccess) return fail(h, MDG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+// Appends what `enqueue` launches on the handle's stream to graph g after
+// node `dep` (none when dep is null); *last receives the final node.
+template <class F>
+int append_captured(mdg_handle *h, cudaGraph_t g, const cudaGraphNode_t *dep, F enqueue, cudaGraphNode_t *last) {
+  MDG_CK(cudaStreamBeginCaptureToGraph(h->stream, g, dep, nullptr, dep ? 1 : 0, cudaStreamCaptureModeThreadLocal));
+  enqueue();
+  cudaStreamCaptureStatus st;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(h->stream, &st, nullptr, nullptr, &deps, nullptr, &nd);
+  cudaGraphNode_t tail = (e == cudaSuccess && nd == 1) ? deps[0] : nullptr;
+  cudaGraph_t out = nullptr;
+  MDG_CK(cudaStreamEndCapture(h->stream, &out));
+  if (e != cudaSuccess || !tail) return fail(h, MDG_ERR_CUDA, "graph capture did not end in one node");
+  if (last) *last = tail;
   return MDG_OK;
+}
+
+// Adds a conditional node (IF with one body, or SWITCH with `bodies` bodies)
+// after `dep` and fills each body with what `fill(k)` launches.
+template <class F>
+int add_conditional(mdg_handle *h, cudaGraph_t g, cudaGraphNode_t dep, cudaGraphConditionalHandle cond,
+                    cudaGraphConditionalNodeType type, int bodies, F fill, cudaGraphNode_t *node) {
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+  np.conditional.handle = cond;
+  np.conditional.type = type;
+  np.conditional.size = (unsigned)bodies;
+  MDG_CK(cudaGraphAddNode(node, g, &dep, nullptr, 1, &np));
+  for (int k = 0; k < bodies; k++) {
+    cudaGraph_t body = np.conditional.phGraph_out[k];
+    MDG_CK(cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    fill(k);
+    cudaGraph_t out = nullptr;
+    MDG_CK(cudaStreamEndCapture(h->stream, &out));
+  }
+  return MDG_OK;
+}
+
+// A graph of nsteps steps starting at parity par.  Per step: a one-thread
+// prelude (counters, inner-list hand-over) that sets the rebuild condition;
+// IF(rebuild) { wrap, bin, reorder, build }; a one-thread select that sets
+// the variant; SWITCH(variant) { ordinary step | re-selecting step }.  Steps
+// without a rebuild therefore run three kernels.
+int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps) {
+  cudaGraph_t g = nullptr;
+  MDG_CK(cudaGraphCreate(&g, 0));
+  cudaGraphNode_t last = nullptr;
+  int rc = MDG_OK;
+  const int lang = lang_on(h) != 0;
+  for (int k = 0; k < nsteps && rc == MDG_OK; k++) {
+    const int p = par ^ (k & 1);
+    cudaGraphConditionalHandle c_rb = 0, c_var = 0;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&c_rb, g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&c_var, g, 2, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) {
+      rc = fail(h, MDG_ERR_CUDA, std::string("cudaGraphConditionalHandleCreate: ") + cudaGetErrorString(e));
+      break;
+    }
+    cudaGraphNode_t pre = nullptr, cond = nullptr, sel = nullptr, sw = nullptr;
+    rc = append_captured(h, g, last ? &last : nullptr, [&] { mdg::launch_prelude(h->d, lang, c_rb, h->stream); }, &pre);
+    if (rc) break;
+    rc = add_conditional(h, g, pre, c_rb, cudaGraphCondTypeIf, 1, [&](int) {
+      mdg::launch_rebuild(h->g, h->d, p, h->num_sms, h->stream, false, false, true);
+    }, &cond);
+    if (rc) break;
+    rc = append_captured(h, g, &cond, [&] { mdg::launch_select(h->d, c_var, h->stream); }, &sel);
+    if (rc) break;
+    rc = add_conditional(h, g, sel, c_var, cudaGraphCondTypeSwitch, 2, [&](int variant) {
+      mdg::launch_step(h->g, h->d, p, h->prm.thermostat, h->prm.langevin_half_drift_compat, h->prm.precision,
+                       h->stream, variant == 0 ? 1 : 2);
+    }, &sw);
+    last = sw;
+  }
+  if (rc == MDG_OK) {
+    cudaError_t e = cudaGraphInstantiate(out, g, 0);
+    if (e != cudaSuccess) rc = fail(h, MDG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  }
+  cudaGraphDestroy(g);
+  return rc;
 }
 
 int enqueue_steps(mdg_handle *h, int nsteps) {
@@ -262,7 +334,6 @@ int enqueue_steps(mdg_handle *h, int nsteps) {
     }
     while (left >= 2) {
       MDG_CK(cudaGraphLaunch(h->gx_pair[par], h->stream));
-      h->launches += 2 * kernels_per_step(h);
       left -= 2;
     }
   }
@@ -272,7 +343,6 @@ int enqueue_steps(mdg_handle *h, int nsteps) {
       if (rc) return rc;
     }
     MDG_CK(cudaGraphLaunch(h->gx_one[par], h->stream));
-    h->launches += kernels_per_step(h);
     par ^= 1;
   }
   h->par = par;
@@ -491,11 +561,15 @@ int mdg_calculate(mdg_handle *h, int32_t nsteps) {
   long long done = 0;
   for (int attempt = 0; attempt < 64 && done < nsteps; attempt++) {
     const unsigned long long before = (unsigned long long)h->steps_host;
+    const unsigned long long rebuilds0 = h->hflags->rebuilds;
     rc = enqueue_steps(h, (int)(nsteps - done));
     if (rc) return rc;
     rc = read_flags(h);
     if (rc) return rc;
     long long completed = (long long)(h->hflags->steps - before);
+    if (h->prm.use_graphs)  // executed kernels: prelude, select, step (+ NH), and the rebuild bodies that ran
+      h->launches += completed * (2 + mdg::step_kernels(h->prm.thermostat)) +
+                     (long long)(h->hflags->rebuilds - rebuilds0) * mdg::kRebuildKernels;
     if (h->hflags->halt == 0) {
       done += completed;
       h->steps_host = (long long)h->hflags->steps;
@@ -537,8 +611,8 @@ int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms
     const unsigned long long before = (unsigned long long)h->steps_host;
     const int m = (int)((nsteps - done) < kChunk ? (nsteps - done) : kChunk);
     for (int k = 0; k < m; k++) {
-      enqueue_step(h, h->par, ev[2 * k], ev[2 * k + 1]);
-      h->launches += kernels_per_step(h);
+      enqueue_step(h, h->par, 3, ev[2 * k], ev[2 * k + 1]);
+      h->launches += kernels_per_step(h) + 1;
       h->par ^= 1;
     }
     status = read_flags(h);

@@ -53,23 +53,26 @@ __device__ int block_exclusive_scan(int v, int *total) {
   return warp_off + x - v;
 }
 
+// Start of a step: step and Langevin counters; the inner-list re-selection
+// requested by the last step (or by a rebuild outside a step) is handed to
+// this step's kernel.
+__device__ __forceinline__ void start_step(DevFlags *f, int lang_step) {
+  f->steps += 1;
+  if (lang_step) f->lang += 1;
+  f->prune_now = f->prune_next;
+  f->prune_next = 0;
+  if (f->prune_now) {
+    f->prunes += 1;
+    f->inner_pairs = 0;
+  }
+}
+
 // Wraps q_end into the box with the reference rule (one +-L per component),
 // bins it and counts cell occupancy.  Thread 0 also advances the step and
 // Langevin counters of a step that is starting.
 __global__ void k_wrap_bin(Geom g, Dev d, int count_step, int lang_step) {
   DevFlags *f = d.flags;
-  if (count_step && blockIdx.x == 0 && threadIdx.x == 0 && f->halt == 0) {
-    f->steps += 1;
-    if (lang_step) f->lang += 1;
-    // inner-list re-selection requested by the last step (or by a rebuild
-    // outside a step) happens in this step's kernel
-    f->prune_now = f->prune_next;
-    f->prune_next = 0;
-    if (f->prune_now) {
-      f->prunes += 1;
-      f->inner_pairs = 0;
-    }
-  }
+  if (count_step && blockIdx.x == 0 && threadIdx.x == 0 && f->halt == 0) start_step(f, lang_step);
   if (rebuild_off(f)) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
     double4_32a q = d.q_end[i];
@@ -228,6 +231,17 @@ __global__ void k_set_rebuild(DevFlags *f) {
   if (f->halt == 0) f->rebuild = 1;
 }
 
+// Graph path: the step-start bookkeeping of k_wrap_bin, and the condition that
+// runs the rebuild body.
+__global__ void k_prelude(DevFlags *f, int lang_step, cudaGraphConditionalHandle rebuild_cond) {
+  if (f->halt == 0) start_step(f, lang_step);
+  cudaGraphSetConditional(rebuild_cond, (f->halt == 0 && f->rebuild) ? 1u : 0u);
+}
+
+__global__ void k_select(DevFlags *f, cudaGraphConditionalHandle variant_cond) {
+  cudaGraphSetConditional(variant_cond, f->halt != 0 ? 2u : (f->prune_now ? 1u : 0u));
+}
+
 }  // namespace
 
 // Declared in mdg_list.cu.
@@ -235,8 +249,16 @@ void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s,
 
 void launch_set_rebuild(const Dev &d, cudaStream_t s) { k_set_rebuild<<<1, 1, 0, s>>>(d.flags); }
 
+void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle rebuild_cond, cudaStream_t s) {
+  k_prelude<<<1, 1, 0, s>>>(d.flags, lang_step, rebuild_cond);
+}
+
+void launch_select(const Dev &d, cudaGraphConditionalHandle variant_cond, cudaStream_t s) {
+  k_select<<<1, 1, 0, s>>>(d.flags, variant_cond);
+}
+
 void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cudaStream_t s, bool count_step,
-                    bool lang_step) {
+                    bool lang_step, bool in_step) {
   const int threads = 256;
   int grid = (g.n + threads - 1) / threads;
   const int cap = num_sms * 8;
@@ -253,7 +275,7 @@ void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cud
   k_cell_sort<<<cgrid, threads, 0, s>>>(g, d);
   k_reorder<<<grid, threads, 0, s>>>(g, d);
   k_finalize<<<grid, threads, 0, s>>>(g, d, q_mid_dst);
-  launch_build_list(g, d, num_sms, s, count_step);
+  launch_build_list(g, d, num_sms, s, in_step);
 }
 
 }  // namespace mdg

@@ -108,9 +108,17 @@ constexpr int kRebuildKernels = 11;
 inline int step_kernels(int thermostat) { return thermostat == MDG_NOSEHOOVER ? 2 : 1; }
 
 // host-side launchers (stream-ordered; none synchronises)
+// count_step: the first kernel also starts a step (counters, inner-list
+// hand-over); in_step: the rebuild belongs to the step about to run.
 void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cudaStream_t s, bool count_step,
-                    bool lang_step);
-void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compat, int mixed, cudaStream_t s);
+                    bool lang_step, bool in_step);
+void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compat, int mixed, cudaStream_t s,
+                 int pmode);
+// Graph path: step start (counters, hand-over) and the rebuild condition, then
+// the choice of step variant after the rebuild (0 ordinary, 1 re-selecting,
+// 2 none when halted).
+void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle rebuild_cond, cudaStream_t s);
+void launch_select(const Dev &d, cudaGraphConditionalHandle variant_cond, cudaStream_t s);
 void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s);
 void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s);
 void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s);

@@ -204,17 +204,22 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return t;
 }
 
-template <int THERMO, int COMPAT, int MIXED>
+// PMODE: 0 = decide from flags->prune_now in the kernel (both paths compiled);
+// 1 = ordinary step only, 2 = re-selecting step only (each a no-op when the
+// flag says otherwise, so the graph path can run the lighter variant).
+template <int THERMO, int COMPAT, int MIXED, int PMODE>
 __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
   const DevFlags *f = d.flags;
   if (f->halt != 0) return;
+  if (PMODE == 1 && f->prune_now != 0) return;
+  if (PMODE == 2 && f->prune_now == 0) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool active = i < g.n;
   const double4_32a *qm = d.q_mid[par];
   double4_32a *qn = d.q_mid[par ^ 1];
   double ke = 0.0;
   // inner-list re-selection: the same for the whole grid this step
-  const bool prune = f->prune_now != 0;
+  const bool prune = PMODE == 2 ? true : (PMODE == 1 ? false : f->prune_now != 0);
   int kept = 0;
   if (active) {
     double3 F;
@@ -450,19 +455,34 @@ inline int blocks_for(int n) { return n > 0 ? (n + kStepThreads - 1) / kStepThre
 
 }  // namespace
 
-void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compat, int mixed, cudaStream_t s) {
+template <int T, int C, int M>
+void launch_step_variant(const Geom &g, const Dev &d, int par, int pmode, cudaStream_t s) {
   const int grid = blocks_for(g.n);
-#define MDG_STEP(T, C, M) k_step<T, C, M><<<grid, kStepThreads, 0, s>>>(g, d, par)
+  if (pmode == 0) k_step<T, C, M, 0><<<grid, kStepThreads, 0, s>>>(g, d, par);
+  if (pmode == 1 || pmode == 3) k_step<T, C, M, 1><<<grid, kStepThreads, 0, s>>>(g, d, par);
+  if (pmode == 2 || pmode == 3) k_step<T, C, M, 2><<<grid, kStepThreads, 0, s>>>(g, d, par);
+  if (T == MDG_NOSEHOOVER) k_nh_update<<<1, 1024, 0, s>>>(g, d, grid, 0);
+}
+
+// pmode: 0 one kernel deciding on the device; 1 / 2 only the ordinary / the
+// re-selecting variant (graph conditional bodies); 3 both variants in turn.
+void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compat, int mixed, cudaStream_t s,
+                 int pmode) {
   if (thermostat == MDG_LANGEVIN) {
-    if (compat) { if (mixed) MDG_STEP(MDG_LANGEVIN, 1, 1); else MDG_STEP(MDG_LANGEVIN, 1, 0); }
-    else { if (mixed) MDG_STEP(MDG_LANGEVIN, 0, 1); else MDG_STEP(MDG_LANGEVIN, 0, 0); }
+    if (compat) {
+      if (mixed) launch_step_variant<MDG_LANGEVIN, 1, 1>(g, d, par, pmode, s);
+      else launch_step_variant<MDG_LANGEVIN, 1, 0>(g, d, par, pmode, s);
+    } else {
+      if (mixed) launch_step_variant<MDG_LANGEVIN, 0, 1>(g, d, par, pmode, s);
+      else launch_step_variant<MDG_LANGEVIN, 0, 0>(g, d, par, pmode, s);
+    }
   } else if (thermostat == MDG_NOSEHOOVER) {
-    if (mixed) MDG_STEP(MDG_NOSEHOOVER, 0, 1); else MDG_STEP(MDG_NOSEHOOVER, 0, 0);
-    k_nh_update<<<1, 1024, 0, s>>>(g, d, grid, 0);
+    if (mixed) launch_step_variant<MDG_NOSEHOOVER, 0, 1>(g, d, par, pmode, s);
+    else launch_step_variant<MDG_NOSEHOOVER, 0, 0>(g, d, par, pmode, s);
   } else {
-    if (mixed) MDG_STEP(MDG_NVE, 0, 1); else MDG_STEP(MDG_NVE, 0, 0);
+    if (mixed) launch_step_variant<MDG_NVE, 0, 1>(g, d, par, pmode, s);
+    else launch_step_variant<MDG_NVE, 0, 0>(g, d, par, pmode, s);
   }
-#undef MDG_STEP
 }
 
 void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s) {
