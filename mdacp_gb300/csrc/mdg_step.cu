@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
     else
       F = MIXED ? force_mixed<false>(g, d, d.loc[par], i, d.pl, d.pcount, nullptr)
                 : force_fp64<false>(g, d, qm, i, d.pl, d.pcount, nullptr);
-    double4_32a p = d.p[i];
+    const double4_32a p_old = d.p[i];
+    double4_32a p = p_old;
     if (THERMO == MDG_NOSEHOOVER) {
       const double e1 = f->exp1;
       p.x *= e1; p.y *= e1; p.z *= e1; p.w *= e1;
@@ -245,7 +246,18 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
       p.y += (-g.gamma * p.y + g.hb_d * z[1]) * g.dt;
       p.z += (-g.gamma * p.z + g.hb_d * z[2]) * g.dt;
     }
-    const double4_32a q0 = qm[i];
+    // Mid-step position of this particle.  The mixed form gathers float
+    // positions only, so it does not keep q_mid: q_end + p dt/2 with the
+    // momentum of the previous step is exactly what that step computed.
+    double4_32a q0;
+    if (MIXED) {
+      q0 = d.q_end[i];
+      q0.x = __dadd_rn(q0.x, __dmul_rn(p_old.x, g.dt2));
+      q0.y = __dadd_rn(q0.y, __dmul_rn(p_old.y, g.dt2));
+      q0.z = __dadd_rn(q0.z, __dmul_rn(p_old.z, g.dt2));
+    } else {
+      q0 = qm[i];
+    }
     double4_32a qe = q0, q1;
     if (!(THERMO == MDG_LANGEVIN && COMPAT)) {
       qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, g.dt2));
@@ -285,7 +297,7 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
     if (vx * vx + vy * vy + vz * vz > g.half_prune2) d.flags->prune_next = 1;
     d.p[i] = p;
     d.q_end[i] = qe;
-    qn[i] = q1;
+    if (!MIXED) qn[i] = q1;
     if (THERMO == MDG_NOSEHOOVER)
       ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
   }
