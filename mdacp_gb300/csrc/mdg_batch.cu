@@ -78,13 +78,6 @@ __device__ __forceinline__ double rcp_hh3(double x) {
   return fma(y, fma(e, e, e), y);
 }
 
-__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x) {
-  const float t = s + x;
-  const float bp = t - s;
-  c += (s - (t - bp)) + (x - bp);
-  s = t;
-}
-
 __device__ __forceinline__ void cell_xyz(const BoxDesc &b, int c, int &cx, int &cy, int &cz) {
   cx = c % b.nc[0];
   const int t = c / b.nc[0];
@@ -237,7 +230,7 @@ __device__ void rebuild_box(const Params &P, const Dev &d, const BoxDesc &b, int
           const float offx = (float)ox * b.w32[0] + (float)sx * b.dl32[0];
           const int cc = (nz * b.nc[1] + ny) * b.nc[0] + nx;
           const int lo = s_start[cc], hi = s_start[cc + 1];
-          const uint32_t code = (uint32_t)((ox + 1) | ((oy + 1) << 2) | ((oz + 1) << 4)) << kJBits;
+          const uint32_t code = entry_pack(0, ox, oy, oz);
           const bool self_cell = (sx | sy | sz) == 0;
           const float fx = offx - fi.x, fy = offy - fi.y, fz = offz - fi.z;
           for (int j = lo; j < hi; j++) {
@@ -257,7 +250,7 @@ __device__ void rebuild_box(const Params &P, const Dev &d, const BoxDesc &b, int
               take = r2 <= P.sl2;
             }
             if (take) {
-              if (cnt < P.list_cap) d.nl[b.list_off + (long long)cnt * n + a] = (uint32_t)j | code;
+              if (cnt < P.list_cap) d.nl[b.list_off + (long long)cnt * n + a] = ((uint32_t)j << kCodeBits) | code;
               cnt++;
             }
           }
@@ -295,39 +288,39 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (MIXED) {
     const float4 li = d.loc[par][o + a];
-    const float mx0 = -b.w32[0] - (cx == 0 ? b.dl32[0] : 0.0f) - li.x, px0 = b.w32[0] + (cx == b.nc[0] - 1 ? b.dl32[0] : 0.0f) - li.x;
-    const float mx1 = -b.w32[1] - (cy == 0 ? b.dl32[1] : 0.0f) - li.y, px1 = b.w32[1] + (cy == b.nc[1] - 1 ? b.dl32[1] : 0.0f) - li.y;
-    const float mx2 = -b.w32[2] - (cz == 0 ? b.dl32[2] : 0.0f) - li.z, px2 = b.w32[2] + (cz == b.nc[2] - 1 ? b.dl32[2] : 0.0f) - li.z;
-    float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
+    const AxisQuad qx = axis_quad(b.w32[0], b.dl32[0], cx == 0, cx == b.nc[0] - 1, li.x, 1.0f);
+    const AxisQuad qy = axis_quad(b.w32[1], b.dl32[1], cy == 0, cy == b.nc[1] - 1, li.y, 0.25f);
+    const AxisQuad qz = axis_quad(b.w32[2], b.dl32[2], cz == 0, cz == b.nc[2] - 1, li.z, 0.0625f);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
     for (int k = lane; k < cnt; k += LPI) {
       const uint32_t e = __ldg(row + (long long)k * n);
-      const float4 lj = __ldg(d.loc[par] + o + (e & kJMask));
-      const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
-      const float dx = lj.x + (ox == 0 ? mx0 : (ox == 2 ? px0 : -li.x));
-      const float dy = lj.y + (oy == 0 ? mx1 : (oy == 2 ? px1 : -li.y));
-      const float dz = lj.z + (oz == 0 ? mx2 : (oz == 2 ? px2 : -li.z));
+      const float4 lj = __ldg(d.loc[par] + o + entry_slot(e));
+      const float tx = step_float(e, 0x03u, 8388609.0f), ty = step_float(e, 0x0Cu, 8388612.0f),
+                  tz = step_float(e, 0x30u, 8388624.0f);
+      const float dx = lj.x + fmaf(fmaf(qx.b, tx, qx.a), tx, qx.c);
+      const float dy = lj.y + fmaf(fmaf(qy.b, ty, qy.a), ty, qy.c);
+      const float dz = lj.z + fmaf(fmaf(qz.b, tz, qz.a), tz, qz.c);
       const float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 <= P.rc2f) {
-        float inv;
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
-        const float i6 = inv * inv * inv;
-        const float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + P.c2x8f;
-        two_sum_acc(sx, ex, df * dx);
-        two_sum_acc(sy, ey, df * dy);
-        two_sum_acc(sz, ez, df * dz);
-      }
+      float inv;
+      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+      const float i6 = inv * inv * inv;
+      float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + P.c2x8f;
+      df = r2 <= P.rc2f ? df : 0.0f;
+      sx = fmaf(df, dx, sx);
+      sy = fmaf(df, dy, sy);
+      sz = fmaf(df, dz, sz);
     }
-    fx = (double)sx + (double)ex;
-    fy = (double)sy + (double)ey;
-    fz = (double)sz + (double)ez;
+    fx = (double)sx;
+    fy = (double)sy;
+    fz = (double)sz;
   } else {
     const double4_32a qi = d.q_mid[par][o + a];
     const bool edge = cx == 0 || cy == 0 || cz == 0 || cx == b.nc[0] - 1 || cy == b.nc[1] - 1 || cz == b.nc[2] - 1;
     for (int k = lane; k < cnt; k += LPI) {
       const uint32_t e = __ldg(row + (long long)k * n);
-      double4_32a qj = ldg4(d.q_mid[par] + o + (e & kJMask));
+      double4_32a qj = ldg4(d.q_mid[par] + o + entry_slot(e));
       if (edge) {
-        const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+        const int ox = entry_sx(e), oy = entry_sy(e), oz = entry_sz(e);
         if (ox == 0 && cx == 0) qj.x -= b.L[0]; else if (ox == 2 && cx == b.nc[0] - 1) qj.x += b.L[0];
         if (oy == 0 && cy == 0) qj.y -= b.L[1]; else if (oy == 2 && cy == b.nc[1] - 1) qj.y += b.L[1];
         if (oz == 0 && cz == 0) qj.z -= b.L[2]; else if (oz == 2 && cz == b.nc[2] - 1) qj.z += b.L[2];
@@ -434,8 +427,8 @@ __global__ void k_batch_observe(Params P, Dev d) {
     const int cnt = d.ncount[o + a];
     for (int k = 0; k < cnt; k++) {
       const uint32_t e = d.nl[b.list_off + (long long)k * n + a];
-      double4_32a qj = d.q_end[o + (e & kJMask)];
-      const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+      double4_32a qj = d.q_end[o + entry_slot(e)];
+      const int ox = entry_sx(e), oy = entry_sy(e), oz = entry_sz(e);
       if (ox == 0 && cx == 0) qj.x -= b.L[0]; else if (ox == 2 && cx == b.nc[0] - 1) qj.x += b.L[0];
       if (oy == 0 && cy == 0) qj.y -= b.L[1]; else if (oy == 2 && cy == b.nc[1] - 1) qj.y += b.L[1];
       if (oz == 0 && cz == 0) qj.z -= b.L[2]; else if (oz == 2 && cz == b.nc[2] - 1) qj.z += b.L[2];

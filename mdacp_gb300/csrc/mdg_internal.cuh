@@ -9,8 +9,8 @@
 //   id[n]      int      caller's particle index of each slot; inv[id] = slot
 //   cell[n]    int      home cell of each slot at the last build
 //   nl[cap*n]  uint32   neighbour list, ELL layout: entry k of slot i at k*stride+i
-//                       bits 0..25 partner slot, bits 26..31 stencil offset
-//                       (ox+1) | (oy+1)<<2 | (oz+1)<<4
+//                       bits 0..5 stencil step (ox+1) | (oy+1)<<2 | (oz+1)<<4,
+//                       bits 6..31 partner slot
 //   ncount[n]  int      entries in row i
 //   loc[n]     float4   (mixed form) position relative to the home-cell centre
 #pragma once
@@ -28,9 +28,19 @@ __device__ __forceinline__ double4_32a ldg4(const double4_32a *p) {
   return make_double4_32a(a.x, a.y, b.x, b.y);
 }
 
-constexpr int kJBits = 26;
-constexpr uint32_t kJMask = (1u << kJBits) - 1u;
+constexpr int kJBits = 26;     // partner-slot bits of a list entry
+constexpr int kCodeBits = 6;   // stencil-step bits below them
 constexpr int kMaxParticles = 1 << kJBits;
+
+// List entry of partner slot j reached through stencil step (ox, oy, oz), each -1..1.
+__device__ __forceinline__ uint32_t entry_pack(int j, int ox, int oy, int oz) {
+  return ((uint32_t)j << kCodeBits) | (uint32_t)((ox + 1) | ((oy + 1) << 2) | ((oz + 1) << 4));
+}
+__device__ __forceinline__ int entry_slot(uint32_t e) { return (int)(e >> kCodeBits); }
+// stencil step + 1 (0, 1, 2) per axis
+__device__ __forceinline__ int entry_sx(uint32_t e) { return (int)(e & 3u); }
+__device__ __forceinline__ int entry_sy(uint32_t e) { return (int)((e >> 2) & 3u); }
+__device__ __forceinline__ int entry_sz(uint32_t e) { return (int)((e >> 4) & 3u); }
 
 // halt codes
 constexpr int kHaltOverflow = 1;
@@ -126,6 +136,31 @@ void launch_unsort(const Geom &g, const Dev &d, double4_32a *qo, double4_32a *po
 void launch_sort_in(const Geom &g, const Dev &d, const double4_32a *qi, const double4_32a *pi, cudaStream_t s);
 void launch_pairs(const Geom &g, const Dev &d, const long long *row_off, int32_t *rec, cudaStream_t s);
 void launch_set_rebuild(const Dev &d, cudaStream_t s);
+
+// Mixed-form partner offset.  Per axis, the offset between the home cells of
+// i and j minus i's own local coordinate is a quadratic in the stencil step
+// t = -1, 0, 1: v(t) = c + a t + b t^2 with c = -l_i,
+// a = (off(1) - off(-1)) / 2, b = (off(1) + off(-1)) / 2 (b = 0 away from the
+// periodic boundary).  t comes out of the entry's low bits as a float without
+// a conversion: OR-ing a small integer m into the mantissa of 2^23 gives the
+// float 2^23 + m exactly; the y and z fields sit 2 and 4 bits up, so they
+// decode to 4t and 16t and their coefficients carry 1/4 and 1/16 per power.
+struct AxisQuad {
+  float a, b, c;
+};
+
+__device__ __forceinline__ AxisQuad axis_quad(float w, float dl, bool lo, bool hi, float li, float scale) {
+  const float m = -w - (lo ? dl : 0.0f), p = w + (hi ? dl : 0.0f);
+  AxisQuad q;
+  q.a = 0.5f * (p - m) * scale;
+  q.b = 0.5f * (p + m) * (scale * scale);
+  q.c = -li;
+  return q;
+}
+
+__device__ __forceinline__ float step_float(uint32_t e, uint32_t mask, float bias) {
+  return __int_as_float((int)((e & mask) | 0x4B000000u)) - bias;
+}
 
 // device helpers
 __device__ __forceinline__ void halt_with(DevFlags *f, int code) { atomicCAS(&f->halt, 0, code); }

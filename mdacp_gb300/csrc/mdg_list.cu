@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(kListThreads) k_build_list(Geom g, Dev d) {
           const int cc = (nz * g.nc[1] + ny) * g.nc[0] + nx;
           const int a = d.cell_start[cc], b = d.cell_start[cc + 1];
           const float fx = offx - fi.x, fy = offy - fi.y, fz = offz - fi.z;
-          const uint32_t code = (uint32_t)((ox + 1) | ((oy + 1) << 2) | ((oz + 1) << 4)) << kJBits;
+          const uint32_t code = entry_pack(0, ox, oy, oz);
           const bool self_cell = (sx | sy | sz) == 0;
           for (int j = a; j < b; j++) {
             const float4 fj = d.qf[j];
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(kListThreads) k_build_list(Geom g, Dev d) {
             if (r2f > g.acc_hi) continue;
             if (self_cell && j == i) continue;
             if (r2f < g.acc_lo) {
-              if (cnt < g.list_cap) d.nl[(size_t)cnt * g.stride + i] = (uint32_t)j | code;
+              if (cnt < g.list_cap) d.nl[(size_t)cnt * g.stride + i] = ((uint32_t)j << kCodeBits) | code;
               cnt++;
               continue;
             }
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(kListThreads) k_build_list(Geom g, Dev d) {
             const double dx = __dsub_rn(qi.x, xj), dy = __dsub_rn(qi.y, yj), dz = __dsub_rn(qi.z, zj);
             const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
             if (r2 > g.sl2) continue;
-            if (cnt < g.list_cap) d.nl[(size_t)cnt * g.stride + i] = (uint32_t)j | code;
+            if (cnt < g.list_cap) d.nl[(size_t)cnt * g.stride + i] = ((uint32_t)j << kCodeBits) | code;
             cnt++;
           }
         }

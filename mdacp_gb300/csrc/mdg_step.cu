@@ -17,8 +17,14 @@
 // Householder step of order three, y <- y (1 + e + e^2), e = 1 - r^2 y, which
 // cubes the relative error of the estimate.
 // Mixed form: particle positions relative to their home-cell centre in
-// float; the pair force in float; the per-particle sums in compensated float
-// (Knuth's TwoSum); momentum and position updates in double.
+// float; the pair force and the per-particle sum in float; momentum and
+// position updates in double with fused multiply-adds.  A float sum of about
+// 40 terms adds an error near u sqrt(40) |f_ij| (u = 2^-24), a few times
+// below the error each float pair force already carries (its separation is
+// rounded to a float ulp of the cell width), so compensated summation would
+// buy no accuracy.  GB300 runs double precision at 1/64 of the float rate,
+// so the per-particle double work (momentum, two half-drifts, displacement)
+// is kept to one operation per component each.
 #include "mdg_internal.cuh"
 
 namespace mdg {
@@ -26,21 +32,28 @@ namespace mdg {
 namespace {
 
 constexpr int kStepThreads = 128;
+// Resident blocks per SM requested for the ordinary step variant (the
+// register budget follows: 65536 / (blocks * 128) per thread).  The kernel
+// waits on gathers, so occupancy pays: 12 blocks (40 registers, 48 warps per
+// SM) ran 16 % faster than the unconstrained 61-register build at 4M atoms.
+#ifndef MDG_STEP_MIN_BLOCKS
+#define MDG_STEP_MIN_BLOCKS 12
+#endif
+#ifndef MDG_PRUNE_MIN_BLOCKS
+#define MDG_PRUNE_MIN_BLOCKS 1
+#endif
+// Neighbour-list entries whose index and position loads are issued together
+// in the mixed-form force loop.
+#ifndef MDG_STEP_UNROLL
+#define MDG_STEP_UNROLL 4
+#endif
+constexpr int kUnroll = MDG_STEP_UNROLL;
 
 __device__ __forceinline__ double rcp_hh3(double x) {
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
   const double e = fma(-x, y, 1.0);
   return fma(y, fma(e, e, e), y);
-}
-
-// Knuth TwoSum accumulation: s + c carries the sum to about twice float precision.
-__device__ __forceinline__ void two_sum_acc(float &s, float &c, float x) {
-  const float t = s + x;
-  const float bp = t - s;
-  const float err = (s - (t - bp)) + (x - bp);
-  s = t;
-  c += err;
 }
 
 struct CellPos {
@@ -61,7 +74,7 @@ __device__ __forceinline__ CellPos cell_pos(const Geom &g, int c) {
 // Image of partner position qj seen from a particle in cell cp through stencil
 // offset bits of entry e: +-L where the offset crosses the periodic boundary.
 __device__ __forceinline__ void apply_image(const Geom &g, const CellPos &cp, uint32_t e, double4_32a &qj) {
-  const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+  const int ox = entry_sx(e), oy = entry_sy(e), oz = entry_sz(e);
   if (ox == 0 && cp.cx == 0) qj.x -= g.L[0];
   else if (ox == 2 && cp.cx == g.nc[0] - 1) qj.x += g.L[0];
   if (oy == 0 && cp.cy == 0) qj.y -= g.L[1];
@@ -89,7 +102,7 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int k = 0; k < cnt; k++) {
     const uint32_t e = __ldg(row + (size_t)k * g.stride);
-    double4_32a qj = ldg4(pos + (e & kJMask));
+    double4_32a qj = ldg4(pos + entry_slot(e));
     if (cp.edge) apply_image(g, cp, e, qj);
     const double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
     const double r2 = dx * dx + dy * dy + dz * dz;
@@ -109,62 +122,60 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
 
 // Mixed form of force_fp64 on home-cell-local float positions.  The offset
 // between the home cells of i and j is ox*w + s*(L - nc*w) per axis, s the
-// periodic wrap of the stencil step.
+// periodic wrap of the stencil step, evaluated as the quadratic of axis_quad.
 template <bool PRUNE>
 __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
                                                const uint32_t *__restrict__ list, const int *__restrict__ counts,
                                                int *kept) {
   const float4 li = loc[i];
   const CellPos cp = cell_pos(g, d.cell[i]);
-  const float mx0 = -g.w32[0] - (cp.cx == 0 ? g.dl32[0] : 0.0f), px0 = g.w32[0] + (cp.cx == g.nc[0] - 1 ? g.dl32[0] : 0.0f);
-  const float mx1 = -g.w32[1] - (cp.cy == 0 ? g.dl32[1] : 0.0f), px1 = g.w32[1] + (cp.cy == g.nc[1] - 1 ? g.dl32[1] : 0.0f);
-  const float mx2 = -g.w32[2] - (cp.cz == 0 ? g.dl32[2] : 0.0f), px2 = g.w32[2] + (cp.cz == g.nc[2] - 1 ? g.dl32[2] : 0.0f);
-  // offset of the partner's cell centre minus i's own local position, per stencil step
-  const float mxl = mx0 - li.x, pxl = px0 - li.x, zxl = -li.x;
-  const float myl = mx1 - li.y, pyl = px1 - li.y, zyl = -li.y;
-  const float mzl = mx2 - li.z, pzl = px2 - li.z, zzl = -li.z;
+  const AxisQuad qx = axis_quad(g.w32[0], g.dl32[0], cp.cx == 0, cp.cx == g.nc[0] - 1, li.x, 1.0f);
+  const AxisQuad qy = axis_quad(g.w32[1], g.dl32[1], cp.cy == 0, cp.cy == g.nc[1] - 1, li.y, 0.25f);
+  const AxisQuad qz = axis_quad(g.w32[2], g.dl32[2], cp.cz == 0, cp.cz == g.nc[2] - 1, li.z, 0.0625f);
   const int cnt = counts[i];
   const uint32_t *row = list + i;
   const size_t stride = (size_t)g.stride;
-  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
   const float rc2 = g.rc2f, c2x8 = g.c2x8f, thr = g.prune_thr2;
   int m = 0;
   auto pair = [&](uint32_t e, const float4 &lj) {
-    const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
-    const float dx = lj.x + (ox == 0 ? mxl : (ox == 2 ? pxl : zxl));
-    const float dy = lj.y + (oy == 0 ? myl : (oy == 2 ? pyl : zyl));
-    const float dz = lj.z + (oz == 0 ? mzl : (oz == 2 ? pzl : zzl));
+    const float tx = step_float(e, 0x03u, 8388609.0f);   // t
+    const float ty = step_float(e, 0x0Cu, 8388612.0f);   // 4 t
+    const float tz = step_float(e, 0x30u, 8388624.0f);   // 16 t
+    const float dx = lj.x + fmaf(fmaf(qx.b, tx, qx.a), tx, qx.c);
+    const float dy = lj.y + fmaf(fmaf(qy.b, ty, qy.a), ty, qy.c);
+    const float dz = lj.z + fmaf(fmaf(qz.b, tz, qz.a), tz, qz.c);
     const float r2 = dx * dx + dy * dy + dz * dz;
     if (PRUNE && r2 <= thr) d.pl[(size_t)(m++) * stride + i] = e;
-    if (r2 <= rc2) {
-      float inv;
-      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
-      const float i6 = inv * inv * inv;
-      const float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8;
-      two_sum_acc(sx, cx, df * dx);
-      two_sum_acc(sy, cy, df * dy);
-      two_sum_acc(sz, cz, df * dz);
-    }
+    // evaluated for every entry and masked: no divergent branch per pair
+    float inv;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+    const float i6 = inv * inv * inv;
+    float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8;
+    df = r2 <= rc2 ? df : 0.0f;
+    sx = fmaf(df, dx, sx);
+    sy = fmaf(df, dy, sy);
+    sz = fmaf(df, dz, sz);
   };
   int k = 0;
-  // four rows' worth of independent index and position loads in flight per thread
+  // kUnroll entries' independent index and position loads in flight per thread
 #pragma unroll 1
-  for (; k + 4 <= cnt; k += 4) {
-    uint32_t e[4];
-    float4 l[4];
+  for (; k + kUnroll <= cnt; k += kUnroll) {
+    uint32_t e[kUnroll];
+    float4 l[kUnroll];
 #pragma unroll
-    for (int u = 0; u < 4; u++) e[u] = __ldg(row + (size_t)(k + u) * stride);
+    for (int u = 0; u < kUnroll; u++) e[u] = __ldg(row + (size_t)(k + u) * stride);
 #pragma unroll
-    for (int u = 0; u < 4; u++) l[u] = __ldg(loc + (e[u] & kJMask));
+    for (int u = 0; u < kUnroll; u++) l[u] = __ldg(loc + entry_slot(e[u]));
 #pragma unroll
-    for (int u = 0; u < 4; u++) pair(e[u], l[u]);
+    for (int u = 0; u < kUnroll; u++) pair(e[u], l[u]);
   }
   for (; k < cnt; k++) {
     const uint32_t e = __ldg(row + (size_t)k * stride);
-    pair(e, __ldg(loc + (e & kJMask)));
+    pair(e, __ldg(loc + entry_slot(e)));
   }
   if (PRUNE) *kept = m;
-  return make_double3((double)sx + (double)cx, (double)sy + (double)cy, (double)sz + (double)cz);
+  return make_double3((double)sx, (double)sy, (double)sz);
 }
 
 __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) { return __umulhi(a, b); }
@@ -208,7 +219,7 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // 1 = ordinary step only, 2 = re-selecting step only (each a no-op when the
 // flag says otherwise, so the graph path can run the lighter variant).
 template <int THERMO, int COMPAT, int MIXED, int PMODE>
-__global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
+__global__ void __launch_bounds__(kStepThreads, PMODE == 1 ? MDG_STEP_MIN_BLOCKS : MDG_PRUNE_MIN_BLOCKS) k_step(Geom g, Dev d, int par) {
   const DevFlags *f = d.flags;
   if (f->halt != 0) return;
   if (PMODE == 1 && f->prune_now != 0) return;
@@ -229,8 +240,7 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
     else
       F = MIXED ? force_mixed<false>(g, d, d.loc[par], i, d.pl, d.pcount, nullptr)
                 : force_fp64<false>(g, d, qm, i, d.pl, d.pcount, nullptr);
-    const double4_32a p_old = d.p[i];
-    double4_32a p = p_old;
+    double4_32a p = d.p[i];
     if (THERMO == MDG_NOSEHOOVER) {
       const double e1 = f->exp1;
       p.x *= e1; p.y *= e1; p.z *= e1; p.w *= e1;
@@ -246,28 +256,29 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
       p.y += (-g.gamma * p.y + g.hb_d * z[1]) * g.dt;
       p.z += (-g.gamma * p.z + g.hb_d * z[2]) * g.dt;
     }
-    // Mid-step position of this particle.  The mixed form gathers float
-    // positions only, so it does not keep q_mid: q_end + p dt/2 with the
-    // momentum of the previous step is exactly what that step computed.
-    double4_32a q0;
-    if (MIXED) {
-      q0 = d.q_end[i];
-      q0.x = __dadd_rn(q0.x, __dmul_rn(p_old.x, g.dt2));
-      q0.y = __dadd_rn(q0.y, __dmul_rn(p_old.y, g.dt2));
-      q0.z = __dadd_rn(q0.z, __dmul_rn(p_old.z, g.dt2));
-    } else {
-      q0 = qm[i];
-    }
+    const double4_32a q0 = qm[i];
     double4_32a qe = q0, q1;
-    if (!(THERMO == MDG_LANGEVIN && COMPAT)) {
-      qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, g.dt2));
-      qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, g.dt2));
-      qe.z = __dadd_rn(q0.z, __dmul_rn(p.z, g.dt2));
+    if (MIXED) {  // one rounding per half-drift (fused)
+      if (!(THERMO == MDG_LANGEVIN && COMPAT)) {
+        qe.x = fma(p.x, g.dt2, q0.x);
+        qe.y = fma(p.y, g.dt2, q0.y);
+        qe.z = fma(p.z, g.dt2, q0.z);
+      }
+      q1 = qe;
+      q1.x = fma(p.x, g.dt2, qe.x);
+      q1.y = fma(p.y, g.dt2, qe.y);
+      q1.z = fma(p.z, g.dt2, qe.z);
+    } else {  // the reference's separate product and sum
+      if (!(THERMO == MDG_LANGEVIN && COMPAT)) {
+        qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, g.dt2));
+        qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, g.dt2));
+        qe.z = __dadd_rn(q0.z, __dmul_rn(p.z, g.dt2));
+      }
+      q1 = qe;
+      q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, g.dt2));
+      q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, g.dt2));
+      q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, g.dt2));
     }
-    q1 = qe;
-    q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, g.dt2));
-    q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, g.dt2));
-    q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, g.dt2));
     const double4_32a qb = d.q_build[i];
     const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
     // displacement since the build in float: the new home-cell-local position
@@ -297,7 +308,7 @@ __global__ void __launch_bounds__(kStepThreads) k_step(Geom g, Dev d, int par) {
     if (vx * vx + vy * vy + vz * vz > g.half_prune2) d.flags->prune_next = 1;
     d.p[i] = p;
     d.q_end[i] = qe;
-    if (!MIXED) qn[i] = q1;
+    qn[i] = q1;
     if (THERMO == MDG_NOSEHOOVER)
       ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
   }
@@ -363,7 +374,7 @@ __global__ void __launch_bounds__(kStepThreads) k_observe(Geom g, Dev d) {
     const int cnt = d.ncount[i];
     for (int k = 0; k < cnt; k++) {
       const uint32_t e = d.nl[(size_t)k * g.stride + i];
-      double4_32a qj = d.q_end[e & kJMask];
+      double4_32a qj = d.q_end[entry_slot(e)];
       if (cp.edge) apply_image(g, cp, e, qj);
       const double dx = __dsub_rn(qi.x, qj.x), dy = __dsub_rn(qi.y, qj.y), dz = __dsub_rn(qi.z, qj.z);
       const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
@@ -452,8 +463,8 @@ __global__ void k_pairs(Geom g, Dev d, const long long *row_off, int32_t *rec) {
   long long o = row_off[i];
   for (int k = 0; k < cnt; k++) {
     const uint32_t e = d.nl[(size_t)k * g.stride + i];
-    const int j = (int)(e & kJMask);
-    const int ox = (e >> 26) & 3, oy = (e >> 28) & 3, oz = (e >> 30) & 3;
+    const int j = (int)entry_slot(e);
+    const int ox = entry_sx(e), oy = entry_sy(e), oz = entry_sz(e);
     const int sx = (ox == 0 && cp.cx == 0) ? -1 : ((ox == 2 && cp.cx == g.nc[0] - 1) ? 1 : 0);
     const int sy = (oy == 0 && cp.cy == 0) ? -1 : ((oy == 2 && cp.cy == g.nc[1] - 1) ? 1 : 0);
     const int sz = (oz == 0 && cp.cz == 0) ? -1 : ((oz == 2 && cp.cz == g.nc[2] - 1) ? 1 : 0);

@@ -1,10 +1,13 @@
 """Runs one LJ workload through the C ABI for profiling (e.g. under ncu).
 
-    python -m mdacp_gb300.profile_run --cells 63 --precision mixed --steps 8 [--no-graphs]
+    python -m mdacp_gb300.profile_run --cells 63 --precision mixed --steps 8 [--no-graphs | --profiled]
 
 cells^3 FCC unit cells at density 0.5 (cells=100 -> 4,000,000 atoms, cells=63 ->
 1,000,188 atoms), Maxwell velocities at T=1, rc 2.5, margin 0.5, dt 0.001:
-one list build, then `steps` NVE steps.
+one list build, then `steps` NVE steps.  --profiled runs the steps as plain
+launches of both step-kernel variants (ordinary, re-selecting; each returns at
+once when the step is not its kind) with CUDA events around them, the form a
+kernel profiler sees one launch at a time; the mean step-kernel time is printed.
 """
 import argparse
 import os
@@ -20,6 +23,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--no-graphs", action="store_true")
+    ap.add_argument("--profiled", action="store_true")
     a = ap.parse_args()
     from mdacp_gb300 import lattice
     from mdacp_gb300.manager import MDManager
@@ -29,6 +33,13 @@ def main():
                   use_graphs=not a.no_graphs)
     m.set_state(q, p)
     m.make_pairlist()
+    if a.profiled:
+        kms = m.calculate_profiled(a.steps) / max(a.steps, 1)
+        st = m.stats()
+        print("atoms %d steps %d step-kernel ms %.4f pairs/atom %.2f inner %.2f rebuilds %d prunes %d" % (
+            len(q), a.steps, kms, st["listed_pairs"] / len(q), st["inner_pairs"] / len(q), st["rebuilds"],
+            st["prunes"]))
+        return
     m.calculate(a.steps)
     st = m.stats()
     print("atoms %d steps %d ms/step %.4f pairs/atom %.2f rebuilds %d" % (
