@@ -16,7 +16,11 @@ e2e       the same through the public C ABI from host memory: pinned host state
           mdg_get_state; wall clock.
 roofline  the fused step kernel (mixed): algorithmic bytes per launch
           n * (pairs_per_atom * 20 B + 72 B) over its mean launch time from a
-          CUDA-event-bracketed pass of the same workload.
+          CUDA-event-bracketed pass of the same workload; pairs_per_atom is the
+          inner list in ordinary steps and the outer list (+ 4 B per inner
+          entry written) in the steps that re-select the inner list, averaged
+          over the pass.  traffic: DRAM bytes per launch from the committed
+          ncu captures of both variants, weighted the same way.
 --impl reference  the reference's CPU implementation on the host cores: the
           reference binary built from its sources when present (oracle/_ref),
           else the oracle's C restatement, with all host threads.
@@ -254,13 +258,21 @@ def run_mine(args):
     s0 = mf.stats()
     kernel_ms = mf.calculate_profiled(kprof) / kprof
     s1 = mf.stats()
-    # pairs the kernel walks: the inner list (mean over the prunes of the pass
-    # is not exposed; the inner list at the end of the pass is used)
+    # pairs the kernel walks: the inner list in an ordinary step (its size at
+    # the end of the pass), the outer list in a re-selecting step, which also
+    # writes the inner rows (4 B per kept entry)
     ppa = s1["inner_pairs"] / n
-    alg_bytes = n * (ppa * 20.0 + 72.0)
+    opa = s1["listed_pairs"] / n
+    n_sel = min(max(s1["prunes"] - s0["prunes"], 0), kprof)
+    alg_bytes = n * ((kprof - n_sel) * (ppa * 20.0 + 72.0) + n_sel * (opa * 20.0 + ppa * 4.0 + 72.0)) / kprof
     peak, peak_kind = peaks()
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
-    tpa = ncu_traffic_per_atom("mixed")
+    # DRAM bytes per launch from the committed ncu captures of both variants,
+    # weighted by how many steps of the pass re-selected the inner list
+    t_ord, t_sel = ncu_traffic_per_atom("mixed"), ncu_traffic_per_atom("mixed_reselect")
+    tpa = None
+    if t_ord and t_sel:
+        tpa = ((kprof - n_sel) * t_ord + n_sel * t_sel) / kprof
     roof = {"kernel": "k_step<NVE,mixed>", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": (tpa * n) if tpa else None, "algorithmic_bytes": alg_bytes,
