@@ -107,7 +107,15 @@ int setup_geometry(mdg_handle *h) {
     g.dl32[k] = (float)(p.box[k] - (double)nc * (double)g.w32[k]);
     ncell *= nc;
   }
-  if (ncell > 4096LL * 4096LL) return fail(h, MDG_ERR_INVALID, "too many cells");
+  long long nrank = 1LL << (3 * mdg::kTileShift);
+  for (int k = 0; k < 3; k++) {
+    g.nt[k] = (g.nc[k] + mdg::kTileMask) >> mdg::kTileShift;
+    nrank *= g.nt[k];
+  }
+  if (ncell > 4096LL * 4096LL || nrank > 4096LL * 4096LL) return fail(h, MDG_ERR_INVALID, "too many cells");
+  g.nrank = (int)nrank;
+  if (g.nc[0] >= (1 << mdg::kCellXBits) || g.nc[1] >= (1 << mdg::kCellYBits) || g.nc[2] >= (1 << mdg::kCellZBits))
+    return fail(h, MDG_ERR_INVALID, "more than 2047 x 2047 x 1023 cells along the box sides");
   g.ncell = (int)ncell;
   g.sl2 = sl * sl;
   g.rc2 = p.cutoff * p.cutoff;
@@ -195,8 +203,8 @@ int recover_overflow(mdg_handle *h, bool in_step) {
 // partial cell counts; they are cleared here and the halt stays set (every
 // kernel is a no-op) until the next mdg_set_state.
 int halt_error(mdg_handle *h) {
-  cudaMemsetAsync(h->d.cell_count, 0, (size_t)h->g.ncell * sizeof(int), h->stream);
-  cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.ncell * sizeof(int), h->stream);
+  cudaMemsetAsync(h->d.cell_count, 0, (size_t)h->g.nrank * sizeof(int), h->stream);
+  cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.nrank * sizeof(int), h->stream);
   cudaStreamSynchronize(h->stream);
   char buf[160];
   snprintf(buf, sizeof buf, "particle coordinate non-finite or outside the box at a rebuild (slot %d)",
@@ -408,7 +416,7 @@ int mdg_create(const mdg_params *p, mdg_handle **out) {
   const size_t cap = (size_t)p->capacity;
   h->cap = p->capacity;
   mdg::Dev &d = h->d;
-  const size_t ncell = (size_t)h->g.ncell;
+  const size_t ncell = (size_t)h->g.nrank;
   const size_t nred = (cap + 127) / 128 + 1;
   if (e == cudaSuccess) e = dalloc(&d.q_end, cap);
   if (e == cudaSuccess) e = dalloc(&d.q_mid[0], cap);
@@ -486,8 +494,8 @@ static int set_state_common(mdg_handle *h, int32_t n) {
   f.bad_slot = INT_MAX;
   f.exp1 = 1.0;
   *h->hflags = f;
-  MDG_CK(cudaMemsetAsync(h->d.cell_count, 0, (size_t)h->g.ncell * sizeof(int), h->stream));
-  MDG_CK(cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.ncell * sizeof(int), h->stream));
+  MDG_CK(cudaMemsetAsync(h->d.cell_count, 0, (size_t)h->g.nrank * sizeof(int), h->stream));
+  MDG_CK(cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.nrank * sizeof(int), h->stream));
   MDG_CK(cudaMemcpyAsync(h->d.flags, h->hflags, sizeof(DevFlags), cudaMemcpyHostToDevice, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   drop_graphs(h);

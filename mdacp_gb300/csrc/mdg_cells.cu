@@ -9,9 +9,9 @@
 // wave when no rebuild is due.  Grids are a few waves of the SM count with
 // grid-stride loops.
 //
-// Order inside a cell is by caller particle index, which makes the slot order
-// (and with it every later summation order) independent of the atomics used
-// to fill the cells.
+// Cells are stored in the order of cell_rank.  Order inside a cell is by
+// caller particle index, which makes the slot order (and with it every later
+// summation order) independent of the atomics used to fill the cells.
 #include "mdg_internal.cuh"
 
 namespace mdg {
@@ -96,9 +96,8 @@ __global__ void k_wrap_bin(Geom g, Dev d, int count_step, int lang_step) {
     }
     q.x = x[0]; q.y = x[1]; q.z = x[2];
     d.q_end[i] = q;
-    const int cc = (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
-    d.cell[i] = cc;
-    atomicAdd(&d.cell_count[cc], 1);
+    d.cell[i] = cell_key(c[0], c[1], c[2]);
+    atomicAdd(&d.cell_count[cell_rank(g, c[0], c[1], c[2])], 1);
   }
 }
 
@@ -108,7 +107,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(Geom g, Dev d) {
   int s = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; k++)
-    if (base + k < g.ncell) s += d.cell_count[base + k];
+    if (base + k < g.nrank) s += d.cell_count[base + k];
   int total;
   block_exclusive_scan(s, &total);
   if (threadIdx.x == 0) d.block_sums[blockIdx.x] = total;
@@ -138,35 +137,38 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(Geom g, Dev d) {
   int v[kScanItems], s = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
-    v[k] = (base + k < g.ncell) ? d.cell_count[base + k] : 0;
+    v[k] = (base + k < g.nrank) ? d.cell_count[base + k] : 0;
     s += v[k];
   }
   int total;
   int off = block_exclusive_scan(s, &total) + d.block_sums[blockIdx.x];
 #pragma unroll
   for (int k = 0; k < kScanItems; k++) {
-    if (base + k < g.ncell) {
+    if (base + k < g.nrank) {
       d.cell_start[base + k] = off;
       d.cell_count[base + k] = 0;
       d.cell_fill[base + k] = 0;
     }
     off += v[k];
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) d.cell_start[g.ncell] = g.n;
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.cell_start[g.nrank] = g.n;
 }
 
 __global__ void k_scatter(Geom g, Dev d) {
   if (rebuild_off(d.flags)) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
-    const int c = d.cell[i];
+    int cx, cy, cz;
+    cell_unkey(d.cell[i], cx, cy, cz);
+    const int c = cell_rank(g, cx, cy, cz);
     d.order[d.cell_start[c] + atomicAdd(&d.cell_fill[c], 1)] = i;
   }
 }
 
-// Insertion sort of each cell's slots by caller index (cells hold tens of particles).
+// Insertion sort of each cell's slots by caller index (cells hold tens of
+// particles): the order is a function of the state alone.
 __global__ void k_cell_sort(Geom g, Dev d) {
   if (rebuild_off(d.flags)) return;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < g.ncell; c += gridDim.x * blockDim.x) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < g.nrank; c += gridDim.x * blockDim.x) {
     const int a = d.cell_start[c], b = d.cell_start[c + 1];
     for (int k = a + 1; k < b; k++) {
       const int v = d.order[k], key = d.id[v];
@@ -206,24 +208,19 @@ __global__ void k_finalize(Geom g, Dev d, int q_mid_dst) {
     d.cell[k] = c;
     d.inv[id] = k;
     d.q_build[k] = q;
-    {
-      const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
-      d.qf[k] = make_float4((float)(q.x - ((double)cx + 0.5) * (double)g.w32[0]),
-                            (float)(q.y - ((double)cy + 0.5) * (double)g.w32[1]),
-                            (float)(q.z - ((double)cz + 0.5) * (double)g.w32[2]), 0.0f);
-    }
+    int cx, cy, cz;
+    cell_unkey(c, cx, cy, cz);
+    const float cw = __int_as_float(c);
+    const double ox = ((double)cx + 0.5) * (double)g.w32[0];
+    const double oy = ((double)cy + 0.5) * (double)g.w32[1];
+    const double oz = ((double)cz + 0.5) * (double)g.w32[2];
+    d.qf[k] = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), cw);
     double4_32a m = q;
     m.x = __dadd_rn(q.x, __dmul_rn(p.x, g.dt2));
     m.y = __dadd_rn(q.y, __dmul_rn(p.y, g.dt2));
     m.z = __dadd_rn(q.z, __dmul_rn(p.z, g.dt2));
     q_mid[k] = m;
-    if (d.loc[q_mid_dst]) {
-      const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
-      const double ox = ((double)cx + 0.5) * (double)g.w32[0];
-      const double oy = ((double)cy + 0.5) * (double)g.w32[1];
-      const double oz = ((double)cz + 0.5) * (double)g.w32[2];
-      d.loc[q_mid_dst][k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), 0.0f);
-    }
+    if (d.loc[q_mid_dst]) d.loc[q_mid_dst][k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), cw);
   }
 }
 
@@ -264,9 +261,9 @@ void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cud
   const int cap = num_sms * 8;
   if (grid > cap) grid = cap;
   if (grid < 1) grid = 1;
-  int cgrid = (g.ncell + threads - 1) / threads;
+  int cgrid = (g.nrank + threads - 1) / threads;
   if (cgrid > cap) cgrid = cap;
-  const int nb = (g.ncell + kScanTile - 1) / kScanTile;
+  const int nb = (g.nrank + kScanTile - 1) / kScanTile;
   k_wrap_bin<<<grid, threads, 0, s>>>(g, d, count_step ? 1 : 0, lang_step ? 1 : 0);
   k_scan_reduce<<<nb, kScanThreads, 0, s>>>(g, d);
   k_scan_top<<<1, kScanThreads, 0, s>>>(nb, d);

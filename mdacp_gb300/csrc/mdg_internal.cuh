@@ -73,6 +73,8 @@ struct Geom {
   double inv_w[3];
   int nc[3];
   int ncell;
+  int nt[3];          // cell tiles per side (rounded up)
+  int nrank;          // tiles * cells per tile: length of the cell counters and starts
   int n;              // particles
   int stride;         // ELL row stride (allocated particle capacity)
   int list_cap;       // entries per row
@@ -136,6 +138,37 @@ void launch_unsort(const Geom &g, const Dev &d, double4_32a *qo, double4_32a *po
 void launch_sort_in(const Geom &g, const Dev &d, const double4_32a *qi, const double4_32a *pi, cudaStream_t s);
 void launch_pairs(const Geom &g, const Dev &d, const long long *row_off, int32_t *rec, cudaStream_t s);
 void launch_set_rebuild(const Dev &d, cudaStream_t s);
+
+// Home-cell coordinates of a slot packed in one word: bits 0-10 x, 11-21 y,
+// 22-31 z.  `cell[]` holds this key; the w word of the float4 positions (qf,
+// loc) holds the same bits, so the step kernel gets them with the position it
+// loads anyway.
+constexpr int kCellXBits = 11, kCellYBits = 11, kCellZBits = 10;
+__device__ __forceinline__ int cell_key(int cx, int cy, int cz) {
+  return (int)((uint32_t)cx | ((uint32_t)cy << kCellXBits) | ((uint32_t)cz << (kCellXBits + kCellYBits)));
+}
+__device__ __forceinline__ float cell_pack(int cx, int cy, int cz) { return __int_as_float(cell_key(cx, cy, cz)); }
+__device__ __forceinline__ void cell_unkey(int key, int &cx, int &cy, int &cz) {
+  const uint32_t v = (uint32_t)key;
+  cx = (int)(v & ((1u << kCellXBits) - 1u));
+  cy = (int)((v >> kCellXBits) & ((1u << kCellYBits) - 1u));
+  cz = (int)(v >> (kCellXBits + kCellYBits));
+}
+__device__ __forceinline__ void cell_unpack(float w, int &cx, int &cy, int &cz) { cell_unkey(__float_as_int(w), cx, cy, cz); }
+
+// Storage rank of a cell: cells grouped in tiles of 2^kTileShift cells per
+// side, tiles in x-fastest order, cells x-fastest inside a tile (kTileShift 0
+// is the plain x-fastest order).  Slots follow this order.
+#ifndef MDG_TILE_SHIFT
+#define MDG_TILE_SHIFT 0
+#endif
+constexpr int kTileShift = MDG_TILE_SHIFT;
+constexpr int kTileMask = (1 << kTileShift) - 1;
+__host__ __device__ __forceinline__ int cell_rank(const Geom &g, int cx, int cy, int cz) {
+  const int t = ((cz >> kTileShift) * g.nt[1] + (cy >> kTileShift)) * g.nt[0] + (cx >> kTileShift);
+  return (t << (3 * kTileShift)) | ((cz & kTileMask) << (2 * kTileShift)) | ((cy & kTileMask) << kTileShift) |
+         (cx & kTileMask);
+}
 
 // Mixed-form partner offset.  Per axis, the offset between the home cells of
 // i and j minus i's own local coordinate is a quadratic in the stencil step

@@ -14,7 +14,8 @@
 // (meshlist.cc:262-266), accepted when r2 <= SL^2.  Candidates are first
 // measured in float from home-cell-local positions, whose r2 is within 1e-5
 // of the exact value; only those within 1e-4 of SL^2 take the double test,
-// so the result is the exact set at float cost.
+// so the result is the exact set at float cost.  The order of the entries in
+// a row (stencil cell by cell, near side first) carries no meaning.
 #include "mdg_internal.cuh"
 
 namespace mdg {
@@ -22,56 +23,76 @@ namespace mdg {
 namespace {
 
 constexpr int kListThreads = 128;
+#ifndef MDG_LIST_MIN_BLOCKS
+#define MDG_LIST_MIN_BLOCKS 1
+#endif
+#ifndef MDG_LIST_UNROLL
+#define MDG_LIST_UNROLL 4
+#endif
+constexpr int kListUnroll = MDG_LIST_UNROLL;
 
-__global__ void __launch_bounds__(kListThreads) k_build_list(Geom g, Dev d) {
+// Exact acceptance of a candidate in the float band: the reference's image
+// and rounding order (mdunit.cc:167, meshlist.cc:262-266).
+__device__ __forceinline__ bool exact_within(const Geom &g, const double4_32a &qi, const double4_32a &qj, int sx, int sy,
+                                             int sz) {
+  const double xj = sx ? __dadd_rn(qj.x, sx > 0 ? g.L[0] : -g.L[0]) : qj.x;
+  const double yj = sy ? __dadd_rn(qj.y, sy > 0 ? g.L[1] : -g.L[1]) : qj.y;
+  const double zj = sz ? __dadd_rn(qj.z, sz > 0 ? g.L[2] : -g.L[2]) : qj.z;
+  const double dx = __dsub_rn(qi.x, xj), dy = __dsub_rn(qi.y, yj), dz = __dsub_rn(qi.z, zj);
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  return r2 <= g.sl2;
+}
+
+// One thread per slot; each stencil cell's candidates are read kListUnroll at
+// a time (independent loads in flight), then tested in order.
+__global__ void __launch_bounds__(kListThreads, MDG_LIST_MIN_BLOCKS) k_build_list(Geom g, Dev d) {
   DevFlags *f = d.flags;
   if (f->halt != 0 || f->rebuild == 0) return;
   unsigned long long tot = 0;
   int mx = 0;
+  const float acc_lo = g.acc_lo, acc_hi = g.acc_hi;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
     int cnt = 0;
     const float4 fi = d.qf[i];
-    const int c = d.cell[i];
-    const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+    int cx, cy, cz;
+    cell_unpack(fi.w, cx, cy, cz);
+    uint32_t *row = d.nl + i;
+    const size_t stride = (size_t)g.stride;
+    const int cap = g.list_cap;
     for (int oz = -1; oz <= 1; oz++) {
       int nz = cz + oz, sz = 0;
       if (nz < 0) { nz += g.nc[2]; sz = -1; } else if (nz >= g.nc[2]) { nz -= g.nc[2]; sz = 1; }
       // offset of the partner cell's centre: oz*w + sz*(L - nc*w)
-      const float offz = (float)oz * g.w32[2] + (float)sz * g.dl32[2];
+      const float fz = (float)oz * g.w32[2] + (float)sz * g.dl32[2] - fi.z;
       for (int oy = -1; oy <= 1; oy++) {
         int ny = cy + oy, sy = 0;
         if (ny < 0) { ny += g.nc[1]; sy = -1; } else if (ny >= g.nc[1]) { ny -= g.nc[1]; sy = 1; }
-        const float offy = (float)oy * g.w32[1] + (float)sy * g.dl32[1];
+        const float fy = (float)oy * g.w32[1] + (float)sy * g.dl32[1] - fi.y;
         for (int ox = -1; ox <= 1; ox++) {
           int nx = cx + ox, sx = 0;
           if (nx < 0) { nx += g.nc[0]; sx = -1; } else if (nx >= g.nc[0]) { nx -= g.nc[0]; sx = 1; }
-          const float offx = (float)ox * g.w32[0] + (float)sx * g.dl32[0];
-          const int cc = (nz * g.nc[1] + ny) * g.nc[0] + nx;
+          const float fx = (float)ox * g.w32[0] + (float)sx * g.dl32[0] - fi.x;
+          const int cc = cell_rank(g, nx, ny, nz);
           const int a = d.cell_start[cc], b = d.cell_start[cc + 1];
-          const float fx = offx - fi.x, fy = offy - fi.y, fz = offz - fi.z;
           const uint32_t code = entry_pack(0, ox, oy, oz);
-          const bool self_cell = (sx | sy | sz) == 0;
-          for (int j = a; j < b; j++) {
-            const float4 fj = d.qf[j];
-            const float ex = fj.x + fx, ey = fj.y + fy, ez = fj.z + fz;
-            const float r2f = ex * ex + ey * ey + ez * ez;
-            if (r2f > g.acc_hi) continue;
-            if (self_cell && j == i) continue;
-            if (r2f < g.acc_lo) {
-              if (cnt < g.list_cap) d.nl[(size_t)cnt * g.stride + i] = ((uint32_t)j << kCodeBits) | code;
-              cnt++;
-              continue;
+          for (int j0 = a; j0 < b; j0 += kListUnroll) {
+            float4 fj[kListUnroll];
+#pragma unroll
+            for (int u = 0; u < kListUnroll; u++)
+              fj[u] = j0 + u < b ? d.qf[j0 + u] : make_float4(1e30f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < kListUnroll; u++) {
+              const int j = j0 + u;
+              const float ex = fj[u].x + fx, ey = fj[u].y + fy, ez = fj[u].z + fz;
+              const float r2f = fmaf(ez, ez, fmaf(ey, ey, ex * ex));
+              if (r2f > acc_hi || j == i) continue;
+              bool take = r2f < acc_lo;
+              if (!take) take = exact_within(g, d.q_end[i], d.q_end[j], sx, sy, sz);
+              if (take) {
+                if (cnt < cap) row[(size_t)cnt * stride] = ((uint32_t)j << kCodeBits) | code;
+                cnt++;
+              }
             }
-            const double4_32a qi = d.q_end[i];
-            const double4_32a qj = d.q_end[j];
-            const double xj = sx ? __dadd_rn(qj.x, sx > 0 ? g.L[0] : -g.L[0]) : qj.x;
-            const double yj = sy ? __dadd_rn(qj.y, sy > 0 ? g.L[1] : -g.L[1]) : qj.y;
-            const double zj = sz ? __dadd_rn(qj.z, sz > 0 ? g.L[2] : -g.L[2]) : qj.z;
-            const double dx = __dsub_rn(qi.x, xj), dy = __dsub_rn(qi.y, yj), dz = __dsub_rn(qi.z, zj);
-            const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-            if (r2 > g.sl2) continue;
-            if (cnt < g.list_cap) d.nl[(size_t)cnt * g.stride + i] = ((uint32_t)j << kCodeBits) | code;
-            cnt++;
           }
         }
       }

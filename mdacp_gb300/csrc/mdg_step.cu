@@ -48,6 +48,26 @@ constexpr int kStepThreads = 128;
 #define MDG_STEP_UNROLL 4
 #endif
 constexpr int kUnroll = MDG_STEP_UNROLL;
+#ifndef MDG_STEP_PREFETCH
+#define MDG_STEP_PREFETCH 0
+#endif
+// List entries are read once per step: 0 = read-only cache path (ld.global.nc),
+// 1 = the same without L1 allocation, 2 = streaming (evict-first) loads.
+#ifndef MDG_LIST_LOAD
+#define MDG_LIST_LOAD 0
+#endif
+
+__device__ __forceinline__ uint32_t ld_list(const uint32_t *p) {
+#if MDG_LIST_LOAD == 1
+  uint32_t v;
+  asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+#elif MDG_LIST_LOAD == 2
+  return __ldcs(p);
+#else
+  return __ldg(p);
+#endif
+}
 
 __device__ __forceinline__ double rcp_hh3(double x) {
   double y;
@@ -61,12 +81,17 @@ struct CellPos {
   bool edge;
 };
 
-__device__ __forceinline__ CellPos cell_pos(const Geom &g, int c) {
+__device__ __forceinline__ CellPos cell_pos(const Geom &g, int key) {
   CellPos r;
-  r.cx = c % g.nc[0];
-  const int t = c / g.nc[0];
-  r.cy = t % g.nc[1];
-  r.cz = t / g.nc[1];
+  cell_unkey(key, r.cx, r.cy, r.cz);
+  r.edge = r.cx == 0 || r.cy == 0 || r.cz == 0 || r.cx == g.nc[0] - 1 || r.cy == g.nc[1] - 1 || r.cz == g.nc[2] - 1;
+  return r;
+}
+
+// The same from the coordinates packed in the w word of qf / loc.
+__device__ __forceinline__ CellPos cell_pos_packed(const Geom &g, float w) {
+  CellPos r;
+  cell_unpack(w, r.cx, r.cy, r.cz);
   r.edge = r.cx == 0 || r.cy == 0 || r.cz == 0 || r.cx == g.nc[0] - 1 || r.cy == g.nc[1] - 1 || r.cz == g.nc[2] - 1;
   return r;
 }
@@ -91,10 +116,9 @@ __device__ __forceinline__ void apply_image(const Geom &g, const CellPos &cp, ui
 // of slot i (d.pl); *kept receives the new row length.
 template <bool PRUNE>
 __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const double4_32a *__restrict__ pos, int i,
-                                              const uint32_t *__restrict__ list, const int *__restrict__ counts,
-                                              int *kept) {
+                                              const CellPos &cp, const uint32_t *__restrict__ list,
+                                              const int *__restrict__ counts, int *kept) {
   const double4_32a qi = pos[i];
-  const CellPos cp = cell_pos(g, d.cell[i]);
   const int cnt = counts[i];
   const uint32_t *row = list + i;
   const double thr = (double)g.prune_thr2;
@@ -125,10 +149,9 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
 // periodic wrap of the stencil step, evaluated as the quadratic of axis_quad.
 template <bool PRUNE>
 __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
-                                               const uint32_t *__restrict__ list, const int *__restrict__ counts,
-                                               int *kept) {
+                                               const CellPos &cp, const uint32_t *__restrict__ list,
+                                               const int *__restrict__ counts, int *kept) {
   const float4 li = loc[i];
-  const CellPos cp = cell_pos(g, d.cell[i]);
   const AxisQuad qx = axis_quad(g.w32[0], g.dl32[0], cp.cx == 0, cp.cx == g.nc[0] - 1, li.x, 1.0f);
   const AxisQuad qy = axis_quad(g.w32[1], g.dl32[1], cp.cy == 0, cp.cy == g.nc[1] - 1, li.y, 0.25f);
   const AxisQuad qz = axis_quad(g.w32[2], g.dl32[2], cp.cz == 0, cp.cz == g.nc[2] - 1, li.z, 0.0625f);
@@ -159,19 +182,43 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
   };
   int k = 0;
   // kUnroll entries' independent index and position loads in flight per thread
+#if MDG_STEP_PREFETCH
+  // the next group's entries are requested before this group's pairs are
+  // evaluated, so the list stream and the partner gathers overlap
+  if (cnt >= kUnroll) {
+    uint32_t en[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; u++) en[u] = ld_list(row + (size_t)u * stride);
+#pragma unroll 1
+    for (; k + kUnroll <= cnt; k += kUnroll) {
+      uint32_t e[kUnroll];
+      float4 l[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) e[u] = en[u];
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) l[u] = __ldg(loc + entry_slot(e[u]));
+      const int kn = k + kUnroll;
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) en[u] = kn + u < cnt ? ld_list(row + (size_t)(kn + u) * stride) : 0u;
+#pragma unroll
+      for (int u = 0; u < kUnroll; u++) pair(e[u], l[u]);
+    }
+  }
+#else
 #pragma unroll 1
   for (; k + kUnroll <= cnt; k += kUnroll) {
     uint32_t e[kUnroll];
     float4 l[kUnroll];
 #pragma unroll
-    for (int u = 0; u < kUnroll; u++) e[u] = __ldg(row + (size_t)(k + u) * stride);
+    for (int u = 0; u < kUnroll; u++) e[u] = ld_list(row + (size_t)(k + u) * stride);
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) l[u] = __ldg(loc + entry_slot(e[u]));
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) pair(e[u], l[u]);
   }
+#endif
   for (; k < cnt; k++) {
-    const uint32_t e = __ldg(row + (size_t)k * stride);
+    const uint32_t e = ld_list(row + (size_t)k * stride);
     pair(e, __ldg(loc + entry_slot(e)));
   }
   if (PRUNE) *kept = m;
@@ -233,13 +280,16 @@ __global__ void __launch_bounds__(kStepThreads, PMODE == 1 ? MDG_STEP_MIN_BLOCKS
   const bool prune = PMODE == 2 ? true : (PMODE == 1 ? false : f->prune_now != 0);
   int kept = 0;
   if (active) {
+    // build-time local position; its w word holds the home-cell coordinates
+    const float4 lb = d.qf[i];
+    const CellPos cp = cell_pos_packed(g, lb.w);
     double3 F;
     if (prune)
-      F = MIXED ? force_mixed<true>(g, d, d.loc[par], i, d.nl, d.ncount, &kept)
-                : force_fp64<true>(g, d, qm, i, d.nl, d.ncount, &kept);
+      F = MIXED ? force_mixed<true>(g, d, d.loc[par], i, cp, d.nl, d.ncount, &kept)
+                : force_fp64<true>(g, d, qm, i, cp, d.nl, d.ncount, &kept);
     else
-      F = MIXED ? force_mixed<false>(g, d, d.loc[par], i, d.pl, d.pcount, nullptr)
-                : force_fp64<false>(g, d, qm, i, d.pl, d.pcount, nullptr);
+      F = MIXED ? force_mixed<false>(g, d, d.loc[par], i, cp, d.pl, d.pcount, nullptr)
+                : force_fp64<false>(g, d, qm, i, cp, d.pl, d.pcount, nullptr);
     double4_32a p = d.p[i];
     if (THERMO == MDG_NOSEHOOVER) {
       const double e1 = f->exp1;
@@ -284,8 +334,7 @@ __global__ void __launch_bounds__(kStepThreads, PMODE == 1 ? MDG_STEP_MIN_BLOCKS
     // displacement since the build in float: the new home-cell-local position
     // (qf holds the local position at the build) and the inner-list test
     const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
-    const float4 lb = d.qf[i];
-    const float4 ln = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
+    const float4 ln = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, lb.w);
     d.loc[par ^ 1][i] = ln;
     if (MIXED) {
       if (fx * fx + fy * fy + fz * fz > (float)g.half_margin2 || !(fx == fx && fy == fy && fz == fz))
@@ -418,8 +467,9 @@ template <int MIXED>
 __global__ void __launch_bounds__(kStepThreads) k_forces(Geom g, Dev d, const float4 *loc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n) return;
-  const double3 F = MIXED ? force_mixed<false>(g, d, loc, i, d.nl, d.ncount, nullptr)
-                          : force_fp64<false>(g, d, d.q_end, i, d.nl, d.ncount, nullptr);
+  const CellPos cp = cell_pos(g, d.cell[i]);
+  const double3 F = MIXED ? force_mixed<false>(g, d, loc, i, cp, d.nl, d.ncount, nullptr)
+                          : force_fp64<false>(g, d, d.q_end, i, cp, d.nl, d.ncount, nullptr);
   d.io4[d.id[i]] = make_double4_32a(F.x, F.y, F.z, 0.0);
 }
 
@@ -428,11 +478,11 @@ __global__ void k_loc_from_end(Geom g, Dev d, float4 *loc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n) return;
   const double4_32a q = d.q_end[i];
-  const int c = d.cell[i];
-  const int cx = c % g.nc[0], t = c / g.nc[0], cy = t % g.nc[1], cz = t / g.nc[1];
+  int cx, cy, cz;
+  cell_unkey(d.cell[i], cx, cy, cz);
   loc[i] = make_float4((float)(q.x - ((double)cx + 0.5) * (double)g.w32[0]),
                          (float)(q.y - ((double)cy + 0.5) * (double)g.w32[1]),
-                         (float)(q.z - ((double)cz + 0.5) * (double)g.w32[2]), 0.0f);
+                         (float)(q.z - ((double)cz + 0.5) * (double)g.w32[2]), cell_pack(cx, cy, cz));
 }
 
 __global__ void k_unsort(Geom g, Dev d, double4_32a *qo, double4_32a *po) {
