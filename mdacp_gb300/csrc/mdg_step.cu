@@ -48,27 +48,6 @@ constexpr int kStepThreads = 128;
 #define MDG_STEP_UNROLL 4
 #endif
 constexpr int kUnroll = MDG_STEP_UNROLL;
-#ifndef MDG_STEP_PREFETCH
-#define MDG_STEP_PREFETCH 0
-#endif
-// List entries are read once per step: 0 = read-only cache path (ld.global.nc),
-// 1 = the same without L1 allocation, 2 = streaming (evict-first) loads.
-#ifndef MDG_LIST_LOAD
-#define MDG_LIST_LOAD 0
-#endif
-
-__device__ __forceinline__ uint32_t ld_list(const uint32_t *p) {
-#if MDG_LIST_LOAD == 1
-  uint32_t v;
-  asm("ld.global.nc.L1::no_allocate.u32 %0, [%1];" : "=r"(v) : "l"(p));
-  return v;
-#elif MDG_LIST_LOAD == 2
-  return __ldcs(p);
-#else
-  return __ldg(p);
-#endif
-}
-
 __device__ __forceinline__ double rcp_hh3(double x) {
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
@@ -182,43 +161,19 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
   };
   int k = 0;
   // kUnroll entries' independent index and position loads in flight per thread
-#if MDG_STEP_PREFETCH
-  // the next group's entries are requested before this group's pairs are
-  // evaluated, so the list stream and the partner gathers overlap
-  if (cnt >= kUnroll) {
-    uint32_t en[kUnroll];
-#pragma unroll
-    for (int u = 0; u < kUnroll; u++) en[u] = ld_list(row + (size_t)u * stride);
-#pragma unroll 1
-    for (; k + kUnroll <= cnt; k += kUnroll) {
-      uint32_t e[kUnroll];
-      float4 l[kUnroll];
-#pragma unroll
-      for (int u = 0; u < kUnroll; u++) e[u] = en[u];
-#pragma unroll
-      for (int u = 0; u < kUnroll; u++) l[u] = __ldg(loc + entry_slot(e[u]));
-      const int kn = k + kUnroll;
-#pragma unroll
-      for (int u = 0; u < kUnroll; u++) en[u] = kn + u < cnt ? ld_list(row + (size_t)(kn + u) * stride) : 0u;
-#pragma unroll
-      for (int u = 0; u < kUnroll; u++) pair(e[u], l[u]);
-    }
-  }
-#else
 #pragma unroll 1
   for (; k + kUnroll <= cnt; k += kUnroll) {
     uint32_t e[kUnroll];
     float4 l[kUnroll];
 #pragma unroll
-    for (int u = 0; u < kUnroll; u++) e[u] = ld_list(row + (size_t)(k + u) * stride);
+    for (int u = 0; u < kUnroll; u++) e[u] = __ldg(row + (size_t)(k + u) * stride);
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) l[u] = __ldg(loc + entry_slot(e[u]));
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) pair(e[u], l[u]);
   }
-#endif
   for (; k < cnt; k++) {
-    const uint32_t e = ld_list(row + (size_t)k * stride);
+    const uint32_t e = __ldg(row + (size_t)k * stride);
     pair(e, __ldg(loc + entry_slot(e)));
   }
   if (PRUNE) *kept = m;
