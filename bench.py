@@ -408,7 +408,7 @@ def run_adjoint4k(args):
     n = len(q)
     out = {}
     for obj in ("pe", "pressure"):
-        a = Adjoint(L, n, steps=200, checkpoint_every=20, dt=0.002, margin=2.0, objective=obj)
+        a = Adjoint(L, n, steps=200, checkpoint_every=20, dt=0.002, margin=0.5, objective=obj)
         a.forward(q, p)
         a.backward()
         t0 = time.perf_counter()

@@ -193,16 +193,16 @@ int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s);
  * adjoint (reverse steps with a Hessian-vector product over the same pair
  * list), checkpointing every checkpoint_every steps and recomputing each
  * segment in the backward pass.  V(r) = epsilon phi(r / sigma) with the
- * reference's smoothly truncated phi; the cut-off is cutoff * sigma.  The pair
- * list (all pairs within cutoff * sigma + margin at the initial positions) is
- * kept for the whole horizon; a particle moving more than margin / 2 is an
- * error (MDG_ERR_STATE).  FP64 throughout. */
+ * reference's smoothly truncated phi; the cut-off is cutoff * sigma.  Each
+ * checkpoint segment uses the pair list of its first state (all pairs within
+ * cutoff * sigma + margin); a particle moving more than margin / 2 within a
+ * segment is an error (MDG_ERR_STATE).  FP64 throughout. */
 enum mdg_objective { MDG_OBJ_POTENTIAL = 0, MDG_OBJ_PRESSURE = 1 };
 
 typedef struct mdg_adjoint_params {
   double box[3];
   double cutoff;           /* in units of sigma */
-  double margin;           /* absolute list margin for the whole horizon */
+  double margin;           /* absolute list margin for one checkpoint segment */
   double dt;
   double epsilon, sigma;
   int32_t steps;           /* horizon */

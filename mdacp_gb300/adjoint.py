@@ -46,7 +46,7 @@ def _dp(a):
 
 
 class Adjoint:
-    def __init__(self, L, n, steps=200, checkpoint_every=20, dt=0.002, cutoff=2.5, margin=2.0, epsilon=1.0,
+    def __init__(self, L, n, steps=200, checkpoint_every=20, dt=0.002, cutoff=2.5, margin=0.5, epsilon=1.0,
                  sigma=1.0, objective="pe", device=0):
         self.lib = _lib()
         prm = AdjointParams()

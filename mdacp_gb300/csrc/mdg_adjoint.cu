@@ -19,9 +19,12 @@
 // H v is the Hessian-vector product over the same pair list.  States are
 // checkpointed every K steps in the forward pass; the backward pass recomputes
 // each segment from its checkpoint (storing its K half-step positions and
-// states) and then reverses it.  The pair list (every pair within
-// cutoff*sigma + margin at q0, minimum image) is fixed over the horizon; the
-// forward pass verifies that no particle moves more than margin/2.
+// states) and then reverses it.  Each checkpoint segment has its own pair
+// list (every pair within cutoff*sigma + margin at the segment's first state,
+// minimum image), built from the same state in both passes; the forward pass
+// verifies that no particle moves more than margin/2 within a segment.  The
+// pair kernels give each particle kLanes lanes and evaluate the pair terms
+// without divisions (GB300's FP64 rate is 1/64 of FP32).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -36,15 +39,26 @@ namespace mdg {
 namespace adj {
 
 constexpr int kT = 128;
+// Lanes sharing one particle's row in the pair kernels (FP64 runs at 1/64 of
+// the FP32 rate on GB300, so a few thousand particles need several lanes each
+// to occupy every SM's FP64 pipes).
+#ifndef MDG_ADJ_LANES
+#define MDG_ADJ_LANES 8
+#endif
+constexpr int kLanes = MDG_ADJ_LANES;
 
 struct P {
   double L[3];
+  double inv_L[3];
   double eps, sig, dt, dt2;
   double xc2;      // (cutoff in sigma units)^2
   double c0, c2;   // correction constants of phi
   double sl2;      // list radius^2 (absolute)
+  double sl2f;     // the float test's radius^2 (widened by 1e-3)
   double half_margin2;
   double volume;
+  // eps / sigma^k products used per pair (no division in the pair terms)
+  double inv_s2, e_s, e_s2, e_s3, e_s4;
   int n, cap, objective, pad;
 };
 
@@ -52,16 +66,25 @@ struct D {
   double4_32a *q, *p, *qh, *F, *aq, *ap, *aqh, *tmp, *q0;
   double4_32a *ckq, *ckp;    // checkpoints
   double4_32a *segq, *segp, *segqh;  // recomputed segment
-  int *nbr, *cnt;            // fixed list, row-major [n][cap]
+  int *nbr, *cnt;            // the current segment's list, row-major [n][cap]
   double *part;              // block partials
   double *acc;               // running sums: J, g_eps, g_sig
   int *flag;
 };
 
 __device__ __forceinline__ void min_image(const P &c, double &dx, double &dy, double &dz) {
-  dx -= c.L[0] * rint(dx / c.L[0]);
-  dy -= c.L[1] * rint(dy / c.L[1]);
-  dz -= c.L[2] * rint(dz / c.L[2]);
+  dx -= c.L[0] * rint(dx * c.inv_L[0]);
+  dy -= c.L[1] * rint(dy * c.inv_L[1]);
+  dz -= c.L[2] * rint(dz * c.inv_L[2]);
+}
+
+// 1/x from the hardware estimate refined by one cubic Householder step
+// (relative error of the estimate cubed, below double rounding).
+__device__ __forceinline__ double recip(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double e = fma(-x, y, 1.0);
+  return fma(y, fma(e, e, e), y);
 }
 
 // Per pair at distance r (d = q_j - q_i): the reduced quantities.
@@ -77,10 +100,9 @@ struct PairTerms {
 };
 
 __device__ __forceinline__ bool pair_terms(const P &c, double r2, PairTerms &t) {
-  const double s2 = c.sig * c.sig;
-  const double x2 = r2 / s2;
+  const double x2 = r2 * c.inv_s2;
   if (x2 > c.xc2) return false;
-  const double ix2 = 1.0 / x2, ix6 = ix2 * ix2 * ix2, ix8 = ix6 * ix2, ix12 = ix6 * ix6, ix14 = ix12 * ix2;
+  const double ix2 = recip(x2), ix6 = ix2 * ix2 * ix2, ix8 = ix6 * ix2, ix12 = ix6 * ix6, ix14 = ix12 * ix2;
   const double ix10 = ix8 * ix2, ix16 = ix14 * ix2;
   // psi(x) = phi'(x)/x, chi(x) = x^2 psi(x)
   const double psi = -48.0 * ix14 + 24.0 * ix8 + 8.0 * c.c2;
@@ -89,15 +111,14 @@ __device__ __forceinline__ bool pair_terms(const P &c, double r2, PairTerms &t) 
   const double xdphi = 4.0 * (-12.0 * ix12 + 6.0 * ix6 + 2.0 * c.c2 * x2);  // x phi'(x)
   const double chi = x2 * psi;                               // -48 x^-12 + 24 x^-6 + 8 C2 x^2
   const double xdchi = 576.0 * ix12 - 144.0 * ix6 + 16.0 * c.c2 * x2;  // x chi'(x)
-  const double e = c.eps, s = c.sig;
-  t.f = e / s2 * psi;
-  t.fpr = e / (s2 * s2) * dpsi_x;
-  t.phi = e * phi;
-  t.fs = -e / (s2 * s) * (2.0 * psi + x2 * dpsi_x);
-  t.dphis = -e / s * xdphi;
-  t.g = e * chi;
-  t.gpr = e / s2 * (xdchi / x2);
-  t.gs = -e / s * xdchi;
+  t.f = c.e_s2 * psi;
+  t.fpr = c.e_s4 * dpsi_x;
+  t.phi = c.eps * phi;
+  t.fs = -c.e_s3 * (2.0 * psi + x2 * dpsi_x);
+  t.dphis = -c.e_s * xdphi;
+  t.g = c.eps * chi;
+  t.gpr = c.e_s2 * (xdchi * ix2);
+  t.gs = -c.e_s * xdchi;
   return true;
 }
 
@@ -112,41 +133,81 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return t;
 }
 
-__global__ void k_build(P c, D d) {
+// Sum over the kLanes lanes that share a particle (all lanes hold the total).
+__device__ __forceinline__ double lane_sum(double v) {
+#pragma unroll
+  for (int o = 1; o < kLanes; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Pair list at positions q: every partner within the list radius, minimum
+// image, ascending j.  The test runs in float on block-wide tiles of
+// positions against a radius widened by 1e-3 (float positions of a box of
+// tens of sigma are within 1e-5), so every pair within the exact radius is
+// listed; a few more do no harm (the pair terms cut at rc).
+__global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
+  __shared__ float4 tile[kT];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.n) return;
-  const double4_32a qi = d.q[i];
-  int m = 0;
-  for (int j = 0; j < c.n; j++) {
-    if (j == i) continue;
-    const double4_32a qj = d.q[j];
-    double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-    min_image(c, dx, dy, dz);
-    if (dx * dx + dy * dy + dz * dz <= c.sl2) {
-      if (m < c.cap) d.nbr[(size_t)i * c.cap + m] = j;
-      m++;
-    }
+  float4 qi = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (i < c.n) {
+    const double4_32a v = q[i];
+    qi = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
   }
-  d.cnt[i] = m < c.cap ? m : c.cap;
-  if (m > c.cap) atomicMax(d.flag, m);
+  const float lx = (float)c.L[0], ly = (float)c.L[1], lz = (float)c.L[2];
+  const float ilx = (float)c.inv_L[0], ily = (float)c.inv_L[1], ilz = (float)c.inv_L[2];
+  const float sl2f = (float)c.sl2f;
+  int m = 0;
+  for (int base = 0; base < c.n; base += kT) {
+    const int jl = base + threadIdx.x;
+    if (jl < c.n) {
+      const double4_32a v = q[jl];
+      tile[threadIdx.x] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+    }
+    __syncthreads();
+    const int lim = min(kT, c.n - base);
+    if (i < c.n) {
+      for (int t = 0; t < lim; t++) {
+        const float4 qj = tile[t];
+        float dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+        dx -= lx * rintf(dx * ilx);
+        dy -= ly * rintf(dy * ily);
+        dz -= lz * rintf(dz * ilz);
+        const int j = base + t;
+        if (dx * dx + dy * dy + dz * dz <= sl2f && j != i) {
+          if (m < c.cap) d.nbr[(size_t)i * c.cap + m] = j;
+          m++;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (i < c.n) {
+    d.cnt[i] = m < c.cap ? m : c.cap;
+    if (m > c.cap) atomicMax(d.flag, m);
+  }
 }
 
 __global__ void k_force(P c, D d, const double4_32a *q, double4_32a *F) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.n) return;
-  const double4_32a qi = q[i];
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tid / kLanes, lane = tid % kLanes;
   double fx = 0, fy = 0, fz = 0;
-  for (int k = 0; k < d.cnt[i]; k++) {
-    const double4_32a qj = q[d.nbr[(size_t)i * c.cap + k]];
-    double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-    min_image(c, dx, dy, dz);
-    PairTerms t;
-    if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
-    fx += t.f * dx;
-    fy += t.f * dy;
-    fz += t.f * dz;
+  if (i < c.n) {
+    const double4_32a qi = q[i];
+    for (int k = lane; k < d.cnt[i]; k += kLanes) {
+      const double4_32a qj = q[d.nbr[(size_t)i * c.cap + k]];
+      double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
+      min_image(c, dx, dy, dz);
+      PairTerms t;
+      if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
+      fx += t.f * dx;
+      fy += t.f * dy;
+      fz += t.f * dz;
+    }
   }
-  F[i] = make_double4_32a(fx, fy, fz, 0.0);
+  fx = lane_sum(fx);
+  fy = lane_sum(fy);
+  fz = lane_sum(fz);
+  if (i < c.n && lane == 0) F[i] = make_double4_32a(fx, fy, fz, 0.0);
 }
 
 // qh = q + p dt/2 (also records the displacement check against q0)
@@ -185,12 +246,13 @@ __global__ void k_kick_drift(P c, const double4_32a *qh, const double4_32a *F, d
 // also adds w * dj/dq to aq and w * dj/dp to ap (w = 1/Ns).
 __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p, int grad, double w) {
   __shared__ double sh[32];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tid / kLanes, lane = tid % kLanes;
   double val = 0, ge = 0, gs = 0;
+  double gx = 0, gy = 0, gz = 0, u = 0, us = 0, G = 0, Gs = 0;
   if (i < c.n) {
-    const double4_32a qi = q[i], pi = p[i];
-    double gx = 0, gy = 0, gz = 0, u = 0, us = 0, G = 0, Gs = 0;
-    for (int k = 0; k < d.cnt[i]; k++) {
+    const double4_32a qi = q[i];
+    for (int k = lane; k < d.cnt[i]; k += kLanes) {
       const double4_32a qj = q[d.nbr[(size_t)i * c.cap + k]];
       double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
       min_image(c, dx, dy, dz);
@@ -210,6 +272,19 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
         gz += t.gpr * dz;
       }
     }
+  }
+  gx = lane_sum(gx);
+  gy = lane_sum(gy);
+  gz = lane_sum(gz);
+  if (c.objective == 0) {
+    u = lane_sum(u);
+    us = lane_sum(us);
+  } else {
+    G = lane_sum(G);
+    Gs = lane_sum(Gs);
+  }
+  if (i < c.n && lane == 0) {
+    const double4_32a pi = p[i];
     const double ke = 0.5 * (pi.x * pi.x + pi.y * pi.y + pi.z * pi.z);
     if (c.objective == 0) {
       const double inv_n = 1.0 / (double)c.n;
@@ -241,11 +316,11 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
       }
     }
   }
-  const double a = block_sum(val, sh), b = block_sum(ge, sh), e = block_sum(gs, sh);
+  const double A = block_sum(val, sh), B = block_sum(ge, sh), E = block_sum(gs, sh);
   if (threadIdx.x == 0) {
-    d.part[3 * blockIdx.x + 0] = a;
-    d.part[3 * blockIdx.x + 1] = b;
-    d.part[3 * blockIdx.x + 2] = e;
+    d.part[3 * blockIdx.x + 0] = A;
+    d.part[3 * blockIdx.x + 1] = B;
+    d.part[3 * blockIdx.x + 2] = E;
   }
 }
 
@@ -284,12 +359,13 @@ __global__ void k_reverse(P c, D d) {
 
 __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
   __shared__ double sh[32];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tid / kLanes, lane = tid % kLanes;
   double te = 0, ts = 0;
+  double hx = 0, hy = 0, hz = 0, fx = 0, fy = 0, fz = 0, sx = 0, sy = 0, sz = 0;
   if (i < c.n) {
     const double4_32a qi = qh[i], vi = d.tmp[i];
-    double hx = 0, hy = 0, hz = 0, fx = 0, fy = 0, fz = 0, sx = 0, sy = 0, sz = 0;
-    for (int k = 0; k < d.cnt[i]; k++) {
+    for (int k = lane; k < d.cnt[i]; k += kLanes) {
       const int j = d.nbr[(size_t)i * c.cap + k];
       const double4_32a qj = qh[j], vj = d.tmp[j];
       double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
@@ -309,6 +385,11 @@ __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
       sy += t.fs * dy;
       sz += t.fs * dz;
     }
+  }
+  hx = lane_sum(hx); hy = lane_sum(hy); hz = lane_sum(hz);
+  fx = lane_sum(fx); fy = lane_sum(fy); fz = lane_sum(fz);
+  sx = lane_sum(sx); sy = lane_sum(sy); sz = lane_sum(sz);
+  if (i < c.n && lane == 0) {
     const double4_32a b = d.tmp[i];
     // parameter terms: dt * a_p . dF_i/deps (= F_i/eps), dt * a_p . dF_i/dsigma
     te = c.dt * (b.x * fx + b.y * fy + b.z * fz) / c.eps;
@@ -344,7 +425,8 @@ struct mdg_adjoint {
   P c;
   D d;
   cudaStream_t s = nullptr;
-  int grid = 1;
+  int grid = 1;    // one thread per particle
+  int gridp = 1;   // kLanes threads per particle (pair kernels)
   int nck = 0;
   bool forward_done = false;
 };
@@ -371,7 +453,7 @@ cudaError_t aalloc(T **p, size_t n) {
 // One forward step from (q, p): qh_out, then (q, p) updated in place.
 void fwd_step(mdg_adjoint *a, double4_32a *q, double4_32a *p, double4_32a *qh) {
   k_drift<<<a->grid, kT, 0, a->s>>>(a->c, a->d, q, p, qh);
-  k_force<<<a->grid, kT, 0, a->s>>>(a->c, a->d, qh, a->d.F);
+  k_force<<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, a->d.F);
   k_kick_drift<<<a->grid, kT, 0, a->s>>>(a->c, qh, a->d.F, q, p);
 }
 
@@ -404,9 +486,17 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   a->prm = *p;
   memset(&a->d, 0, sizeof(a->d));
   P &c = a->c;
-  for (int k = 0; k < 3; k++) c.L[k] = p->box[k];
+  for (int k = 0; k < 3; k++) {
+    c.L[k] = p->box[k];
+    c.inv_L[k] = 1.0 / p->box[k];
+  }
   c.eps = p->epsilon;
   c.sig = p->sigma;
+  c.inv_s2 = 1.0 / (p->sigma * p->sigma);
+  c.e_s = p->epsilon / p->sigma;
+  c.e_s2 = c.e_s / p->sigma;
+  c.e_s3 = c.e_s2 / p->sigma;
+  c.e_s4 = c.e_s3 / p->sigma;
   c.dt = p->dt;
   c.dt2 = 0.5 * p->dt;
   c.xc2 = p->cutoff * p->cutoff;
@@ -414,6 +504,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   c.c2 = 6.0 * s14 - 3.0 * s8;  // variables.cc:16-28 in sigma units
   c.c0 = -s12 + s6 - c.c2 / s2;
   c.sl2 = sl * sl;
+  c.sl2f = (sl + 1e-3) * (sl + 1e-3);
   c.half_margin2 = 0.25 * p->margin * p->margin;
   c.volume = p->box[0] * p->box[1] * p->box[2];
   c.n = n;
@@ -421,6 +512,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   const double rho = n / c.volume;
   c.cap = ((int)(rho * 4.18879020478639 * sl * sl * sl * 1.5 + 32) + 7) & ~7;
   a->grid = (n + kT - 1) / kT;
+  a->gridp = (int)(((long long)n * kLanes + kT - 1) / kT);
   a->nck = p->steps / p->checkpoint_every + 1;
   const size_t N = (size_t)n, K = (size_t)p->checkpoint_every;
   D &d = a->d;
@@ -436,7 +528,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   if (e == cudaSuccess) e = aalloc(&d.segqh, N * (K + 1));
   if (e == cudaSuccess) e = aalloc(&d.nbr, N * (size_t)c.cap);
   if (e == cudaSuccess) e = aalloc(&d.cnt, N);
-  if (e == cudaSuccess) e = aalloc(&d.part, 3 * (size_t)a->grid);
+  if (e == cudaSuccess) e = aalloc(&d.part, 3 * (size_t)a->gridp);
   if (e == cudaSuccess) e = aalloc(&d.acc, 3);
   if (e == cudaSuccess) e = aalloc(&d.flag, 2);
   if (e != cudaSuccess) {
@@ -471,22 +563,21 @@ int mdg_adjoint_forward(mdg_adjoint *a, const double *q4, const double *p4, doub
   D &d = a->d;
   MDG_ACK(cudaMemcpyAsync(d.q, q4, bytes, cudaMemcpyHostToDevice, a->s));
   MDG_ACK(cudaMemcpyAsync(d.p, p4, bytes, cudaMemcpyHostToDevice, a->s));
-  MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
   MDG_ACK(cudaMemsetAsync(d.flag, 0, 2 * sizeof(int), a->s));
   MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
-  k_build<<<a->grid, kT, 0, a->s>>>(a->c, d);
   int flag[2] = {0, 0};
-  MDG_ACK(cudaMemcpyAsync(flag, d.flag, sizeof flag, cudaMemcpyDeviceToHost, a->s));
-  MDG_ACK(cudaStreamSynchronize(a->s));
-  if (flag[0]) return afail(a, MDG_ERR_CAPACITY, "adjoint pair list capacity exceeded");
   const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
   const double w = 1.0 / Ns;
   MDG_ACK(cudaMemcpyAsync(d.ckq, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
   MDG_ACK(cudaMemcpyAsync(d.ckp, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
   for (int n = 1; n <= Ns; n++) {
+    if ((n - 1) % K == 0) {  // a checkpoint segment starts: its own list
+      MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+      k_build<<<a->grid, kT, 0, a->s>>>(a->c, d, d.q);
+    }
     fwd_step(a, d.q, d.p, d.qh);
-    k_objective<<<a->grid, kT, 0, a->s>>>(a->c, d, d.q, d.p, 0, w);
-    k_accumulate<<<1, 1024, 0, a->s>>>(d, a->grid, w);
+    k_objective<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.q, d.p, 0, w);
+    k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, w);
     if (n % K == 0) {
       MDG_ACK(cudaMemcpyAsync(d.ckq + N * (n / K), d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
       MDG_ACK(cudaMemcpyAsync(d.ckp + N * (n / K), d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
@@ -496,7 +587,9 @@ int mdg_adjoint_forward(mdg_adjoint *a, const double *q4, const double *p4, doub
   MDG_ACK(cudaMemcpyAsync(acc, d.acc, sizeof acc, cudaMemcpyDeviceToHost, a->s));
   MDG_ACK(cudaMemcpyAsync(flag, d.flag, sizeof flag, cudaMemcpyDeviceToHost, a->s));
   MDG_ACK(cudaStreamSynchronize(a->s));
-  if (flag[1]) return afail(a, MDG_ERR_STATE, "a particle moved more than margin/2 over the horizon; raise margin");
+  if (flag[0]) return afail(a, MDG_ERR_CAPACITY, "adjoint pair list capacity exceeded");
+  if (flag[1])
+    return afail(a, MDG_ERR_STATE, "a particle moved more than margin/2 within a checkpoint segment; raise margin");
   *J = acc[0];
   a->forward_done = true;
   return MDG_OK;
@@ -519,6 +612,9 @@ int mdg_adjoint_backward(mdg_adjoint *a, double *dq0, double *dp0, double *deps,
     // recompute the segment from its checkpoint: states 0..len, half steps 1..len
     MDG_ACK(cudaMemcpyAsync(d.segq, d.ckq + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
     MDG_ACK(cudaMemcpyAsync(d.segp, d.ckp + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
+    // the segment's list, built from the same state as in the forward pass
+    MDG_ACK(cudaMemcpyAsync(d.q0, d.segq, bytes, cudaMemcpyDeviceToDevice, a->s));
+    k_build<<<a->grid, kT, 0, a->s>>>(a->c, d, d.segq);
     for (int k = 1; k <= len; k++) {
       MDG_ACK(cudaMemcpyAsync(d.segq + N * k, d.segq + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
       MDG_ACK(cudaMemcpyAsync(d.segp + N * k, d.segp + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
@@ -526,12 +622,12 @@ int mdg_adjoint_backward(mdg_adjoint *a, double *dq0, double *dp0, double *deps,
     }
     for (int k = len; k >= 1; k--) {
       // objective terms of state (seg_start + k)
-      k_objective<<<a->grid, kT, 0, a->s>>>(a->c, d, d.segq + N * k, d.segp + N * k, 1, w);
-      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->grid, w);
+      k_objective<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segq + N * k, d.segp + N * k, 1, w);
+      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, w);
       // reverse the step that produced it
       k_reverse<<<a->grid, kT, 0, a->s>>>(a->c, d);
-      k_reverse_hvp<<<a->grid, kT, 0, a->s>>>(a->c, d, d.segqh + N * k);
-      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->grid, 1.0);
+      k_reverse_hvp<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segqh + N * k);
+      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, 1.0);
     }
     seg_end = seg_start;
   }
