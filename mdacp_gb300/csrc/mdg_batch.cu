@@ -7,11 +7,15 @@
 // the GPU.  Design:
 //   * the grid is a few CTAs per SM; each CTA owns a fixed list of boxes
 //     assigned longest-first to the least-loaded CTA (host, deterministic);
-//   * a CTA advances each of its boxes by one step: when the box's own
-//     displacement test fired it first rebuilds the box's cell list and pair
-//     list in place (counting sort with the cell counters in shared memory,
-//     stable by particle index, same float-first exact acceptance test as the
-//     single-box path), then runs the fused force/kick/drift over the box;
+//   * a CTA advances each of its boxes by one step (the fused force/kick/
+//     drift over the box);
+//   * a box whose displacement test fired is rebuilt at the start of the next
+//     step by two kernels ahead of the persistent one: k_batch_prep (one CTA
+//     per rebuilding box: counting sort with the cell counters in shared
+//     memory, stable by particle index) and k_batch_list (one thread per
+//     particle of every rebuilding box, same float-first exact acceptance test
+//     as the single-box path), so a rebuild is spread over the whole GPU
+//     instead of stalling the CTA that steps the box;
 //   * lanes-per-particle (1, 2 or 4 lanes share one particle's row and reduce
 //     with shuffles), threads per CTA and CTAs per SM are chosen by the
 //     autotuner (mdg_batch_tune);
@@ -69,7 +73,13 @@ struct Dev {
   int *box_rebuild, *box_err, *box_need;
   long long *box_steps, *box_rebuilds, *goal;
   double *partials;  // per box: KE, PE, virial
+  const int *box_of_slot;
 };
+
+// A box takes part in this step's rebuild: flagged, healthy, behind the goal.
+__device__ __forceinline__ bool rebuilding(const Dev &d, int bi, long long goal) {
+  return d.box_rebuild[bi] != 0 && d.box_err[bi] == 0 && d.box_steps[bi] < goal;
+}
 
 __device__ __forceinline__ double rcp_hh3(double x) {
   double y;
@@ -124,11 +134,11 @@ __device__ void cta_scan(int *cnt, int *out, int m) {
   __syncthreads();
 }
 
-// Rebuild of one box by the whole CTA: wrap (one +-L per component), bin,
-// stable reorder by (cell, particle index), mid-step positions, pair list.
-template <int MIXED>
-__device__ void rebuild_box(const Params &P, const Dev &d, const BoxDesc &b, int bi, int par, int *s_cnt,
-                            int *s_start, int *s_err) {
+// Rebuild of one box by the whole CTA, up to the pair list: wrap (one +-L
+// per component), bin, stable reorder by (cell, particle index), cell starts,
+// build-time and mid-step positions.
+__device__ void prep_box(const Params &P, const Dev &d, const BoxDesc &b, int bi, int par, int *s_cnt, int *s_start,
+                         int *s_err) {
   const int n = b.n, o = b.atom_off;
   for (int c = threadIdx.x; c < b.ncell; c += blockDim.x) s_cnt[c] = 0;
   if (threadIdx.x == 0) *s_err = 0;
@@ -210,70 +220,88 @@ __device__ void rebuild_box(const Params &P, const Dev &d, const BoxDesc &b, int
     d.loc[par][o + k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), 0.0f);
   }
   __syncthreads();
-  int need = 0;
-  for (int a = threadIdx.x; a < n; a += blockDim.x) {
-    const float4 fi = d.qf[o + a];
-    int cx, cy, cz;
-    cell_xyz(b, d.cell[o + a], cx, cy, cz);
-    int cnt = 0;
-    for (int oz = -1; oz <= 1; oz++) {
-      int nz = cz + oz, sz = 0;
-      if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
-      const float offz = (float)oz * b.w32[2] + (float)sz * b.dl32[2];
-      for (int oy = -1; oy <= 1; oy++) {
-        int ny = cy + oy, sy = 0;
-        if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
-        const float offy = (float)oy * b.w32[1] + (float)sy * b.dl32[1];
-        for (int ox = -1; ox <= 1; ox++) {
-          int nx = cx + ox, sx = 0;
-          if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
-          const float offx = (float)ox * b.w32[0] + (float)sx * b.dl32[0];
-          const int cc = (nz * b.nc[1] + ny) * b.nc[0] + nx;
-          const int lo = s_start[cc], hi = s_start[cc + 1];
-          const uint32_t code = entry_pack(0, ox, oy, oz);
-          const bool self_cell = (sx | sy | sz) == 0;
-          const float fx = offx - fi.x, fy = offy - fi.y, fz = offz - fi.z;
-          for (int j = lo; j < hi; j++) {
-            const float4 fj = d.qf[o + j];
-            const float ex = fj.x + fx, ey = fj.y + fy, ez = fj.z + fz;
-            const float r2f = ex * ex + ey * ey + ez * ez;
-            if (r2f > P.acc_hi) continue;
-            if (self_cell && j == a) continue;
-            bool take = r2f < P.acc_lo;
-            if (!take) {
-              const double4_32a qi = d.q_end[o + a], qj = d.q_end[o + j];
-              const double xj = sx ? __dadd_rn(qj.x, sx > 0 ? b.L[0] : -b.L[0]) : qj.x;
-              const double yj = sy ? __dadd_rn(qj.y, sy > 0 ? b.L[1] : -b.L[1]) : qj.y;
-              const double zj = sz ? __dadd_rn(qj.z, sz > 0 ? b.L[2] : -b.L[2]) : qj.z;
-              const double dx = __dsub_rn(qi.x, xj), dy = __dsub_rn(qi.y, yj), dz = __dsub_rn(qi.z, zj);
-              const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-              take = r2 <= P.sl2;
-            }
-            if (take) {
-              if (cnt < P.list_cap) d.nl[b.list_off + (long long)cnt * n + a] = ((uint32_t)j << kCodeBits) | code;
-              cnt++;
-            }
+}
+
+// Pair-list row of local particle a of box b (the box's cell starts and
+// build-time positions are in place): the 27 stencil cells with periodic
+// wrap, float-first exact acceptance.  Returns the row length (rows longer
+// than the capacity are truncated and flag the box).
+__device__ int build_row(const Params &P, const Dev &d, const BoxDesc &b, int bi, int a) {
+  const int n = b.n, o = b.atom_off;
+  const int *cstart = d.cell_start + b.cell_off;
+  const float4 fi = d.qf[o + a];
+  int cx, cy, cz;
+  cell_xyz(b, d.cell[o + a], cx, cy, cz);
+  int cnt = 0;
+  for (int oz = -1; oz <= 1; oz++) {
+    int nz = cz + oz, sz = 0;
+    if (nz < 0) { nz += b.nc[2]; sz = -1; } else if (nz >= b.nc[2]) { nz -= b.nc[2]; sz = 1; }
+    const float offz = (float)oz * b.w32[2] + (float)sz * b.dl32[2];
+    for (int oy = -1; oy <= 1; oy++) {
+      int ny = cy + oy, sy = 0;
+      if (ny < 0) { ny += b.nc[1]; sy = -1; } else if (ny >= b.nc[1]) { ny -= b.nc[1]; sy = 1; }
+      const float offy = (float)oy * b.w32[1] + (float)sy * b.dl32[1];
+      for (int ox = -1; ox <= 1; ox++) {
+        int nx = cx + ox, sx = 0;
+        if (nx < 0) { nx += b.nc[0]; sx = -1; } else if (nx >= b.nc[0]) { nx -= b.nc[0]; sx = 1; }
+        const float offx = (float)ox * b.w32[0] + (float)sx * b.dl32[0];
+        const int cc = (nz * b.nc[1] + ny) * b.nc[0] + nx;
+        const int lo = cstart[cc], hi = cstart[cc + 1];
+        const uint32_t code = entry_pack(0, ox, oy, oz);
+        const bool self_cell = (sx | sy | sz) == 0;
+        const float fx = offx - fi.x, fy = offy - fi.y, fz = offz - fi.z;
+        for (int j = lo; j < hi; j++) {
+          const float4 fj = d.qf[o + j];
+          const float ex = fj.x + fx, ey = fj.y + fy, ez = fj.z + fz;
+          const float r2f = ex * ex + ey * ey + ez * ez;
+          if (r2f > P.acc_hi) continue;
+          if (self_cell && j == a) continue;
+          bool take = r2f < P.acc_lo;
+          if (!take) {
+            const double4_32a qi = d.q_end[o + a], qj = d.q_end[o + j];
+            const double xj = sx ? __dadd_rn(qj.x, sx > 0 ? b.L[0] : -b.L[0]) : qj.x;
+            const double yj = sy ? __dadd_rn(qj.y, sy > 0 ? b.L[1] : -b.L[1]) : qj.y;
+            const double zj = sz ? __dadd_rn(qj.z, sz > 0 ? b.L[2] : -b.L[2]) : qj.z;
+            const double dx = __dsub_rn(qi.x, xj), dy = __dsub_rn(qi.y, yj), dz = __dsub_rn(qi.z, zj);
+            const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            take = r2 <= P.sl2;
+          }
+          if (take) {
+            if (cnt < P.list_cap) d.nl[b.list_off + (long long)cnt * n + a] = ((uint32_t)j << kCodeBits) | code;
+            cnt++;
           }
         }
       }
     }
-    d.ncount[o + a] = cnt < P.list_cap ? cnt : P.list_cap;
-    need = max(need, cnt);
   }
-  if (need > P.list_cap) {
-    atomicMax(&d.box_need[bi], need);
-    *s_err = kErrOverflow;
+  d.ncount[o + a] = cnt < P.list_cap ? cnt : P.list_cap;
+  return cnt;
+}
+
+// Rebuild part 1 for every box that rebuilds this step: one CTA per box.
+__global__ void k_batch_prep(Params P, Dev d, int par) {
+  __shared__ int s_cnt[kMaxCellsPerBox];
+  __shared__ int s_start[kMaxCellsPerBox + 1];
+  __shared__ int s_err;
+  const int bi = blockIdx.x;
+  if (!rebuilding(d, bi, *d.goal)) return;  // uniform over the CTA
+  const BoxDesc b = d.boxes[bi];
+  prep_box(P, d, b, bi, par, s_cnt, s_start, &s_err);
+}
+
+// Rebuild part 2: one thread per particle slot of every rebuilding box, so a
+// box's list is built by the whole GPU rather than by the CTA that steps it.
+__global__ void __launch_bounds__(128) k_batch_list(Params P, Dev d, int total) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= total) return;
+  const int bi = d.box_of_slot[s];
+  if (!rebuilding(d, bi, *d.goal)) return;
+  const BoxDesc &b = d.boxes[bi];
+  const int cnt = build_row(P, d, b, bi, s - b.atom_off);
+  if (cnt > P.list_cap) {
+    atomicMax(&d.box_need[bi], cnt);
+    atomicExch(&d.box_err[bi], kErrOverflow);
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (*s_err) {
-      d.box_err[bi] = kErrOverflow;
-    } else {
-      d.box_rebuild[bi] = 0;
-      d.box_rebuilds[bi] += 1;
-    }
-  }
-  __syncthreads();
 }
 
 // Force on local particle a of box b from its row, lanes l = 0..LPI-1 of a group
@@ -348,10 +376,11 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
   return make_double3(fx, fy, fz);
 }
 
+// The advance of every box by one step, one persistent kernel: each CTA
+// steps its boxes in turn.  The lists of the boxes that rebuilt this step
+// were made by k_batch_prep and k_batch_list just before.
 template <int MIXED, int LPI>
 __global__ void k_batch_step(Params P, Dev d, int par) {
-  __shared__ int s_cnt[kMaxCellsPerBox];
-  __shared__ int s_start[kMaxCellsPerBox + 1];
   __shared__ int s_flag[2];
   const long long goal = *d.goal;
   for (int t = d.cta_start[blockIdx.x]; t < d.cta_start[blockIdx.x + 1]; t++) {
@@ -365,13 +394,9 @@ __global__ void k_batch_step(Params P, Dev d, int par) {
     __syncthreads();
     if (!go) continue;
     const BoxDesc b = d.boxes[bi];
-    if (rb) {
-      rebuild_box<MIXED>(P, d, b, bi, par, s_cnt, s_start, &s_flag[0]);
-      if (threadIdx.x == 0) s_flag[1] = d.box_err[bi];
-      __syncthreads();
-      const int err = s_flag[1];
-      __syncthreads();
-      if (err) continue;
+    if (rb && threadIdx.x == 0) {  // the rebuild of this step completed
+      d.box_rebuild[bi] = 0;
+      d.box_rebuilds[bi] += 1;
     }
     const int o = b.atom_off, n = b.n;
     const int groups = blockDim.x / LPI, lane = threadIdx.x % LPI;
@@ -408,6 +433,7 @@ __global__ void k_batch_step(Params P, Dev d, int par) {
       if (any) d.box_rebuild[bi] = 1;
       d.box_steps[bi] += 1;
     }
+    __syncthreads();
   }
 }
 
@@ -571,6 +597,8 @@ int alloc_batch_list(mdg_batch *b, int cap) {
 void launch_batch_step(mdg_batch *b, int par) {
   const int T = b->threads;
   const bool mixed = b->prm.precision == MDG_MIXED;
+  k_batch_prep<<<b->nbox, 256, 0, b->stream>>>(b->P, b->d, par);
+  k_batch_list<<<(b->total + 127) / 128, 128, 0, b->stream>>>(b->P, b->d, b->total);
 #define MDG_BSTEP(M, L) k_batch_step<M, L><<<b->grid, T, 0, b->stream>>>(b->P, b->d, par)
   if (mixed) {
     if (b->lpi == 4) MDG_BSTEP(1, 4); else if (b->lpi == 2) MDG_BSTEP(1, 2); else MDG_BSTEP(1, 1);
@@ -578,7 +606,7 @@ void launch_batch_step(mdg_batch *b, int par) {
     if (b->lpi == 4) MDG_BSTEP(0, 4); else if (b->lpi == 2) MDG_BSTEP(0, 2); else MDG_BSTEP(0, 1);
   }
 #undef MDG_BSTEP
-  b->launches += 1;
+  b->launches += 3;
 }
 
 int run_steps(mdg_batch *b, int nsteps) {
@@ -606,7 +634,7 @@ int run_steps(mdg_batch *b, int nsteps) {
         if (e != cudaSuccess) return bfail(b, MDG_ERR_CUDA, cudaGetErrorString(e));
       }
       MDG_BCK(cudaGraphLaunch(b->gx[par], b->stream));
-      b->launches += 2;
+      b->launches += 6;
       left -= 2;
     } else {
       launch_batch_step(b, par);
@@ -737,6 +765,7 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
   if (e == cudaSuccess) e = balloc(&d.partials, 3 * (size_t)nbox);
   if (e == cudaSuccess) e = balloc(&b->d_box_of_slot, n);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_box_of_slot, b->box_of_slot.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+  d.box_of_slot = b->d_box_of_slot;
   if (e != cudaSuccess) {
     fprintf(stderr, "mdg_batch_create: %s\n", cudaGetErrorString(e));
     mdg_batch_destroy(b);
