@@ -40,7 +40,7 @@ constexpr int kStepThreads = 128;
 #define MDG_STEP_MIN_BLOCKS 12
 #endif
 #ifndef MDG_PRUNE_MIN_BLOCKS
-#define MDG_PRUNE_MIN_BLOCKS 1
+#define MDG_PRUNE_MIN_BLOCKS 8
 #endif
 // Neighbour-list entries whose index and position loads are issued together
 // in the mixed-form force loop.
