@@ -55,9 +55,11 @@ def parse():
     ap.add_argument("--density", type=float, default=DENSITY,
                     help="number density of the NVE workload (the large configuration runs 0.5 and 0.8)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
-    ap.add_argument("--workload", default="nve4m", choices=["nve4m", "langevin16m", "batch1024", "adjoint4k"],
+    ap.add_argument("--workload", default="nve4m",
+                    choices=["nve4m", "langevin16m", "batch1024", "adjoint4k", "io4m"],
                     help="nve4m: the headline (4M atoms NVE); langevin16m: 160^3 FCC Langevin NVT; "
-                         "batch1024: 1024 replica boxes; adjoint4k: 4000-atom trajectory gradient")
+                         "batch1024: 1024 replica boxes; adjoint4k: 4000-atom trajectory gradient; "
+                         "io4m: the reference's dump and stream files of the 4M-atom state")
     return ap.parse_args()
 
 
@@ -434,10 +436,47 @@ def run_adjoint4k(args):
     print(json.dumps(line), flush=True)
 
 
+def run_io4m(args):
+    """Writes the 4M-atom state in the reference's dump (SaveAsDumpFile) and
+    stream (SaveToStream) formats: from the device handle (state read back,
+    then written) and from host arrays; wall clock, file in a temporary
+    directory, median of a few repetitions."""
+    from mdacp_gb300 import io as mio
+    from mdacp_gb300.manager import MDManager
+    q, p, L = workload(args.cells, 1, args.density)
+    n = len(q)
+    m = MDManager(L, capacity=n, cutoff=RC, margin=MARGIN, dt=DT, precision="mixed")
+    m.set_state(q, p)
+    m.calculate(10)
+    qs, ps = m.state()
+    res = {}
+    with tempfile.TemporaryDirectory(prefix="mdg_io_") as d:
+        fn = os.path.join(d, "conf.dump")
+        for name, fun, nbytes in (("save_dump (device state)", lambda: m.save_dump(fn), 48 * n),
+                                  ("write_dump (host arrays)", lambda: mio.write_dump(fn, qs, ps), 48 * n),
+                                  ("write_stream (host arrays)", lambda: mio.write_stream(fn, qs, ps), 64 * n)):
+            ts = []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                fun()
+                ts.append(time.perf_counter() - t0)
+            ts.sort()
+            res[name] = {"ms": ts[2] * 1e3, "GB_per_s": nbytes / ts[2] / 1e9, "bytes": nbytes}
+    m.close()
+    v = n / (res["save_dump (device state)"]["ms"] * 1e-3)
+    cfg = {"workload": "dump and stream files of the %d-atom NVE state" % n, "atoms": n}
+    line = base_line("atoms/s written in the reference's dump format from the device state", v, 1, 5, 0,
+                     res["save_dump (device state)"]["ms"], cfg, "f64")
+    line["unit"] = "atoms/s"
+    line.update({"files": res})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "mdg" and args.workload != "nve4m":
-        {"langevin16m": run_langevin16m, "batch1024": run_batch1024, "adjoint4k": run_adjoint4k}[args.workload](args)
+        {"langevin16m": run_langevin16m, "batch1024": run_batch1024, "adjoint4k": run_adjoint4k,
+         "io4m": run_io4m}[args.workload](args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -249,6 +249,32 @@ int mdg_adjoint_backward(mdg_adjoint *a, double *dq0, double *dp0, double *depsi
 int mdg_observe_noalloc(const double *q4_dev, const double *p4_dev, int32_t n, const double box[3], double cutoff,
                         double *out3_dev, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Output and restart formats of the reference, written from host [n][4]
+ * arrays (no GPU needed), byte for byte what the reference's writers produce
+ * for the same particles in the same order.  append != 0 appends (the
+ * reference truncates once and then appends unit by unit). */
+/* MDManager::SaveAsDumpFile (mdmanager.cc:475-505): qx qy qz px py pz doubles. */
+int mdg_write_dump(const char *path, const double *q4, const double *p4, int32_t n, int32_t append);
+/* MDUnit::SaveAsCdview (mdunit.cc:52-67): "0 type qx qy qz px py pz" lines;
+ * type may be NULL (all 0, the LJ particle type of AddParticle). */
+int mdg_write_cdview(const char *path, const double *q4, const double *p4, const int32_t *type, int32_t n,
+                     int32_t append);
+/* Variables::SaveConfiguration (variables.cc:45-56): "qx qy qz px py pz" lines
+ * (real particles; the reference's file also holds its ghost copies). */
+int mdg_write_configuration(const char *path, const double *q4, const double *p4, int32_t n);
+/* Variables::SaveToStream (variables.cc:111-118): per particle q[d], p[d] for d = 0..3. */
+int mdg_write_stream(const char *path, const double *q4, const double *p4, int32_t n, int32_t append);
+/* Variables::LoadFromStream (variables.cc:121-131): int32 count, double time,
+ * double zeta, then the stream body.  *n receives the count; MDG_ERR_CAPACITY
+ * when it exceeds capacity (nothing else is read). */
+int mdg_read_stream(const char *path, double *q4, double *p4, int32_t capacity, int32_t *n, double *time,
+                    double *zeta);
+/* MDManager::SaveAsDumpFile / SaveAsCdview of a handle's current state
+ * (caller order, type 0). */
+int mdg_save_dump(mdg_handle *h, const char *path);
+int mdg_save_cdview(mdg_handle *h, const char *path);
+
 #ifdef __cplusplus
 }
 #endif

@@ -226,6 +226,28 @@ void MDManager::SaveStateRaw(const std::string &path) {
   fclose(f);
 }
 
+void MDManager::SaveAsDumpFile(const char *filename) {
+  Sync();
+  Check(mdg_save_dump(h_, filename), "mdg_save_dump");
+}
+
+void MDManager::SaveAsDumpFileSequential() {
+  char filename[256];
+  snprintf(filename, sizeof filename, "conf%04d.dump", dump_index_++);
+  SaveAsDumpFile(filename);
+}
+
+void MDManager::SaveAsCdview(const char *filename) {
+  Sync();
+  Check(mdg_save_cdview(h_, filename), "mdg_save_cdview");
+}
+
+void MDManager::SaveAsCdviewSequential() {
+  char filename[256];
+  snprintf(filename, sizeof filename, "conf%04d.cd", cdview_index_++);
+  SaveAsCdview(filename);
+}
+
 void MakeFCC(const Parameter &param, MDManager &m) {
   const double *L = m.GetSystemSize();
   const double density = param.GetDoubleDef("Density", 0.5);

@@ -80,6 +80,12 @@ class MDManager {
   // state exchange in the reference's [n][4] layout
   void GetState(std::vector<double> &q4, std::vector<double> &p4);
   void SaveStateRaw(const std::string &path);  // int64 n, n x {q,p}
+  // the reference's writers (mdmanager.h:54-57): conf%04d.dump / conf%04d.cd
+  // in the working directory for the Sequential forms
+  void SaveAsDumpFile(const char *filename);
+  void SaveAsDumpFileSequential();
+  void SaveAsCdview(const char *filename);
+  void SaveAsCdviewSequential();
   mdg_handle *Handle() { return h_; }
 
  private:
@@ -91,6 +97,7 @@ class MDManager {
   std::vector<double> q_, p_;
   bool uploaded_ = false;
   double s_time_ = 0.0;
+  int dump_index_ = 0, cdview_index_ = 0;
 };
 
 // ConfigurationMaker (confmaker.cc:9-44): FCC sites with a 1e-7 offset.

@@ -39,6 +39,13 @@ void setup(const mdghost::Parameter &param, mdghost::MDManager &m) {
   if (param.Contains("InitialStateFile")) m.SaveStateRaw(param.GetStringDef("InitialStateFile", ""));
 }
 
+// Added keys FinalDumpFile / FinalCdviewFile: the final state in the
+// reference's dump (SaveAsDumpFile) and CDView (SaveAsCdview) formats.
+void final_files(const mdghost::Parameter &param, mdghost::MDManager &m) {
+  if (param.Contains("FinalDumpFile")) m.SaveAsDumpFile(param.GetStringDef("FinalDumpFile", "").c_str());
+  if (param.Contains("FinalCdviewFile")) m.SaveAsCdview(param.GetStringDef("FinalCdviewFile", "").c_str());
+}
+
 void run_benchmark(const mdghost::Parameter &param) {
   const int n = lattice_count(param);
   mdghost::MDManager m(param, n > 0 ? n : 1);
@@ -62,6 +69,7 @@ void run_benchmark(const mdghost::Parameter &param) {
   const double sec = now() - start;
   const unsigned long pn = m.GetTotalParticleNumber();
   printf("# N = %lu %g [SEC] %g [MUPS]\n", pn, sec, (double)LOOP * (double)pn / sec / 1.0e6);
+  final_files(param, m);
 }
 
 void run_langevin(const mdghost::Parameter &param) {

@@ -92,6 +92,14 @@ class MDManager:
         self._ck(self.lib.mdg_get_state(self._h, _dp(q4), _dp(p4)))
         return q4[:, :3], p4[:, :3]
 
+    def save_dump(self, path):
+        """MDManager::SaveAsDumpFile of the current state (mdmanager.cc:475-505)."""
+        self._ck(self.lib.mdg_save_dump(self._h, str(path).encode()))
+
+    def save_cdview(self, path):
+        """MDManager::SaveAsCdview of the current state (mdmanager.cc:90-105)."""
+        self._ck(self.lib.mdg_save_cdview(self._h, str(path).encode()))
+
     # hot path ------------------------------------------------------------
     def make_pairlist(self):
         self._ck(self.lib.mdg_make_pairlist(self._h))

@@ -57,6 +57,15 @@ SIGNATURES = {
     "mdg_set_state_device": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32]),
     "mdg_get_state_device": (ctypes.c_int, [_P, _P, _P]),
     "mdg_observe_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int32, _D, ctypes.c_double, _P, _P]),
+    "mdg_write_dump": (ctypes.c_int, [ctypes.c_char_p, _D, _D, ctypes.c_int32, ctypes.c_int32]),
+    "mdg_write_cdview": (ctypes.c_int, [ctypes.c_char_p, _D, _D, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                                        ctypes.c_int32]),
+    "mdg_write_configuration": (ctypes.c_int, [ctypes.c_char_p, _D, _D, ctypes.c_int32]),
+    "mdg_write_stream": (ctypes.c_int, [ctypes.c_char_p, _D, _D, ctypes.c_int32, ctypes.c_int32]),
+    "mdg_read_stream": (ctypes.c_int, [ctypes.c_char_p, _D, _D, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                       _D, _D]),
+    "mdg_save_dump": (ctypes.c_int, [_P, ctypes.c_char_p]),
+    "mdg_save_cdview": (ctypes.c_int, [_P, ctypes.c_char_p]),
 }
 
 _lib = None

@@ -10,7 +10,7 @@
 // (observer.h:13-16, mdunit.h:73), which hands an observer the unit's MeshList.
 //
 // .cfg keys read here (all other keys are the reference's own):
-//   OracleTask=pairs|force|trace|bench   what to run
+//   OracleTask=pairs|force|trace|bench|write   what to run
 //   OracleInput=<file>                    int64 n, then n x {qx qy qz px py pz} doubles
 //   OracleOutput=<prefix>                 output file prefix
 //   OracleBufferLength=<margin>           overrides BufferLength (simulationinfo.cc:6)
@@ -21,6 +21,7 @@
 // else on this path.
 #include <cstddef>
 #include <cstdint>
+#include <fstream>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -210,6 +211,15 @@ class OracleProject : public Project {
       StateDumper sd(g);
       mdm->ExecuteAllSerial(&sd);
       fclose(g);
+    } else if (task == "write") {
+      // the reference's writers on the loaded state (no step, no ghosts yet):
+      // MDManager::SaveAsDumpFile, MDManager::SaveAsCdview,
+      // MDUnit::SaveConfiguration (writes conf000.cnf), Variables::SaveToStream
+      mdm->SaveAsDumpFile((out + "_dump.bin").c_str());
+      mdm->SaveAsCdview((out + "_cdview.cd").c_str());
+      mdm->GetMDUnit(0)->SaveConfiguration();
+      std::ofstream fs((out + "_stream.bin").c_str(), std::ios::binary);
+      mdm->GetMDUnit(0)->GetVariables()->SaveToStream(fs);
     } else if (task == "bench") {
       // Timed like Benchmark::Run (benchmark.cc:24-51): list build and warm-up
       // outside, the stepping loop with its periodic observation inside.

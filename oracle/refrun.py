@@ -75,6 +75,11 @@ def run(task, q, p, L, rc=2.5, margin=0.5, dt=0.001, steps=100, observe_every=10
         fn = os.path.join(d, "o_trace.bin")
         if os.path.exists(fn):
             out["trace"] = np.fromfile(fn, dtype="<f8").reshape(-1, 7)
+        for key, fn in (("dump", "o_dump.bin"), ("cdview", "o_cdview.cd"), ("configuration", "conf000.cnf"),
+                        ("stream", "o_stream.bin")):
+            if os.path.exists(os.path.join(d, fn)):
+                with open(os.path.join(d, fn), "rb") as f:
+                    out[key] = f.read()
         fn = os.path.join(d, "o_state.bin")
         if os.path.exists(fn):
             rec = np.fromfile(fn, dtype="<f8").reshape(-1, 7)

@@ -13,6 +13,9 @@ Each fixture stores the injected input and the reference's outputs:
   langevin.npz   2048 atoms, the reference's Langevin project at T=0.9,
                  gamma=1.0, dt=0.005, Seed=12345 (mt19937 noise): temperature
                  trace over 3000 steps, for statistical comparison.
+  io_small.npz   108 atoms: the bytes of the reference's writers for the
+                 loaded state (SaveAsDumpFile, SaveAsCdview with type = input
+                 index, MDUnit::SaveConfiguration, Variables::SaveToStream).
 
 Run from the repository root: python tests/golden/make_golden.py
 """
@@ -50,12 +53,20 @@ def langevin_fixture():
                         temperature=0.9, gamma=1.0, trace=tr["trace"])
 
 
+def io_fixture():
+    q, p, L = liquid_like(0.5, 3, seed=5)
+    o = refrun.run("write", q, p, L, rc=RC, margin=MARGIN)
+    blobs = {k: np.frombuffer(o[k], dtype=np.uint8) for k in ("dump", "cdview", "configuration", "stream")}
+    np.savez_compressed(os.path.join(HERE, "io_small"), q=q, p=p, L=L, **blobs)
+
+
 if __name__ == "__main__":
     if not refrun.available(RC):
         refrun.build()
     nve_fixture("c1_small", 0.5, 8, seed=1)
     nve_fixture("rho08", 0.8, 6, seed=2)
     langevin_fixture()
+    io_fixture()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

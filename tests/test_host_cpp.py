@@ -55,7 +55,7 @@ def test_benchmark_project_matches_oracle(host_bin, tmp_path):
     init = str(tmp_path / "init.bin")
     text = ("Mode=Benchmark\nSystemSize=16\nDensity=0.5\nInitialVelocity=1.7320508\nThermalizeLoop=0\n"
             "TotalLoop=200\nObserveLoop=50\nTimeStep=0.001\nCutoffLength=2.5\nBufferLength=0.5\n"
-            "InitialStateFile=%s\n" % init)
+            "InitialStateFile=%s\nFinalDumpFile=%s\n" % (init, tmp_path / "final.dump"))
     out = subprocess.run([host_bin, _cfg(tmp_path, text)], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     rows = np.array([[float(x) for x in l.split()[:4]] for l in out.stdout.splitlines() if l.endswith("#observe")])
@@ -70,6 +70,13 @@ def test_benchmark_project_matches_oracle(host_bin, tmp_path):
         T, P, E = s.observe()[:3]
         ref.append([c * 0.001, T, P, E])
     np.testing.assert_allclose(rows, np.array(ref), rtol=1e-10, atol=1e-12)
+    # the final state in the reference's dump format (qx qy qz px py pz doubles)
+    s.calculate(200 - done)
+    qf, pf = s.state()
+    dump = np.fromfile(tmp_path / "final.dump", dtype="<f8").reshape(-1, 6)
+    assert dump.shape == (2048, 6)
+    dq = (dump[:, :3] - qf + 8.0) % 16.0 - 8.0
+    assert np.abs(dq).max() < 1e-9 and np.abs(dump[:, 3:] - pf).max() < 1e-9
 
 
 @pytest.mark.gpu
