@@ -46,10 +46,13 @@ int mdg_write_dump(const char *path, const double *q4, const double *p4, int32_t
   if (!path || n < 0 || (n > 0 && (!q4 || !p4))) return MDG_ERR_INVALID;
   std::ofstream ofs(path, mode(append != 0, true));
   if (!ofs) return MDG_ERR_INVALID;
-  for (int32_t i = 0; i < n; i++) {
-    const double rec[6] = {q4[4 * i + 0], q4[4 * i + 1], q4[4 * i + 2], p4[4 * i + 0], p4[4 * i + 1], p4[4 * i + 2]};
-    ofs.write(reinterpret_cast<const char *>(rec), sizeof rec);
-  }
+  std::vector<double> buf((size_t)n * 6);
+  for (int32_t i = 0; i < n; i++)
+    for (int d = 0; d < 3; d++) {
+      buf[6 * (size_t)i + d] = q4[4 * i + d];
+      buf[6 * (size_t)i + 3 + d] = p4[4 * i + d];
+    }
+  ofs.write(reinterpret_cast<const char *>(buf.data()), (std::streamsize)(buf.size() * sizeof(double)));
   return ofs ? MDG_OK : MDG_ERR_INVALID;
 }
 
@@ -80,11 +83,13 @@ int mdg_write_stream(const char *path, const double *q4, const double *p4, int32
   if (!path || n < 0 || (n > 0 && (!q4 || !p4))) return MDG_ERR_INVALID;
   std::ofstream ofs(path, mode(append != 0, true));
   if (!ofs) return MDG_ERR_INVALID;
+  std::vector<double> buf((size_t)n * 8);
   for (int32_t i = 0; i < n; i++)
     for (int d = 0; d < 4; d++) {
-      ofs.write(reinterpret_cast<const char *>(&q4[4 * i + d]), sizeof(double));
-      ofs.write(reinterpret_cast<const char *>(&p4[4 * i + d]), sizeof(double));
+      buf[8 * (size_t)i + 2 * d] = q4[4 * i + d];
+      buf[8 * (size_t)i + 2 * d + 1] = p4[4 * i + d];
     }
+  ofs.write(reinterpret_cast<const char *>(buf.data()), (std::streamsize)(buf.size() * sizeof(double)));
   return ofs ? MDG_OK : MDG_ERR_INVALID;
 }
 
