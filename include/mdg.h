@@ -275,6 +275,30 @@ int mdg_read_stream(const char *path, double *q4, double *p4, int32_t capacity, 
 int mdg_save_dump(mdg_handle *h, const char *path);
 int mdg_save_cdview(mdg_handle *h, const char *path);
 
+/* ------------------------------------------------------------------------
+ * Initial conditions of the reference's makers, generated on the device.
+ * Positions are bit-identical to the reference's for the same box and
+ * parameters (same site order); velocities agree to a few ulps (device
+ * cos/sin).  The functions allocate temporary device memory and synchronise
+ * `stream` (a cudaStream_t; NULL = legacy default stream). */
+enum mdg_maker {
+  MDG_MAKER_FCC = 0,      /* ConfigurationMaker (confmaker.cc:9-44) */
+  MDG_MAKER_EXTRACT = 1,  /* ExtractConfigurationMaker (confmaker.cc:174-252) for one unit spanning the box */
+  MDG_MAKER_DROPLET = 2   /* DropletMaker (burst.cc:10-61): sites within `radius` of the box centre */
+};
+/* Writes the maker's positions to q4_dev ([capacity][4], lane 3 zero); *n
+ * receives the count (MDG_ERR_CAPACITY, nothing written, when it exceeds
+ * capacity).  unit_id seeds ExtractConfigurationMaker's mt19937 as
+ * MDUnit::GetID does (0 for the single-unit drop-in). */
+int mdg_make_configuration(const double box[3], int32_t maker, double density, double radius, int32_t unit_id,
+                           double *q4_dev, int32_t capacity, int32_t *n, void *stream);
+/* Variables::SetInitialVelocity (variables.cc:82-108): p4_dev[n][4] <- speed v0,
+ * directions from mt19937(seed), mean subtracted. */
+int mdg_make_velocity(double v0, int32_t seed, double *p4_dev, int32_t n, void *stream);
+/* Both into a handle's state (MDManager's makers + SetInitialVelocity(v0),
+ * seed = unit id 0); v0 = 0 leaves the momenta zero. */
+int mdg_make_state(mdg_handle *h, int32_t maker, double density, double radius, double v0);
+
 #ifdef __cplusplus
 }
 #endif

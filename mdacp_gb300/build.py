@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmdg.so")
 SOURCES = ["mdg_cells.cu", "mdg_list.cu", "mdg_step.cu", "mdg_batch.cu", "mdg_api.cu", "mdg_adjoint.cu", "mdg_noalloc.cu",
-           "mdg_io.cu"]
+           "mdg_io.cu", "mdg_init.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

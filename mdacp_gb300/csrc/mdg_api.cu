@@ -529,6 +529,25 @@ int mdg_set_state_device(mdg_handle *h, const double *q4, const double *p4, int3
   return set_state_common(h, n);
 }
 
+int mdg_make_state(mdg_handle *h, int32_t maker, double density, double radius, double v0) {
+  int rc = check_handle(h, false);
+  if (rc) return rc;
+  int32_t n = 0;
+  rc = mdg_make_configuration(h->g.L, maker, density, radius, 0, (double *)h->d.io4, h->cap, &n, h->stream);
+  if (rc == MDG_ERR_CAPACITY) return fail(h, rc, "the configuration has more particles than the handle capacity");
+  if (rc) return fail(h, rc, "configuration maker failed");
+  if (n <= 0) return fail(h, MDG_ERR_INVALID, "the configuration is empty");
+  MDG_CK(cudaMemsetAsync(h->d.io4b, 0, (size_t)n * sizeof(double4_32a), h->stream));
+  if (v0 != 0.0) {
+    rc = mdg_make_velocity(v0, 0, (double *)h->d.io4b, n, h->stream);
+    if (rc) return fail(h, rc, "velocity maker failed");
+  }
+  h->g.n = n;
+  mdg::launch_sort_in(h->g, h->d, h->d.io4, h->d.io4b, h->stream);
+  h->launches += 1;
+  return set_state_common(h, n);
+}
+
 int mdg_get_state(mdg_handle *h, double *q4, double *p4) {
   int rc = check_handle(h, true);
   if (rc) return rc;

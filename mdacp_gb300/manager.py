@@ -92,6 +92,18 @@ class MDManager:
         self._ck(self.lib.mdg_get_state(self._h, _dp(q4), _dp(p4)))
         return q4[:, :3], p4[:, :3]
 
+    def make_state(self, maker, density, radius=0.0, v0=0.0):
+        """The reference's configuration makers and SetInitialVelocity, on the device.
+
+        maker: "fcc" (ConfigurationMaker, confmaker.cc:9-44), "extract"
+        (ExtractConfigurationMaker for one unit spanning the box,
+        confmaker.cc:174-252) or "droplet" (DropletMaker, burst.cc:10-61, sites
+        within `radius` of the centre).  v0 > 0 draws velocities as
+        Variables::SetInitialVelocity(v0, 0) (variables.cc:82-108).
+        """
+        self._ck(self.lib.mdg_make_state(self._h, native.MAKERS[maker], float(density), float(radius), float(v0)))
+        self.n = self.stats()["particles"]
+
     def save_dump(self, path):
         """MDManager::SaveAsDumpFile of the current state (mdmanager.cc:475-505)."""
         self._ck(self.lib.mdg_save_dump(self._h, str(path).encode()))

@@ -10,7 +10,10 @@
 // (observer.h:13-16, mdunit.h:73), which hands an observer the unit's MeshList.
 //
 // .cfg keys read here (all other keys are the reference's own):
-//   OracleTask=pairs|force|trace|bench|write   what to run
+//   OracleTask=pairs|force|trace|bench|write|make   what to run
+//   OracleMaker=fcc|extract (task make: ConfigurationMaker or
+//     ExtractConfigurationMaker on the empty system, then
+//     MDManager::SetInitialVelocity(InitialVelocity); Density as the reference reads it)
 //   OracleInput=<file>                    int64 n, then n x {qx qy qz px py pz} doubles
 //   OracleOutput=<prefix>                 output file prefix
 //   OracleBufferLength=<margin>           overrides BufferLength (simulationinfo.cc:6)
@@ -30,6 +33,7 @@
 #include <tuple>
 #include <omp.h>
 #include "projectmanager.h"
+#include "confmaker.h"
 #include "communicator.h"
 #include "mpistream.h"
 
@@ -124,6 +128,20 @@ class PairDumper : public DoubleObserver {
   }
 };
 
+// Unit particles in order: q, p (6 doubles each).
+class OrderDumper : public Executor {
+  FILE *out;
+ public:
+  OrderDumper(FILE *f) : out(f) {}
+  void Execute(MDUnit *mdu) {
+    Variables *v = mdu->GetVariables();
+    for (int i = 0; i < v->GetParticleNumber(); i++) {
+      double rec[6] = {v->q[i][X], v->q[i][Y], v->q[i][Z], v->p[i][X], v->p[i][Y], v->p[i][Z]};
+      fwrite(rec, sizeof(double), 6, out);
+    }
+  }
+};
+
 class StateDumper : public Executor {
   FILE *out;
  public:
@@ -164,6 +182,22 @@ class OracleProject : public Project {
       sinfo->BufferLength = param->GetDouble("OracleBufferLength");
       sinfo->SearchLength = CUTOFF_LENGTH + sinfo->BufferLength;
       for (int i = 0; i < mdm->GetTotalThreads(); i++) mdm->GetMDUnit(i)->ChangeScale(1.0);
+    }
+    if (task == "make") {
+      const std::string maker = param->GetStringDef("OracleMaker", "fcc");
+      if (maker == "extract") {
+        ExtractConfigurationMaker c(param);
+        mdm->ExecuteAll(&c);
+      } else {
+        ConfigurationMaker c(param);
+        mdm->ExecuteAll(&c);
+      }
+      if (param->Contains("InitialVelocity")) mdm->SetInitialVelocity(param->GetDouble("InitialVelocity"));
+      FILE *f = fopen((out + "_made.bin").c_str(), "wb");
+      OrderDumper od(f);
+      mdm->ExecuteAllSerial(&od);
+      fclose(f);
+      return;
     }
     InputState s;
     if (!read_input(param->GetStringDef("OracleInput", "oracle_in.bin"), s)) {

@@ -80,6 +80,10 @@ def run(task, q, p, L, rc=2.5, margin=0.5, dt=0.001, steps=100, observe_every=10
             if os.path.exists(os.path.join(d, fn)):
                 with open(os.path.join(d, fn), "rb") as f:
                     out[key] = f.read()
+        fn = os.path.join(d, "o_made.bin")
+        if os.path.exists(fn):
+            rec = np.fromfile(fn, dtype="<f8").reshape(-1, 6)
+            out["q"], out["p"] = rec[:, :3].copy(), rec[:, 3:].copy()
         fn = os.path.join(d, "o_state.bin")
         if os.path.exists(fn):
             rec = np.fromfile(fn, dtype="<f8").reshape(-1, 7)

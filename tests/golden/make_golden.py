@@ -16,6 +16,9 @@ Each fixture stores the injected input and the reference's outputs:
   io_small.npz   108 atoms: the bytes of the reference's writers for the
                  loaded state (SaveAsDumpFile, SaveAsCdview with type = input
                  index, MDUnit::SaveConfiguration, Variables::SaveToStream).
+  makers.npz     the reference's ConfigurationMaker and ExtractConfigurationMaker
+                 states (positions, then MDManager::SetInitialVelocity(1.5)) for
+                 a few boxes and densities, in the unit's particle order.
 
 Run from the repository root: python tests/golden/make_golden.py
 """
@@ -60,6 +63,21 @@ def io_fixture():
     np.savez_compressed(os.path.join(HERE, "io_small"), q=q, p=p, L=L, **blobs)
 
 
+MAKER_CASES = [("fcc", (10.0, 10.0, 10.0), 0.5), ("fcc", (10.0, 12.0, 11.0), 0.8), ("extract", (10.0,) * 3, 0.5),
+               ("extract", (23.7,) * 3, 0.8), ("extract", (30.0,) * 3, 0.5)]
+
+
+def makers_fixture():
+    out = {}
+    dummy = np.zeros((1, 3))
+    for k, (maker, L, rho) in enumerate(MAKER_CASES):
+        o = refrun.run("make", dummy, dummy, np.array(L), rc=RC, margin=MARGIN,
+                       extra={"OracleMaker": maker, "Density": rho, "InitialVelocity": 1.5})
+        out["q%d" % k], out["p%d" % k] = o["q"], o["p"]
+        out["L%d" % k], out["rho%d" % k] = np.array(L), rho
+    np.savez_compressed(os.path.join(HERE, "makers"), makers=np.array([m for m, _, _ in MAKER_CASES]), **out)
+
+
 if __name__ == "__main__":
     if not refrun.available(RC):
         refrun.build()
@@ -67,6 +85,7 @@ if __name__ == "__main__":
     nve_fixture("rho08", 0.8, 6, seed=2)
     langevin_fixture()
     io_fixture()
+    makers_fixture()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
