@@ -56,10 +56,11 @@ def parse():
                     help="number density of the NVE workload (the large configuration runs 0.5 and 0.8)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--workload", default="nve4m",
-                    choices=["nve4m", "langevin16m", "batch1024", "adjoint4k", "io4m"],
+                    choices=["nve4m", "langevin16m", "batch1024", "adjoint4k", "io4m", "init16m"],
                     help="nve4m: the headline (4M atoms NVE); langevin16m: 160^3 FCC Langevin NVT; "
                          "batch1024: 1024 replica boxes; adjoint4k: 4000-atom trajectory gradient; "
-                         "io4m: the reference's dump and stream files of the 4M-atom state")
+                         "io4m: the reference's dump and stream files of the 4M-atom state; "
+                         "init16m: the reference's exact-density initial state of the 16.4M-atom box, on the device")
     return ap.parse_args()
 
 
@@ -472,11 +473,47 @@ def run_io4m(args):
     print(json.dumps(line), flush=True)
 
 
+def run_init16m(args):
+    """ExtractConfigurationMaker + SetInitialVelocity (the reference Benchmark
+    project's initial state) for the 160^3-cell box at density 0.5 (L = 320,
+    16,384,000 atoms) on the device, against the reference's algorithm on the
+    host cores (oracle/makers.cc: the same generator and linear search for
+    distinct deletions) for the 4M-atom box (L = 200)."""
+    from mdacp_gb300.manager import MDManager
+    L = 320.0
+    n_expect = int(L ** 3 * DENSITY)
+    m = MDManager(L, capacity=n_expect, cutoff=RC, margin=MARGIN, dt=DT, precision="mixed")
+    m.make_state("extract", DENSITY, v0=1.0)  # warm-up (allocations, module load)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        m.make_state("extract", DENSITY, v0=1.0)
+        n = m.stats()["particles"]
+        ts.append(time.perf_counter() - t0)
+    m.close()
+    t = sorted(ts)[1]
+    from oracle import port  # the reference's algorithm, timed as the CPU baseline
+    Lc = 200.0
+    t0 = time.perf_counter()
+    qc = port.make_configuration("extract", Lc, DENSITY)
+    port.initial_velocity(len(qc), 1.0, 0)
+    tc = time.perf_counter() - t0
+    cfg = {"workload": "ExtractConfigurationMaker + SetInitialVelocity, L %.0f, density %.1f, %d atoms" % (
+        L, DENSITY, n), "atoms": n}
+    line = base_line("atoms/s of the reference's initial state made on the device", n / t, 1, 3, 1, t * 1e3, cfg,
+                     "f64")
+    line["unit"] = "atoms/s"
+    line["cpu_baseline"] = {"value": len(qc) / tc, "unit": "atoms/s", "cores": 1, "kind": "port",
+                            "sample": "oracle/makers.cc (the reference's algorithm: std::mt19937, linear search for "
+                                      "distinct deletions) for L %.0f, %d atoms, %.2f s" % (Lc, len(qc), tc)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "mdg" and args.workload != "nve4m":
         {"langevin16m": run_langevin16m, "batch1024": run_batch1024, "adjoint4k": run_adjoint4k,
-         "io4m": run_io4m}[args.workload](args)
+         "io4m": run_io4m, "init16m": run_init16m}[args.workload](args)
         return
     if args.impl == "reference":
         run_reference(args)

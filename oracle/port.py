@@ -30,6 +30,63 @@ def build(force=False):
     return LIB
 
 
+MAKERS_LIB = os.path.join(BUILD, "libmdacp_makers.so")
+
+
+def build_makers(force=False):
+    """Builds the C++ restatement of the reference's configuration makers."""
+    src = os.path.join(HERE, "makers.cc")
+    if not force and os.path.exists(MAKERS_LIB) and os.path.getmtime(MAKERS_LIB) >= os.path.getmtime(src):
+        return MAKERS_LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = MAKERS_LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-Wall", src,
+                           "-o", tmp])
+    os.replace(tmp, MAKERS_LIB)
+    return MAKERS_LIB
+
+
+_makers = None
+
+
+def _mk():
+    global _makers
+    if _makers is None:
+        lib = ctypes.CDLL(build_makers())
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib.orc_make_fcc.restype = ctypes.c_long
+        lib.orc_make_fcc.argtypes = [dp, ctypes.c_double, dp, ctypes.c_long]
+        lib.orc_make_extract.restype = ctypes.c_long
+        lib.orc_make_extract.argtypes = [dp, ctypes.c_double, ctypes.c_int, dp, ctypes.c_long]
+        lib.orc_initial_velocity.restype = None
+        lib.orc_initial_velocity.argtypes = [dp, ctypes.c_long, ctypes.c_double, ctypes.c_int]
+        _makers = lib
+    return _makers
+
+
+def make_configuration(maker, L, density, unit_id=0):
+    """ConfigurationMaker ("fcc") or ExtractConfigurationMaker ("extract") positions, (n, 3)."""
+    L3 = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)))
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib = _mk()
+    if maker == "fcc":
+        n = lib.orc_make_fcc(L3.ctypes.data_as(dp), density, None, 0)
+        q = np.zeros((n, 3))
+        lib.orc_make_fcc(L3.ctypes.data_as(dp), density, q.ctypes.data_as(dp), n)
+    else:
+        n = lib.orc_make_extract(L3.ctypes.data_as(dp), density, unit_id, None, 0)
+        q = np.zeros((n, 3))
+        lib.orc_make_extract(L3.ctypes.data_as(dp), density, unit_id, q.ctypes.data_as(dp), n)
+    return q
+
+
+def initial_velocity(n, v0, seed=0):
+    """Variables::SetInitialVelocity(v0, seed) momenta, (n, 3)."""
+    p = np.zeros((n, 3))
+    _mk().orc_initial_velocity(p.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n, v0, seed)
+    return p
+
+
 class _Params(ctypes.Structure):
     _fields_ = [("L", ctypes.c_double * 3), ("rc", ctypes.c_double), ("margin", ctypes.c_double),
                 ("dt", ctypes.c_double), ("gamma", ctypes.c_double), ("temperature", ctypes.c_double),

@@ -150,3 +150,13 @@ def test_nosehoover_relaxes_temperature():
     s.make_pairlist()
     s.calculate(2000)
     assert abs(s.observe()[0] - 1.0) < 0.2
+
+
+def test_maker_restatement_matches_reference_fixture():
+    # oracle/makers.cc against the states the reference's own makers wrote
+    gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "makers.npz"))
+    for k, maker in enumerate(gold["makers"]):
+        q = port.make_configuration(str(maker), gold["L%d" % k], float(gold["rho%d" % k]))
+        assert np.array_equal(q, gold["q%d" % k])
+        p = port.initial_velocity(len(q), 1.5, 0)
+        np.testing.assert_allclose(p, gold["p%d" % k], rtol=0, atol=1e-15)
