@@ -226,6 +226,15 @@ void MDManager::SaveStateRaw(const std::string &path) {
   fclose(f);
 }
 
+void MDManager::MakeStateOnDevice(int maker, double density, double radius, double v0) {
+  Check(mdg_make_state(h_, maker, density, radius, v0), "mdg_make_state");
+  mdg_stats st;
+  Check(mdg_get_stats(h_, &st), "mdg_get_stats");
+  q_.assign((size_t)st.particles * 4, 0.0);  // the state lives on the device
+  p_.assign((size_t)st.particles * 4, 0.0);
+  uploaded_ = true;
+}
+
 void MDManager::SaveAsDumpFile(const char *filename) {
   Sync();
   Check(mdg_save_dump(h_, filename), "mdg_save_dump");

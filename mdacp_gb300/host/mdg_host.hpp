@@ -80,6 +80,8 @@ class MDManager {
   // state exchange in the reference's [n][4] layout
   void GetState(std::vector<double> &q4, std::vector<double> &p4);
   void SaveStateRaw(const std::string &path);  // int64 n, n x {q,p}
+  // the reference's makers + SetInitialVelocity(v0) on the device (mdg_make_state)
+  void MakeStateOnDevice(int maker, double density, double radius, double v0);
   // the reference's writers (mdmanager.h:54-57): conf%04d.dump / conf%04d.cd
   // in the working directory for the Sequential forms
   void SaveAsDumpFile(const char *filename);

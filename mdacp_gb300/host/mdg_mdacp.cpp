@@ -3,11 +3,15 @@
 // (the reference reads input.cfg when no file is given, mdmanager.cc:18-23).
 //
 // Output lines keep the reference's layout: "time T P E #observe" every
-// ObserveLoop steps and "# N = n sec [SEC] mups [MUPS]" at the end.  Both
-// projects build the lattice with ConfigurationMaker's sites (with the 1e-7
-// offset) and give every particle the fixed-speed isotropic velocity of
-// Variables::SetInitialVelocity seeded with the unit id 0.  Extra key:
-// InitialStateFile=<path> writes the initial state (int64 n, n x {q, p}).
+// ObserveLoop steps and "# N = n sec [SEC] mups [MUPS]" at the end.  The
+// initial state is the reference project's: Benchmark uses
+// ExtractConfigurationMaker (benchmark.cc:15-19, Density default 0.7), made on
+// the device; Langevin uses ConfigurationMaker's sites with the 1e-7 offset
+// (langevin.cc:12-15, Density default 0.5), made on the host; both give the
+// fixed-speed isotropic velocity of Variables::SetInitialVelocity seeded with
+// the unit id 0.  Extra keys: InitialConfiguration=extract|fcc overrides the
+// project's maker; InitialStateFile=<path> writes the initial state (int64 n,
+// n x {q, p}); FinalDumpFile / FinalCdviewFile write the final state.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -33,9 +37,27 @@ void observe_line(mdghost::MDManager &m, bool tag) {
   printf("%.15g %.15g %.15g %.15g%s\n", m.GetSimulationTime(), T, P, E, tag ? " #observe" : "");
 }
 
-void setup(const mdghost::Parameter &param, mdghost::MDManager &m) {
-  mdghost::MakeFCC(param, m);
-  m.SetInitialVelocity(param.GetDoubleDef("InitialVelocity", 1.0), 0);
+std::string maker_of(const mdghost::Parameter &param, const char *project_default) {
+  return param.GetStringDef("InitialConfiguration", project_default);
+}
+
+// Particles the project's maker places (the handle's capacity).
+int maker_count(const mdghost::Parameter &param, const std::string &maker) {
+  if (maker == "extract") {
+    const mdghost::SimulationInfo si(param);
+    return (int)(si.L[0] * si.L[1] * si.L[2] * param.GetDoubleDef("Density", 0.7));
+  }
+  return lattice_count(param);
+}
+
+void setup(const mdghost::Parameter &param, mdghost::MDManager &m, const std::string &maker) {
+  const double v0 = param.GetDoubleDef("InitialVelocity", 1.0);
+  if (maker == "extract") {
+    m.MakeStateOnDevice(MDG_MAKER_EXTRACT, param.GetDoubleDef("Density", 0.7), 0.0, v0);
+  } else {
+    mdghost::MakeFCC(param, m);
+    m.SetInitialVelocity(v0, 0);
+  }
   if (param.Contains("InitialStateFile")) m.SaveStateRaw(param.GetStringDef("InitialStateFile", ""));
 }
 
@@ -47,9 +69,10 @@ void final_files(const mdghost::Parameter &param, mdghost::MDManager &m) {
 }
 
 void run_benchmark(const mdghost::Parameter &param) {
-  const int n = lattice_count(param);
+  const std::string maker = maker_of(param, "extract");
+  const int n = maker_count(param, maker);
   mdghost::MDManager m(param, n > 0 ? n : 1);
-  setup(param, m);
+  setup(param, m, maker);
   const int T_LOOP = param.GetIntegerDef("ThermalizeLoop", 150);
   const int LOOP = param.GetIntegerDef("TotalLoop", 1000);
   const int OBSERVE_LOOP = param.GetIntegerDef("ObserveLoop", 100);
@@ -73,9 +96,10 @@ void run_benchmark(const mdghost::Parameter &param) {
 }
 
 void run_langevin(const mdghost::Parameter &param) {
-  const int n = lattice_count(param);
+  const std::string maker = maker_of(param, "fcc");
+  const int n = maker_count(param, maker);
   mdghost::MDManager m(param, n > 0 ? n : 1);
-  setup(param, m);
+  setup(param, m, maker);
   const int LOOP = param.GetIntegerDef("TotalLoop", 1000);
   const int OBSERVE_LOOP = param.GetIntegerDef("ObserveLoop", 100);
   m.SetSeed(param.GetIntegerDef("Seed", 1));

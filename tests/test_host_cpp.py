@@ -53,8 +53,11 @@ def test_bad_heatbath_rejected(host_bin, tmp_path):
 def test_benchmark_project_matches_oracle(host_bin, tmp_path):
     from oracle import port
     init = str(tmp_path / "init.bin")
+    # ConfigurationMaker sites: the extract lattice puts sites on the box faces,
+    # where the reference's ghost search misses images until the first rebuild
     text = ("Mode=Benchmark\nSystemSize=16\nDensity=0.5\nInitialVelocity=1.7320508\nThermalizeLoop=0\n"
             "TotalLoop=200\nObserveLoop=50\nTimeStep=0.001\nCutoffLength=2.5\nBufferLength=0.5\n"
+            "InitialConfiguration=fcc\n"
             "InitialStateFile=%s\nFinalDumpFile=%s\n" % (init, tmp_path / "final.dump"))
     out = subprocess.run([host_bin, _cfg(tmp_path, text)], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
@@ -88,3 +91,19 @@ def test_langevin_project_runs(host_bin, tmp_path):
     assert out.returncode == 0, out.stdout + out.stderr
     T = np.array([float(l.split()[1]) for l in out.stdout.splitlines() if l and l[0].isdigit()])
     assert len(T) == 20 and abs(T[10:].mean() - 0.9) < 0.08
+
+
+@pytest.mark.gpu
+def test_benchmark_project_starts_from_the_reference_extract_state(host_bin, tmp_path):
+    # Benchmark::Run makes ExtractConfigurationMaker's state (benchmark.cc:15-19)
+    from oracle import port
+    init = str(tmp_path / "init.bin")
+    text = ("Mode=Benchmark\nSystemSize=20\nDensity=0.6\nInitialVelocity=1.2\nThermalizeLoop=0\nTotalLoop=20\n"
+            "ObserveLoop=10\nTimeStep=0.001\nCutoffLength=2.5\nBufferLength=0.5\nInitialStateFile=%s\n" % init)
+    out = subprocess.run([host_bin, _cfg(tmp_path, text)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    raw = np.fromfile(init, dtype="<f8", offset=8).reshape(-1, 6)
+    q = port.make_configuration("extract", 20.0, 0.6)
+    assert raw.shape[0] == len(q) == int(20.0 ** 3 * 0.6)
+    assert np.array_equal(raw[:, :3], q)
+    np.testing.assert_allclose(raw[:, 3:], port.initial_velocity(len(q), 1.2, 0), rtol=0, atol=1e-13)
