@@ -320,9 +320,8 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
     const AxisQuad qy = axis_quad(b.w32[1], b.dl32[1], cy == 0, cy == b.nc[1] - 1, li.y, 0.25f);
     const AxisQuad qz = axis_quad(b.w32[2], b.dl32[2], cz == 0, cz == b.nc[2] - 1, li.z, 0.0625f);
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    for (int k = lane; k < cnt; k += LPI) {
-      const uint32_t e = __ldg(row + (long long)k * n);
-      const float4 lj = __ldg(d.loc[par] + o + entry_slot(e));
+    const float4 *loc = d.loc[par] + o;
+    auto pair = [&](uint32_t e, const float4 &lj) {
       const float tx = step_float(e, 0x03u, 8388609.0f), ty = step_float(e, 0x0Cu, 8388612.0f),
                   tz = step_float(e, 0x30u, 8388624.0f);
       const float dx = lj.x + fmaf(fmaf(qx.b, tx, qx.a), tx, qx.c);
@@ -337,6 +336,22 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
       sx = fmaf(df, dx, sx);
       sy = fmaf(df, dy, sy);
       sz = fmaf(df, dz, sz);
+    };
+    int k = lane;
+    // four entries' index and position loads in flight per lane
+    for (; k + 3 * LPI < cnt; k += 4 * LPI) {
+      uint32_t e[4];
+      float4 l[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) e[u] = __ldg(row + (long long)(k + u * LPI) * n);
+#pragma unroll
+      for (int u = 0; u < 4; u++) l[u] = __ldg(loc + entry_slot(e[u]));
+#pragma unroll
+      for (int u = 0; u < 4; u++) pair(e[u], l[u]);
+    }
+    for (; k < cnt; k += LPI) {
+      const uint32_t e = __ldg(row + (long long)k * n);
+      pair(e, __ldg(loc + entry_slot(e)));
     }
     fx = (double)sx;
     fy = (double)sy;
@@ -379,8 +394,14 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
 // The advance of every box by one step, one persistent kernel: each CTA
 // steps its boxes in turn.  The lists of the boxes that rebuilt this step
 // were made by k_batch_prep and k_batch_list just before.
+// Resident 512-thread blocks per SM the mixed step is compiled for: 2 (64
+// registers) measured 9 % faster on 1,024 boxes than 3 (40 registers); the
+// FP64 form stays at 2 (it spills at 40 registers).
+#ifndef MDG_BATCH_MIN_BLOCKS
+#define MDG_BATCH_MIN_BLOCKS 2
+#endif
 template <int MIXED, int LPI>
-__global__ void k_batch_step(Params P, Dev d, int par) {
+__global__ void __launch_bounds__(512, MIXED ? MDG_BATCH_MIN_BLOCKS : 2) k_batch_step(Params P, Dev d, int par) {
   __shared__ int s_flag[2];
   const long long goal = *d.goal;
   for (int t = d.cta_start[blockIdx.x]; t < d.cta_start[blockIdx.x + 1]; t++) {
@@ -412,18 +433,33 @@ __global__ void k_batch_step(Params P, Dev d, int par) {
       p.z += F.z * P.dt;
       const double4_32a q0 = d.q_mid[par][o + a];
       double4_32a qe = q0, q1 = q0;
-      qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, P.dt2));
-      qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, P.dt2));
-      qe.z = __dadd_rn(q0.z, __dmul_rn(p.z, P.dt2));
-      q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, P.dt2));
-      q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, P.dt2));
-      q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, P.dt2));
+      if (MIXED) {  // one rounding per half-drift (fused), as the single-box mixed form
+        qe.x = fma(p.x, P.dt2, q0.x);
+        qe.y = fma(p.y, P.dt2, q0.y);
+        qe.z = fma(p.z, P.dt2, q0.z);
+        q1.x = fma(p.x, P.dt2, qe.x);
+        q1.y = fma(p.y, P.dt2, qe.y);
+        q1.z = fma(p.z, P.dt2, qe.z);
+      } else {
+        qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, P.dt2));
+        qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, P.dt2));
+        qe.z = __dadd_rn(q0.z, __dmul_rn(p.z, P.dt2));
+        q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, P.dt2));
+        q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, P.dt2));
+        q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, P.dt2));
+      }
       const double4_32a qb = d.q_build[o + a];
       const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
-      if (ux * ux + uy * uy + uz * uz > P.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
-        rebuild = true;
+      const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
+      if (MIXED) {
+        if (fx * fx + fy * fy + fz * fz > (float)P.half_margin2 || !(fx == fx && fy == fy && fz == fz))
+          rebuild = true;
+      } else {
+        if (ux * ux + uy * uy + uz * uz > P.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
+          rebuild = true;
+      }
       const float4 lb = d.qf[o + a];
-      d.loc[par ^ 1][o + a] = make_float4(lb.x + (float)ux, lb.y + (float)uy, lb.z + (float)uz, 0.0f);
+      d.loc[par ^ 1][o + a] = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
       d.p[o + a] = p;
       d.q_end[o + a] = qe;
       d.q_mid[par ^ 1][o + a] = q1;
@@ -919,7 +955,7 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
   const int T0 = b->threads, L0 = b->lpi, C0 = b->ctas_per_sm;
   double best = 1e300;
   int bt = T0, bl = L0, bc = C0;
-  const int Ts[] = {128, 256, 512}, Ls[] = {1, 2, 4}, Cs[] = {1, 2, 4};
+  const int Ts[] = {128, 256, 512}, Ls[] = {1, 2, 4}, Cs[] = {1, 2, 3, 4};
   for (int T : Ts)
     for (int Lp : Ls)
       for (int C : Cs) {

@@ -1,6 +1,7 @@
 """Runs one LJ workload through the C ABI for profiling (e.g. under ncu).
 
     python -m mdacp_gb300.profile_run --cells 63 --precision mixed --steps 8 [--no-graphs | --profiled]
+    python -m mdacp_gb300.profile_run --boxes 256 --precision mixed --steps 20
 
 cells^3 FCC unit cells at density 0.5 (cells=100 -> 4,000,000 atoms, cells=63 ->
 1,000,188 atoms), Maxwell velocities at T=1, rc 2.5, margin 0.5, dt 0.001:
@@ -24,7 +25,26 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--no-graphs", action="store_true")
     ap.add_argument("--profiled", action="store_true")
+    ap.add_argument("--boxes", type=int, default=0,
+                    help="run the batched-replica workload instead: this many boxes (N ~ U[500, 8000], "
+                         "density ~ U[0.3, 0.9], T ~ U[0.7, 1.5], margin 0.4, dt 0.002), autotuned shape")
+    ap.add_argument("--shape", default="", help="threads,lanes,ctas_per_sm for --boxes instead of the autotuner")
     a = ap.parse_args()
+    if a.boxes:
+        from mdacp_gb300.batch import Batch, make_replicas
+        boxes = make_replicas(a.boxes, seed=1)
+        b = Batch(boxes, cutoff=2.5, margin=0.4, dt=0.002, precision=a.precision)
+        if a.shape:
+            shape = tuple(int(x) for x in a.shape.split(","))
+            b.set_shape(*shape)
+        else:
+            shape = b.tune(trial_steps=10)
+        b.calculate(a.steps)
+        st = b.stats()
+        print("boxes %d atoms %d steps %d ms/step %.4f shape %s rebuilds %d" % (
+            a.boxes, sum(len(x[0]) for x in boxes), a.steps, st["elapsed_ms"] / max(a.steps, 1), shape,
+            st["rebuilds"]))
+        return
     from mdacp_gb300 import lattice
     from mdacp_gb300.manager import MDManager
     q, L = lattice.fcc_cube(a.cells, a.density)
