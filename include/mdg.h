@@ -61,7 +61,7 @@ typedef struct mdg_params {
   double prune_buffer;     /* inner-list buffer: the force kernels walk the pairs within
                               cutoff + prune_buffer, re-selected from the list whenever a
                               particle moved prune_buffer/2 (default -1 = automatic,
-                              min(100 dt, margin); 0 keeps every listed pair) */
+                              min(0.1, margin / 2); 0 keeps every listed pair) */
 } mdg_params;
 
 typedef struct mdg_stats {
