@@ -429,6 +429,9 @@ struct mdg_adjoint {
   int gridp = 1;   // kLanes threads per particle (pair kernels)
   int nck = 0;
   bool forward_done = false;
+  // the device work of a forward and of a backward pass, captured once and
+  // replayed (every pointer is fixed at creation)
+  cudaGraphExec_t gx_forward = nullptr, gx_backward = nullptr;
 };
 
 namespace {
@@ -455,6 +458,91 @@ void fwd_step(mdg_adjoint *a, double4_32a *q, double4_32a *p, double4_32a *qh) {
   k_drift<<<a->grid, kT, 0, a->s>>>(a->c, a->d, q, p, qh);
   k_force<<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, a->d.F);
   k_kick_drift<<<a->grid, kT, 0, a->s>>>(a->c, qh, a->d.F, q, p);
+}
+
+// The horizon from the state in d.q, d.p: per segment its list, per step the
+// step and the objective terms, checkpoints every K steps.
+int enqueue_forward(mdg_adjoint *a) {
+  const size_t N = (size_t)a->c.n, bytes = N * 32;
+  D &d = a->d;
+  MDG_ACK(cudaMemsetAsync(d.flag, 0, 2 * sizeof(int), a->s));
+  MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
+  const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
+  const double w = 1.0 / Ns;
+  MDG_ACK(cudaMemcpyAsync(d.ckq, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+  MDG_ACK(cudaMemcpyAsync(d.ckp, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
+  for (int n = 1; n <= Ns; n++) {
+    if ((n - 1) % K == 0) {  // a checkpoint segment starts: its own list
+      MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+      k_build<<<a->grid, kT, 0, a->s>>>(a->c, d, d.q);
+    }
+    fwd_step(a, d.q, d.p, d.qh);
+    k_objective<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.q, d.p, 0, w);
+    k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, w);
+    if (n % K == 0) {
+      MDG_ACK(cudaMemcpyAsync(d.ckq + N * (n / K), d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+      MDG_ACK(cudaMemcpyAsync(d.ckp + N * (n / K), d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? MDG_OK : afail(a, MDG_ERR_CUDA, "adjoint forward launch failed");
+}
+
+// Reverse of the horizon, segment by segment from the last: recompute the
+// segment from its checkpoint (with the same list), then reverse its steps.
+int enqueue_backward(mdg_adjoint *a) {
+  const size_t N = (size_t)a->c.n, bytes = N * 32;
+  D &d = a->d;
+  const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
+  const double w = 1.0 / Ns;
+  MDG_ACK(cudaMemsetAsync(d.aq, 0, bytes, a->s));
+  MDG_ACK(cudaMemsetAsync(d.ap, 0, bytes, a->s));
+  MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
+  for (int seg_end = Ns; seg_end > 0;) {
+    const int seg_start = ((seg_end - 1) / K) * K;
+    const int len = seg_end - seg_start;
+    // recompute the segment from its checkpoint: states 0..len, half steps 1..len
+    MDG_ACK(cudaMemcpyAsync(d.segq, d.ckq + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
+    MDG_ACK(cudaMemcpyAsync(d.segp, d.ckp + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
+    // the segment's list, built from the same state as in the forward pass
+    MDG_ACK(cudaMemcpyAsync(d.q0, d.segq, bytes, cudaMemcpyDeviceToDevice, a->s));
+    k_build<<<a->grid, kT, 0, a->s>>>(a->c, d, d.segq);
+    for (int k = 1; k <= len; k++) {
+      MDG_ACK(cudaMemcpyAsync(d.segq + N * k, d.segq + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
+      MDG_ACK(cudaMemcpyAsync(d.segp + N * k, d.segp + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
+      fwd_step(a, d.segq + N * k, d.segp + N * k, d.segqh + N * k);
+    }
+    for (int k = len; k >= 1; k--) {
+      // objective terms of state (seg_start + k)
+      k_objective<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segq + N * k, d.segp + N * k, 1, w);
+      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, w);
+      // reverse the step that produced it
+      k_reverse<<<a->grid, kT, 0, a->s>>>(a->c, d);
+      k_reverse_hvp<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segqh + N * k);
+      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, 1.0);
+    }
+    seg_end = seg_start;
+  }
+  return cudaGetLastError() == cudaSuccess ? MDG_OK : afail(a, MDG_ERR_CUDA, "adjoint backward launch failed");
+}
+
+// Runs `enqueue` as a CUDA graph captured on first use.
+int run_graph(mdg_adjoint *a, cudaGraphExec_t *gx, int (*enqueue)(mdg_adjoint *)) {
+  if (!*gx) {
+    MDG_ACK(cudaStreamBeginCapture(a->s, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue(a);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(a->s, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    MDG_ACK(e);
+    const cudaError_t ei = cudaGraphInstantiate(gx, g, 0);
+    cudaGraphDestroy(g);
+    MDG_ACK(ei);
+  }
+  MDG_ACK(cudaGraphLaunch(*gx, a->s));
+  return MDG_OK;
 }
 
 }  // namespace
@@ -544,6 +632,8 @@ int mdg_adjoint_destroy(mdg_adjoint *a) {
   if (!a) return MDG_OK;
   cudaSetDevice(a->prm.device);
   if (a->s) cudaStreamSynchronize(a->s);
+  if (a->gx_forward) cudaGraphExecDestroy(a->gx_forward);
+  if (a->gx_backward) cudaGraphExecDestroy(a->gx_backward);
   D &d = a->d;
   void *ptrs[] = {d.q, d.p, d.qh, d.F, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
                   d.nbr, d.cnt, d.part, d.acc, d.flag};
@@ -563,26 +653,9 @@ int mdg_adjoint_forward(mdg_adjoint *a, const double *q4, const double *p4, doub
   D &d = a->d;
   MDG_ACK(cudaMemcpyAsync(d.q, q4, bytes, cudaMemcpyHostToDevice, a->s));
   MDG_ACK(cudaMemcpyAsync(d.p, p4, bytes, cudaMemcpyHostToDevice, a->s));
-  MDG_ACK(cudaMemsetAsync(d.flag, 0, 2 * sizeof(int), a->s));
-  MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
+  const int rc = run_graph(a, &a->gx_forward, enqueue_forward);
+  if (rc) return rc;
   int flag[2] = {0, 0};
-  const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
-  const double w = 1.0 / Ns;
-  MDG_ACK(cudaMemcpyAsync(d.ckq, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
-  MDG_ACK(cudaMemcpyAsync(d.ckp, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
-  for (int n = 1; n <= Ns; n++) {
-    if ((n - 1) % K == 0) {  // a checkpoint segment starts: its own list
-      MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
-      k_build<<<a->grid, kT, 0, a->s>>>(a->c, d, d.q);
-    }
-    fwd_step(a, d.q, d.p, d.qh);
-    k_objective<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.q, d.p, 0, w);
-    k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, w);
-    if (n % K == 0) {
-      MDG_ACK(cudaMemcpyAsync(d.ckq + N * (n / K), d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
-      MDG_ACK(cudaMemcpyAsync(d.ckp + N * (n / K), d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
-    }
-  }
   double acc[3];
   MDG_ACK(cudaMemcpyAsync(acc, d.acc, sizeof acc, cudaMemcpyDeviceToHost, a->s));
   MDG_ACK(cudaMemcpyAsync(flag, d.flag, sizeof flag, cudaMemcpyDeviceToHost, a->s));
@@ -601,36 +674,8 @@ int mdg_adjoint_backward(mdg_adjoint *a, double *dq0, double *dp0, double *deps,
   MDG_ACK(cudaSetDevice(a->prm.device));
   const size_t N = (size_t)a->c.n, bytes = N * 32;
   D &d = a->d;
-  const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
-  const double w = 1.0 / Ns;
-  MDG_ACK(cudaMemsetAsync(d.aq, 0, bytes, a->s));
-  MDG_ACK(cudaMemsetAsync(d.ap, 0, bytes, a->s));
-  MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
-  for (int seg_end = Ns; seg_end > 0;) {
-    const int seg_start = ((seg_end - 1) / K) * K;
-    const int len = seg_end - seg_start;
-    // recompute the segment from its checkpoint: states 0..len, half steps 1..len
-    MDG_ACK(cudaMemcpyAsync(d.segq, d.ckq + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
-    MDG_ACK(cudaMemcpyAsync(d.segp, d.ckp + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
-    // the segment's list, built from the same state as in the forward pass
-    MDG_ACK(cudaMemcpyAsync(d.q0, d.segq, bytes, cudaMemcpyDeviceToDevice, a->s));
-    k_build<<<a->grid, kT, 0, a->s>>>(a->c, d, d.segq);
-    for (int k = 1; k <= len; k++) {
-      MDG_ACK(cudaMemcpyAsync(d.segq + N * k, d.segq + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
-      MDG_ACK(cudaMemcpyAsync(d.segp + N * k, d.segp + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
-      fwd_step(a, d.segq + N * k, d.segp + N * k, d.segqh + N * k);
-    }
-    for (int k = len; k >= 1; k--) {
-      // objective terms of state (seg_start + k)
-      k_objective<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segq + N * k, d.segp + N * k, 1, w);
-      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, w);
-      // reverse the step that produced it
-      k_reverse<<<a->grid, kT, 0, a->s>>>(a->c, d);
-      k_reverse_hvp<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segqh + N * k);
-      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, 1.0);
-    }
-    seg_end = seg_start;
-  }
+  const int rc = run_graph(a, &a->gx_backward, enqueue_backward);
+  if (rc) return rc;
   double acc[3];
   MDG_ACK(cudaMemcpyAsync(acc, d.acc, sizeof acc, cudaMemcpyDeviceToHost, a->s));
   if (dq0) MDG_ACK(cudaMemcpyAsync(dq0, d.aq, bytes, cudaMemcpyDeviceToHost, a->s));
