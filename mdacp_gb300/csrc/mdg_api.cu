@@ -673,8 +673,8 @@ int mdg_observe(mdg_handle *h, double out[3]) {
   if (!out) return fail(h, MDG_ERR_INVALID, "null output");
   rc = ensure_list(h, false);
   if (rc) return rc;
-  mdg::launch_observe(h->g, h->d, h->dobs, h->stream);
-  h->launches += 2;
+  mdg::launch_observe(h->g, h->d, h->dobs, h->stream, h->prm.precision == MDG_MIXED, h->par);
+  h->launches += h->prm.precision == MDG_MIXED ? 3 : 2;
   MDG_CK(cudaMemcpyAsync(h->hobs, h->dobs, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   out[0] = h->hobs[0];

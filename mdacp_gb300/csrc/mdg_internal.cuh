@@ -132,7 +132,7 @@ void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compa
 void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle rebuild_cond, cudaStream_t s);
 void launch_select(const Dev &d, cudaGraphConditionalHandle variant_cond, cudaStream_t s);
 void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s);
-void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s);
+void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s, int mixed, int par);
 void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s);
 void launch_unsort(const Geom &g, const Dev &d, double4_32a *qo, double4_32a *po, cudaStream_t s);
 void launch_sort_in(const Geom &g, const Dev &d, const double4_32a *qi, const double4_32a *pi, cudaStream_t s);

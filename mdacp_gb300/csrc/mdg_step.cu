@@ -422,6 +422,56 @@ __global__ void __launch_bounds__(kStepThreads) k_observe(Geom g, Dev d) {
   }
 }
 
+// Mixed-form observers: the same sums with the pair terms in float (from the
+// home-cell-local float positions of q_end, as the mixed force), each
+// particle's sum converted to double and reduced in double.  The FP64 form
+// keeps k_observe's reference rounding.
+__global__ void __launch_bounds__(kStepThreads) k_observe_mixed(Geom g, Dev d, const float4 *__restrict__ loc) {
+  __shared__ double sh[kStepThreads / 32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double ke = 0.0, pe = 0.0, vir = 0.0;
+  if (i < g.n) {
+    const double4_32a p = d.p[i];
+    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+    const float4 li = loc[i];
+    const CellPos cp = cell_pos_packed(g, li.w);
+    const AxisQuad qx = axis_quad(g.w32[0], g.dl32[0], cp.cx == 0, cp.cx == g.nc[0] - 1, li.x, 1.0f);
+    const AxisQuad qy = axis_quad(g.w32[1], g.dl32[1], cp.cy == 0, cp.cy == g.nc[1] - 1, li.y, 0.25f);
+    const AxisQuad qz = axis_quad(g.w32[2], g.dl32[2], cp.cz == 0, cp.cz == g.nc[2] - 1, li.z, 0.0625f);
+    const float rc2 = g.rc2f, c2 = (float)g.c2, c0 = (float)g.c0, c2x8 = g.c2x8f;
+    float e_sum = 0.f, v_sum = 0.f;
+    const int cnt = d.ncount[i];
+    for (int k = 0; k < cnt; k++) {
+      const uint32_t e = __ldg(d.nl + (size_t)k * g.stride + i);
+      const float4 lj = __ldg(loc + entry_slot(e));
+      const float tx = step_float(e, 0x03u, 8388609.0f), ty = step_float(e, 0x0Cu, 8388612.0f),
+                  tz = step_float(e, 0x30u, 8388624.0f);
+      const float dx = lj.x + fmaf(fmaf(qx.b, tx, qx.a), tx, qx.c);
+      const float dy = lj.y + fmaf(fmaf(qy.b, ty, qy.a), ty, qy.c);
+      const float dz = lj.z + fmaf(fmaf(qz.b, tz, qz.a), tz, qz.c);
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      float inv;
+      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+      const float i6 = inv * inv * inv;
+      const float e_ij = 4.0f * (i6 * i6 - i6 + fmaf(c2, r2, c0));
+      const float v_ij = ((i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8) * r2;
+      const bool in = r2 <= rc2;
+      e_sum += in ? e_ij : 0.0f;
+      v_sum += in ? v_ij : 0.0f;
+    }
+    pe = 0.5 * (double)e_sum;
+    vir = 0.5 * (double)v_sum;
+  }
+  const double a = block_sum(ke, sh);
+  const double b = block_sum(pe, sh);
+  const double c = block_sum(vir, sh);
+  if (threadIdx.x == 0) {
+    d.partials[3 * blockIdx.x + 0] = a;
+    d.partials[3 * blockIdx.x + 1] = b;
+    d.partials[3 * blockIdx.x + 2] = c;
+  }
+}
+
 __global__ void k_observe_final(Dev d, int nparts, double *out) {
   __shared__ double sh[32];
   double a = 0.0, b = 0.0, c = 0.0;
@@ -540,9 +590,15 @@ void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s) {
   k_nh_update<<<1, 1024, 0, s>>>(g, d, grid, 1);
 }
 
-void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s) {
+void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s, int mixed, int par) {
   const int grid = blocks_for(g.n);
-  k_observe<<<grid, kStepThreads, 0, s>>>(g, d);
+  if (mixed) {
+    // the buffer the next step overwrites before reading it
+    k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
+    k_observe_mixed<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
+  } else {
+    k_observe<<<grid, kStepThreads, 0, s>>>(g, d);
+  }
   k_observe_final<<<1, 1024, 0, s>>>(d, grid, out_dev);
 }
 

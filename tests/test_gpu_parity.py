@@ -115,6 +115,22 @@ def test_mixed_trace_close():
     np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-5, atol=1e-6)
 
 
+def test_mixed_observer_matches_fp64_observer():
+    # the mixed form evaluates pair energies and virials in float from the
+    # home-cell-local positions; on the same state the sums agree with the FP64
+    # observer to float rounding (per-pair relative 1e-7, summed in double)
+    q, p, L = liquid_like(0.8, 24, seed=29)
+    a = _gpu(L, len(q), precision="mixed")
+    b = _gpu(L, len(q))
+    for m in (a, b):
+        m.set_state(q, p)
+    np.testing.assert_allclose(a.observe_raw(), b.observe_raw(), rtol=2e-6, atol=0)
+    a.calculate(150)
+    qa, pa = a.state()
+    b.set_state(qa, pa)
+    np.testing.assert_allclose(a.observe_raw(), b.observe_raw(), rtol=2e-6, atol=0)
+
+
 def test_langevin_matches_oracle_stream():
     q, p, L = liquid_like(0.5, 12, seed=31)
     kw = dict(dt=0.005, thermostat="langevin", temperature=0.9, gamma=1.0, seed=12345)
