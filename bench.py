@@ -294,6 +294,8 @@ def run_mine(args):
     ph = torch.zeros((n, 4), dtype=torch.float64).pin_memory().numpy()
     qh[:, :3] = q
     ph[:, :3] = p
+    qo = torch.zeros((n, 4), dtype=torch.float64).pin_memory().numpy()
+    po = torch.zeros((n, 4), dtype=torch.float64).pin_memory().numpy()
     me = MDManager(L, capacity=n, cutoff=RC, margin=MARGIN, dt=DT, precision="mixed", device=d.local)
     me.set_state(qh, ph)
     me.calculate(W)
@@ -306,7 +308,7 @@ def run_mine(args):
         if k % 100 == 0:
             me.observe_raw()
             nobs += 1
-    qo, po = me.state()
+    me.state(qo, po)
     t_e2e = d.max(time.perf_counter() - t0)
     me.close()
     e2e_value = d.world * n * K / t_e2e

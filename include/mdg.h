@@ -73,7 +73,7 @@ typedef struct mdg_stats {
   int32_t cells[3];        /* cell grid */
   int32_t particles;
   double zeta;             /* Nose-Hoover friction (Variables::Zeta) */
-  double elapsed_ms;       /* device time of the last mdg_calculate call */
+  double elapsed_ms;       /* device time of the last confirmed mdg_calculate calls */
   int64_t kernel_launches; /* kernels this handle has enqueued (graph replays count each node) */
   int64_t inner_pairs;     /* directed pairs in the inner list at the last prune */
   int64_t prunes;          /* inner-list selections since the last mdg_set_state */
@@ -102,8 +102,16 @@ int mdg_get_state(mdg_handle *h, double *q4, double *p4);
 
 /* Replaces MDManager::MakePairList (mdmanager.cc:262-280): wrap, bin, build. */
 int mdg_make_pairlist(mdg_handle *h);
-/* Replaces nsteps calls of MDManager::Calculate (mdmanager.cc:116-148). */
+/* Replaces nsteps calls of MDManager::Calculate (mdmanager.cc:116-148).
+ * The steps are enqueued on the handle's stream and the call returns without
+ * waiting until 1024 steps are outstanding.  Every other call on the handle
+ * first waits for them and confirms them: a list overflow is recovered there
+ * (rows regrown, the steps behind it run again), and a particle found outside
+ * the box at a rebuild is reported there as MDG_ERR_STATE (the steps after it
+ * do nothing).  mdg_set_state and mdg_make_state discard that report. */
 int mdg_calculate(mdg_handle *h, int32_t nsteps);
+/* Waits for and confirms the steps mdg_calculate left outstanding. */
+int mdg_synchronize(mdg_handle *h);
 /* mdg_calculate without graph replay, with a CUDA event pair on the handle's
  * stream around every launch of the fused step kernel; *step_kernel_ms receives
  * the summed device time of those launches (for roofline accounting). */

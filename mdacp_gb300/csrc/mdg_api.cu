@@ -41,7 +41,11 @@ struct mdg_handle {
   double last_ms = 0.0;
   long long steps_host = 0;  // completed steps as last read from the device
   long long launches = 0;    // kernels enqueued (counting every node of a graph replay)
+  long long pending = 0;     // steps enqueued by mdg_calculate and not yet confirmed
 };
+
+// Steps mdg_calculate may leave enqueued before it waits for them.
+constexpr long long kMaxPending = 1024;
 
 namespace {
 
@@ -359,11 +363,59 @@ int enqueue_steps(mdg_handle *h, int nsteps) {
   return MDG_OK;
 }
 
-int check_handle(mdg_handle *h, bool need_state) {
+// Confirms the steps mdg_calculate enqueued without waiting: reads the device
+// counters once, and after a halt on list overflow (the steps behind the halt
+// ran as no-ops) regrows the rows and runs the steps that are still owed.
+int settle(mdg_handle *h) {
+  if (h->pending == 0) return MDG_OK;
+  const long long want = h->pending;
+  h->pending = 0;
+  long long done = 0;
+  for (int attempt = 0; attempt < 64 && done < want; attempt++) {
+    const unsigned long long before = (unsigned long long)h->steps_host;
+    const unsigned long long rebuilds0 = h->hflags->rebuilds;
+    if (attempt > 0) {
+      int rc = enqueue_steps(h, (int)(want - done));
+      if (rc) return rc;
+      MDG_CK(cudaEventRecord(h->ev1, h->stream));
+    }
+    int rc = read_flags(h);
+    if (rc) return rc;
+    long long completed = (long long)(h->hflags->steps - before);
+    if (h->prm.use_graphs)  // executed kernels: prelude, select, step (+ NH), and the rebuild bodies that ran
+      h->launches += completed * (2 + mdg::step_kernels(h->prm.thermostat)) +
+                     (long long)(h->hflags->rebuilds - rebuilds0) * mdg::kRebuildKernels;
+    if (h->hflags->halt == 0) {
+      done += completed;
+      h->steps_host = (long long)h->hflags->steps;
+      continue;
+    }
+    if (h->hflags->halt != mdg::kHaltOverflow) return halt_error(h);
+    done += completed - 1;
+    rc = recover_overflow(h, true);
+    if (rc) return rc;
+    h->steps_host = (long long)h->hflags->steps - 1;
+  }
+  MDG_CK(cudaEventSynchronize(h->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  if (done != want) return fail(h, MDG_ERR_CAPACITY, "neighbour list could not be sized");
+  return MDG_OK;
+}
+
+// What an entry point does with steps still unconfirmed: confirm them first
+// (every reader of the state), leave them (mdg_calculate), or drop the
+// bookkeeping because the state is about to be replaced.
+enum Pending { kSettle, kKeep, kDrop };
+
+int check_handle(mdg_handle *h, bool need_state, Pending pending = kSettle) {
   if (!h) return MDG_ERR_INVALID;
   if (need_state && !h->has_state) return fail(h, MDG_ERR_NOT_READY, "no particle state loaded");
   cudaError_t e = cudaSetDevice(h->prm.device);
   if (e != cudaSuccess) return fail(h, MDG_ERR_CUDA, cudaGetErrorString(e));
+  if (pending == kSettle) return settle(h);
+  if (pending == kDrop) h->pending = 0;
   return MDG_OK;
 }
 
@@ -509,7 +561,7 @@ static int set_state_common(mdg_handle *h, int32_t n) {
 }
 
 int mdg_set_state(mdg_handle *h, const double *q4, const double *p4, int32_t n) {
-  int rc = check_handle(h, false);
+  int rc = check_handle(h, false, kDrop);
   if (rc) return rc;
   if (!q4 || !p4 || n <= 0) return fail(h, MDG_ERR_INVALID, "null state or n <= 0");
   if (n > h->cap) return fail(h, MDG_ERR_CAPACITY, "more particles than the handle capacity");
@@ -522,7 +574,7 @@ int mdg_set_state(mdg_handle *h, const double *q4, const double *p4, int32_t n) 
 }
 
 int mdg_set_state_device(mdg_handle *h, const double *q4, const double *p4, int32_t n) {
-  int rc = check_handle(h, false);
+  int rc = check_handle(h, false, kDrop);
   if (rc) return rc;
   if (!q4 || !p4 || n <= 0) return fail(h, MDG_ERR_INVALID, "null state or n <= 0");
   if (n > h->cap) return fail(h, MDG_ERR_CAPACITY, "more particles than the handle capacity");
@@ -532,7 +584,7 @@ int mdg_set_state_device(mdg_handle *h, const double *q4, const double *p4, int3
 }
 
 int mdg_make_state(mdg_handle *h, int32_t maker, double density, double radius, double v0) {
-  int rc = check_handle(h, false);
+  int rc = check_handle(h, false, kDrop);
   if (rc) return rc;
   int32_t n = 0;
   rc = mdg_make_configuration(h->g.L, maker, density, radius, 0, (double *)h->d.io4, h->cap, &n, h->stream);
@@ -577,7 +629,7 @@ int mdg_make_pairlist(mdg_handle *h) {
 }
 
 int mdg_calculate(mdg_handle *h, int32_t nsteps) {
-  int rc = check_handle(h, true);
+  int rc = check_handle(h, true, kKeep);
   if (rc) return rc;
   if (nsteps < 0) return fail(h, MDG_ERR_INVALID, "negative step count");
   if (nsteps == 0) return MDG_OK;
@@ -586,39 +638,16 @@ int mdg_calculate(mdg_handle *h, int32_t nsteps) {
     h->launches += 2;
     h->nh_init = false;
   }
-  MDG_CK(cudaEventRecord(h->ev0, h->stream));
-  long long done = 0;
-  for (int attempt = 0; attempt < 64 && done < nsteps; attempt++) {
-    const unsigned long long before = (unsigned long long)h->steps_host;
-    const unsigned long long rebuilds0 = h->hflags->rebuilds;
-    rc = enqueue_steps(h, (int)(nsteps - done));
-    if (rc) return rc;
-    rc = read_flags(h);
-    if (rc) return rc;
-    long long completed = (long long)(h->hflags->steps - before);
-    if (h->prm.use_graphs)  // executed kernels: prelude, select, step (+ NH), and the rebuild bodies that ran
-      h->launches += completed * (2 + mdg::step_kernels(h->prm.thermostat)) +
-                     (long long)(h->hflags->rebuilds - rebuilds0) * mdg::kRebuildKernels;
-    if (h->hflags->halt == 0) {
-      done += completed;
-      h->steps_host = (long long)h->hflags->steps;
-      continue;
-    }
-    if (h->hflags->halt != mdg::kHaltOverflow) return halt_error(h);
-    completed -= 1;
-    done += completed;
-    rc = recover_overflow(h, true);
-    if (rc) return rc;
-    h->steps_host = (long long)h->hflags->steps - 1;
-  }
+  if (h->pending == 0) MDG_CK(cudaEventRecord(h->ev0, h->stream));
+  rc = enqueue_steps(h, nsteps);
+  if (rc) return rc;
   MDG_CK(cudaEventRecord(h->ev1, h->stream));
-  MDG_CK(cudaEventSynchronize(h->ev1));
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-  h->last_ms = ms;
-  if (done != nsteps) return fail(h, MDG_ERR_CAPACITY, "neighbour list could not be sized");
+  h->pending += nsteps;
+  if (h->pending >= kMaxPending) return settle(h);
   return MDG_OK;
 }
+
+int mdg_synchronize(mdg_handle *h) { return check_handle(h, false); }
 
 int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms) {
   int rc = check_handle(h, true);

@@ -19,6 +19,11 @@ def _dp(a):
 
 
 def _as4(x):
+    """[n][4] float64 rows; a C-contiguous [n][4] float64 array (pinned host
+    memory included) is passed on as it is."""
+    if isinstance(x, np.ndarray) and x.dtype == np.float64 and x.ndim == 2 and x.shape[1] == 4 \
+            and x.flags.c_contiguous:
+        return x
     x = np.asarray(x, dtype=np.float64)
     out = np.zeros((len(x), 4), dtype=np.float64)
     out[:, :3] = x[:, :3]
@@ -86,11 +91,21 @@ class MDManager:
         self.n = len(q4)
         self._ck(self.lib.mdg_set_state(self._h, _dp(q4), _dp(p4), self.n))
 
-    def state(self):
-        q4 = np.zeros((self.n, 4))
-        p4 = np.zeros((self.n, 4))
+    def state(self, q4=None, p4=None):
+        """Positions and momenta in the caller's order, as [n][3] views of
+        [n][4] buffers; q4/p4 may be given (C-contiguous float64 [n][4], e.g.
+        pinned host memory) to receive the state without an allocation."""
+        q4 = np.zeros((self.n, 4)) if q4 is None else q4
+        p4 = np.zeros((self.n, 4)) if p4 is None else p4
+        for x in (q4, p4):
+            if x.dtype != np.float64 or x.shape != (self.n, 4) or not x.flags.c_contiguous:
+                raise ValueError("state buffers must be C-contiguous float64 [n][4]")
         self._ck(self.lib.mdg_get_state(self._h, _dp(q4), _dp(p4)))
         return q4[:, :3], p4[:, :3]
+
+    def synchronize(self):
+        """Waits for the steps calculate() left outstanding and reports their errors."""
+        self._ck(self.lib.mdg_synchronize(self._h))
 
     def make_state(self, maker, density, radius=0.0, v0=0.0):
         """The reference's configuration makers and SetInitialVelocity, on the device.

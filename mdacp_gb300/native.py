@@ -46,6 +46,7 @@ SIGNATURES = {
     "mdg_get_state": (ctypes.c_int, [_P, _D, _D]),
     "mdg_make_pairlist": (ctypes.c_int, [_P]),
     "mdg_calculate": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "mdg_synchronize": (ctypes.c_int, [_P]),
     "mdg_calculate_profiled": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
     "mdg_observe": (ctypes.c_int, [_P, _D]),
     "mdg_forces": (ctypes.c_int, [_P, _D]),

@@ -174,6 +174,55 @@ def test_overflow_regrows_list():
     np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-10, atol=1e-12)
 
 
+def test_outstanding_steps_recover_overflow():
+    # single-step calls return before the steps run; the list overflow of the
+    # first rebuild halts the device, and the next reader regrows the rows and
+    # runs the owed steps
+    q, p, L = liquid_like(0.8, 8, seed=52)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+    ref.make_pairlist()
+    m = _gpu(L, len(q), list_capacity=8)
+    m.set_state(q, p)
+    for _ in range(30):
+        m.calculate(1)
+    ref.calculate(30)
+    np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-10, atol=1e-12)
+    st = m.stats()
+    assert st["steps"] == 30 and st["list_capacity"] > 8
+
+
+def test_single_step_calls_match_one_call():
+    q, p, L = liquid_like(0.5, 10, seed=53)
+    a = _gpu(L, len(q), precision="mixed")
+    b = _gpu(L, len(q), precision="mixed")
+    for m in (a, b):
+        m.set_state(q, p)
+    a.calculate(1500)
+    for _ in range(1500):   # crosses the 1024-step confirmation bound once
+        b.calculate(1)
+    b.synchronize()
+    qa, pa = a.state()
+    qb, pb = b.state()
+    assert np.array_equal(qa, qb) and np.array_equal(pa, pb)
+    assert a.stats()["steps"] == b.stats()["steps"] == 1500
+
+
+def test_bad_state_reported_by_the_next_reader():
+    from mdacp_gb300 import native
+    q, p, L = liquid_like(0.5, 6, seed=62)
+    m = _gpu(L, len(q))
+    bad = q.copy()
+    bad[5, 0] = np.inf
+    m.set_state(bad, p)
+    m.calculate(5)           # enqueued only
+    with pytest.raises(native.MDGError, match="bad particle state"):
+        m.observe()
+    m.set_state(q, p)
+    m.calculate(5)
+    m.synchronize()
+    assert m.stats()["steps"] == 5
+
+
 def test_state_roundtrip_and_bad_state():
     from mdacp_gb300 import native
     q, p, L = liquid_like(0.5, 6, seed=61)
