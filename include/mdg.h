@@ -292,19 +292,26 @@ int mdg_save_cdview(mdg_handle *h, const char *path);
 enum mdg_maker {
   MDG_MAKER_FCC = 0,      /* ConfigurationMaker (confmaker.cc:9-44) */
   MDG_MAKER_EXTRACT = 1,  /* ExtractConfigurationMaker (confmaker.cc:174-252) for one unit spanning the box */
-  MDG_MAKER_DROPLET = 2   /* DropletMaker (burst.cc:10-61): sites within `radius` of the box centre */
+  MDG_MAKER_DROPLET = 2,  /* DropletMaker (burst.cc:10-61): sites within `radius` of the box centre */
+  MDG_MAKER_COLLISION = 3 /* BallAdder pair of Collision::Run (collision.cc:8-63): balls of `radius`
+                             (the reference uses L_y / 4, density 0.374) at (L_x/4, L_y/2, L_z/2) and
+                             (3 L_x/4, L_y/2, L_z/2) moving at +speed and -speed along x */
 };
 /* Writes the maker's positions to q4_dev ([capacity][4], lane 3 zero); *n
  * receives the count (MDG_ERR_CAPACITY, nothing written, when it exceeds
- * capacity).  unit_id seeds ExtractConfigurationMaker's mt19937 as
- * MDUnit::GetID does (0 for the single-unit drop-in). */
+ * capacity).  p4_dev (NULL to skip) receives the velocities the maker sets
+ * itself: (+speed, 0, 0) and (-speed, 0, 0) for the collision maker's two
+ * balls, zero for the others.  unit_id seeds ExtractConfigurationMaker's
+ * mt19937 as MDUnit::GetID does (0 for the single-unit drop-in). */
 int mdg_make_configuration(const double box[3], int32_t maker, double density, double radius, int32_t unit_id,
-                           double *q4_dev, int32_t capacity, int32_t *n, void *stream);
+                           double speed, double *q4_dev, double *p4_dev, int32_t capacity, int32_t *n, void *stream);
 /* Variables::SetInitialVelocity (variables.cc:82-108): p4_dev[n][4] <- speed v0,
  * directions from mt19937(seed), mean subtracted. */
 int mdg_make_velocity(double v0, int32_t seed, double *p4_dev, int32_t n, void *stream);
 /* Both into a handle's state (MDManager's makers + SetInitialVelocity(v0),
- * seed = unit id 0); v0 = 0 leaves the momenta zero. */
+ * seed = unit id 0; v0 = 0 leaves the momenta zero).  For the collision maker
+ * v0 is the balls' speed and SetInitialVelocity is not applied, as in
+ * Collision::Run. */
 int mdg_make_state(mdg_handle *h, int32_t maker, double density, double radius, double v0);
 
 #ifdef __cplusplus

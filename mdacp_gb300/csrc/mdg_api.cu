@@ -587,12 +587,15 @@ int mdg_make_state(mdg_handle *h, int32_t maker, double density, double radius, 
   int rc = check_handle(h, false, kDrop);
   if (rc) return rc;
   int32_t n = 0;
-  rc = mdg_make_configuration(h->g.L, maker, density, radius, 0, (double *)h->d.io4, h->cap, &n, h->stream);
+  // the collision maker sets its own velocities (speed v0 along x); the other
+  // makers leave them zero for SetInitialVelocity
+  const bool own_velocity = maker == MDG_MAKER_COLLISION;
+  rc = mdg_make_configuration(h->g.L, maker, density, radius, 0, own_velocity ? v0 : 0.0, (double *)h->d.io4,
+                              (double *)h->d.io4b, h->cap, &n, h->stream);
   if (rc == MDG_ERR_CAPACITY) return fail(h, rc, "the configuration has more particles than the handle capacity");
   if (rc) return fail(h, rc, "configuration maker failed");
   if (n <= 0) return fail(h, MDG_ERR_INVALID, "the configuration is empty");
-  MDG_CK(cudaMemsetAsync(h->d.io4b, 0, (size_t)n * sizeof(double4_32a), h->stream));
-  if (v0 != 0.0) {
+  if (!own_velocity && v0 != 0.0) {
     rc = mdg_make_velocity(v0, 0, (double *)h->d.io4b, n, h->stream);
     if (rc) return fail(h, rc, "velocity maker failed");
   }

@@ -6,6 +6,9 @@
 //     the first n_delete distinct sites drawn from mt19937(unit id) through
 //     uniform_real_distribution<double>(0, 1);
 //   DropletMaker (burst.cc:10-61): FCC sites inside a sphere at the box centre;
+//   BallAdder (collision.cc:8-51) as Collision::Run places it (collision.cc:55-63):
+//     two balls of a simple-cubic lattice with three half-shifted sites per
+//     cell, moving at +speed and -speed along x;
 //   Variables::SetInitialVelocity (variables.cc:82-108): speed V0 in directions
 //     drawn from mt19937(seed), minus the mean.
 // Positions are bit-identical to the reference's: the same double operations
@@ -148,6 +151,10 @@ struct Lattice {
   double ox, oy, oz;  // unit origin
   int sx, sy, sz;     // cells per side
   int pad;
+  // collision maker: two balls of radius br at centres bc[0], bc[1], each with
+  // per_ball sites; the box [0, L) the reference's unit accepts
+  double bc[2][3], br, L[3];
+  long long per_ball;
 };
 
 // Position of site n in the makers' loop order (iz, iy, ix, then the four
@@ -173,6 +180,26 @@ __device__ __forceinline__ void site_pos(const Lattice &l, long long n, double x
   }
 }
 
+// Site n of the collision maker (BallAdder::Execute, collision.cc:34-50): the
+// first ball's sites, then the second's; per ball is^3 cells in (iz, iy, ix)
+// order, each giving its corner x1 = ix s - r + c, then x1 shifted by s/2
+// along x, along y, along z.  Returns the ball.
+__device__ __forceinline__ int ball_pos(const Lattice &l, long long n, double x[3]) {
+  const int b = n >= l.per_ball ? 1 : 0;
+  const long long m = b ? n - l.per_ball : n;
+  const int sub = (int)(m & 3);
+  const long long c = m >> 2;
+  const int ix = (int)(c % l.sx);
+  const long long r = c / l.sx;
+  const int iy = (int)(r % l.sx), iz = (int)(r / l.sx);
+  const double *cb = l.bc[b];
+  x[0] = __dadd_rn(__dsub_rn(__dmul_rn((double)ix, l.s), l.br), cb[0]);
+  x[1] = __dadd_rn(__dsub_rn(__dmul_rn((double)iy, l.s), l.br), cb[1]);
+  x[2] = __dadd_rn(__dsub_rn(__dmul_rn((double)iz, l.s), l.br), cb[2]);
+  if (sub > 0) x[sub - 1] = __dadd_rn(x[sub - 1], l.hs);
+  return b;
+}
+
 // keep[n] for every site: 0 deleted / outside, 1 kept.
 __global__ void k_keep(Lattice l, long long n_sites, int mode, const int *first, long long cut, double cx, double r2max,
                        int *keep) {
@@ -186,20 +213,39 @@ __global__ void k_keep(Lattice l, long long n_sites, int mode, const int *first,
       site_pos(l, n, x);
       const double dx = __dsub_rn(x[0], cx), dy = __dsub_rn(x[1], cx), dz = __dsub_rn(x[2], cx);
       k = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)) < r2max ? 1 : 0;
+    } else if (mode == 3) {
+      // BallAdder::Add (collision.cc:23-31): r^2 <= r*r, then MDUnit::AddParticle's
+      // MDRect::IsInside (mdunit.cc:44-49, mdrect.h:35-38) for the unit [0, L)
+      double x[3];
+      const double *c = l.bc[ball_pos(l, n, x)];
+      const double dx = __dsub_rn(x[0], c[0]), dy = __dsub_rn(x[1], c[1]), dz = __dsub_rn(x[2], c[2]);
+      const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+      const bool inside = 0.0 <= x[0] && x[0] < l.L[0] && 0.0 <= x[1] && x[1] < l.L[1] && 0.0 <= x[2] && x[2] < l.L[2];
+      k = (!(r2 > r2max) && inside) ? 1 : 0;
     }
     keep[n] = k;
   }
 }
 
-__global__ void k_emit(Lattice l, long long n_sites, const int *keep, const int *keep_scan, double4_32a *q4, int cap) {
+// Writes the kept sites in order; p4 (when given) receives the velocities the
+// maker sets: (+speed, 0, 0) for the first ball and (-speed, 0, 0) for the
+// second (mode 3), zero otherwise.
+__global__ void k_emit(Lattice l, long long n_sites, int mode, const int *keep, const int *keep_scan, double4_32a *q4,
+                       double4_32a *p4, double speed, int cap) {
   for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < n_sites;
        n += (long long)gridDim.x * blockDim.x) {
     if (!keep[n]) continue;
     const int slot = keep_scan[n] - 1;
     if (slot >= cap) continue;
     double x[3];
-    site_pos(l, n, x);
+    double vx = 0.0;
+    if (mode == 3) {
+      vx = ball_pos(l, n, x) == 0 ? speed : -speed;
+    } else {
+      site_pos(l, n, x);
+    }
     q4[slot] = make_double4_32a(x[0], x[1], x[2], 0.0);
+    if (p4) p4[slot] = make_double4_32a(vx, 0.0, 0.0, 0.0);
   }
 }
 
@@ -290,9 +336,10 @@ using namespace mdg::init;
 extern "C" {
 
 int mdg_make_configuration(const double box[3], int32_t maker, double density, double radius, int32_t unit_id,
-                           double *q4_dev, int32_t capacity, int32_t *n, void *stream) {
-  if (!box || !n || !(density > 0.0) || capacity < 0 || maker < MDG_MAKER_FCC || maker > MDG_MAKER_DROPLET)
+                           double speed, double *q4_dev, double *p4_dev, int32_t capacity, int32_t *n, void *stream) {
+  if (!box || !n || !(density > 0.0) || capacity < 0 || maker < MDG_MAKER_FCC || maker > MDG_MAKER_COLLISION)
     return MDG_ERR_INVALID;
+  if (maker == MDG_MAKER_COLLISION && !(radius > 0.0)) return MDG_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   Buf buf;
   Lattice l;
@@ -351,6 +398,23 @@ int mdg_make_configuration(const double box[3], int32_t maker, double density, d
       }
     }
     first = d_first;
+  } else if (maker == MDG_MAKER_COLLISION) {
+    // Collision::Run (collision.cc:55-63): balls at (L/4, L/2, L/2) and
+    // (3L/4, L/2, L/2); BallAdder::Execute: is = int(2 r / s) cells per side
+    const double is = 2.0 * radius / s0;
+    if (!(is < 1024.0)) return MDG_ERR_CAPACITY;
+    l.sx = l.sy = l.sz = (int)is;
+    l.s = s0;
+    l.hs = s0 * 0.5;
+    l.br = radius;
+    for (int d = 0; d < 3; d++) {
+      l.bc[0][d] = box[d] * (d == 0 ? 0.25 : 0.5);
+      l.bc[1][d] = box[d] * (d == 0 ? 0.75 : 0.5);
+      l.L[d] = box[d];
+    }
+    l.per_ball = (long long)l.sx * l.sx * l.sx * 4;
+    n_sites = 2 * l.per_ball;
+    mode = 3;
   } else {
     // ConfigurationMaker / DropletMaker: floor(L / s) cells per side, offset 1e-7
     l.sx = (int)(box[0] / s0);
@@ -367,7 +431,7 @@ int mdg_make_configuration(const double box[3], int32_t maker, double density, d
   if (buf.get(&keep, (size_t)n_sites) != cudaSuccess || buf.get(&keep_scan, (size_t)n_sites) != cudaSuccess)
     return MDG_ERR_CUDA;
   const double c = box[0] * 0.5;
-  k_keep<<<grid_for(n_sites), kT, 0, s>>>(l, n_sites, mode, first, cut, c, radius * radius, keep);
+  if (n_sites > 0) k_keep<<<grid_for(n_sites), kT, 0, s>>>(l, n_sites, mode, first, cut, c, radius * radius, keep);
   if (cudaMemcpyAsync(keep_scan, keep, (size_t)n_sites * sizeof(int), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
     return MDG_ERR_CUDA;
   if (n_sites > 0 && scan(keep_scan, n_sites, s, buf) != cudaSuccess) return MDG_ERR_CUDA;
@@ -380,7 +444,8 @@ int mdg_make_configuration(const double box[3], int32_t maker, double density, d
   if (count > capacity) return MDG_ERR_CAPACITY;
   if (count > 0) {
     if (!q4_dev) return MDG_ERR_INVALID;
-    k_emit<<<grid_for(n_sites), kT, 0, s>>>(l, n_sites, keep, keep_scan, (double4_32a *)q4_dev, capacity);
+    k_emit<<<grid_for(n_sites), kT, 0, s>>>(l, n_sites, mode, keep, keep_scan, (double4_32a *)q4_dev,
+                                            (double4_32a *)p4_dev, speed, capacity);
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return MDG_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? MDG_OK : MDG_ERR_CUDA;

@@ -1,5 +1,6 @@
-// mdg_mdacp: runs MDACP's Benchmark and Langevin projects (benchmark.cc:12-52,
-// langevin.cc:9-32) on one GB300 through the C ABI.  Usage: mdg_mdacp [input.cfg]
+// mdg_mdacp: runs MDACP's Benchmark, Langevin, Collision and Burst projects
+// (benchmark.cc:12-52, langevin.cc:9-32, collision.cc:55-81, burst.cc:103-140)
+// on one GB300 through the C ABI.  Usage: mdg_mdacp [input.cfg]
 // (the reference reads input.cfg when no file is given, mdmanager.cc:18-23).
 //
 // Output lines keep the reference's layout: "time T P E #observe" every
@@ -15,6 +16,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <stdexcept>
 #include <string>
 
 #include "mdg_host.hpp"
@@ -112,6 +114,65 @@ void run_langevin(const mdghost::Parameter &param) {
   }
 }
 
+// Collision::Run (collision.cc:55-81): two balls of radius L_y / 4 at density
+// 0.374 moving at +1 and -1 along x, made on the device; no SetInitialVelocity.
+void run_collision(const mdghost::Parameter &param) {
+  const mdghost::SimulationInfo si(param);
+  const double radius = si.L[1] * 0.25, density = 0.374;
+  const double s = 1.0 / pow(density * 0.25, 1.0 / 3.0);
+  const long is = (long)(2 * radius / s);
+  const long sites = 8 * is * is * is;  // both balls' candidate sites bound the count
+  if (sites > 2000000000L) throw std::runtime_error("collision balls too large");
+  mdghost::MDManager m(param, sites > 0 ? (int)sites : 1);
+  m.MakeStateOnDevice(MDG_MAKER_COLLISION, density, radius, 1.0);
+  m.SaveAsCdviewSequential();
+  const int OBSERVE_LOOP = param.GetIntegerDef("ObserveLoop", 100);
+  const int TOTAL_LOOP = param.GetIntegerDef("TotalLoop", 1000);
+  const bool save_cdview_file = param.GetBooleanDef("SaveCdviewFile", false);
+  printf("# Number of Particles = %lu\n", m.GetTotalParticleNumber());
+  for (int i = 0; i < TOTAL_LOOP; i++) {
+    m.Calculate();
+    if (i % OBSERVE_LOOP == 0) {
+      printf("%.15g %.15g# observe\n", m.GetSimulationTime(), m.Temperature());
+      if (save_cdview_file) m.SaveAsCdviewSequential();
+    }
+  }
+  final_files(param, m);
+}
+
+// Burst::Run (burst.cc:103-140): a droplet of radius Radius (default 10) at
+// Density (default 0.5) with SetInitialVelocity(InitialVelocity), thermalised
+// ThermalizeLoop steps under the heat bath, then TotalLoop free steps.
+void run_burst(const mdghost::Parameter &param) {
+  const int n = lattice_count(param);
+  mdghost::MDManager m(param, n > 0 ? n : 1);
+  m.MakeStateOnDevice(MDG_MAKER_DROPLET, param.GetDoubleDef("Density", 0.5), param.GetDoubleDef("Radius", 10),
+                      param.GetDoubleDef("InitialVelocity", 1.0));
+  const int T_LOOP = param.GetIntegerDef("ThermalizeLoop", 150);
+  const int LOOP = param.GetIntegerDef("TotalLoop", 1000);
+  const int OBSERVE_LOOP = param.GetIntegerDef("ObserveLoop", 100);
+  printf("# Number of Particles = %lu\n", m.GetTotalParticleNumber());
+  m.MakePairList();
+  m.SetControlTemperature(true);
+  for (int i = 0; i < T_LOOP; i++) {
+    m.Calculate();
+    if (i % OBSERVE_LOOP == 0) m.SaveAsCdviewSequential();
+  }
+  m.SetControlTemperature(false);
+  const double start = now();
+  for (int i = 0; i < LOOP; i++) {
+    m.Calculate();
+    if (i % OBSERVE_LOOP == 0) {
+      observe_line(m, true);
+      m.SaveAsCdviewSequential();
+    }
+  }
+  const double sec = now() - start;
+  const unsigned long pn = m.GetTotalParticleNumber();
+  printf("# N = %lu %g [SEC] %g [MUPS]\n", pn, sec, (double)LOOP * (double)pn / sec / 1.0e6);
+  final_files(param, m);
+}
+
 }  // namespace
 
 // mdg_mdacp --print-config file.cfg: the parsed simulation settings, no GPU use.
@@ -154,6 +215,8 @@ int main(int argc, char **argv) {
   try {
     if (mode == "Benchmark") run_benchmark(param);
     else if (mode == "Langevin") run_langevin(param);
+    else if (mode == "Collision") run_collision(param);
+    else if (mode == "Burst") run_burst(param);
     else {
       printf("Mode %s is not found.\n", mode.c_str());
       return 1;

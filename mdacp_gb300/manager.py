@@ -112,8 +112,10 @@ class MDManager:
 
         maker: "fcc" (ConfigurationMaker, confmaker.cc:9-44), "extract"
         (ExtractConfigurationMaker for one unit spanning the box,
-        confmaker.cc:174-252) or "droplet" (DropletMaker, burst.cc:10-61, sites
-        within `radius` of the centre).  v0 > 0 draws velocities as
+        confmaker.cc:174-252), "droplet" (DropletMaker, burst.cc:10-61, sites
+        within `radius` of the centre) or "collision" (the two BallAdder balls
+        of Collision::Run, collision.cc:8-63, of `radius`, moving at +v0 and
+        -v0 along x).  For the others v0 > 0 draws velocities as
         Variables::SetInitialVelocity(v0, 0) (variables.cc:82-108).
         """
         self._ck(self.lib.mdg_make_state(self._h, native.MAKERS[maker], float(density), float(radius), float(v0)))

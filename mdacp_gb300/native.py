@@ -68,11 +68,12 @@ SIGNATURES = {
     "mdg_save_dump": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "mdg_save_cdview": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "mdg_make_configuration": (ctypes.c_int, [_D, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
-                                              _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _P]),
+                                              ctypes.c_double, _P, _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                              _P]),
     "mdg_make_velocity": (ctypes.c_int, [ctypes.c_double, ctypes.c_int32, _P, ctypes.c_int32, _P]),
     "mdg_make_state": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
 }
-MAKERS = {"fcc": 0, "extract": 1, "droplet": 2}
+MAKERS = {"fcc": 0, "extract": 1, "droplet": 2, "collision": 3}
 
 _lib = None
 

@@ -6,6 +6,10 @@
 //   orc_make_fcc      ConfigurationMaker::Execute (confmaker.cc:9-44)
 //   orc_make_extract  ExtractConfigurationMaker::Execute (confmaker.cc:174-252),
 //                     one unit spanning the box
+//   orc_make_droplet  DropletMaker::Execute / AddSub (burst.cc:10-61)
+//   orc_make_collision  the two BallAdder balls of Collision::Run
+//                     (collision.cc:8-63), each site kept by MDRect::IsInside
+//                     of the one unit [0, L) (mdunit.cc:44-49, mdrect.h:35-38)
 //   orc_initial_velocity  Variables::SetInitialVelocity (variables.cc:82-108)
 #include <algorithm>
 #include <cmath>
@@ -83,6 +87,63 @@ long orc_make_extract(const double L[3], double density, int unit_id, double *q3
           put(q3, n, cap, sub[k][0], sub[k][1], sub[k][2]);
         }
       }
+  return n;
+}
+
+long orc_make_droplet(const double L[3], double density, double radius, double *q3, long cap) {
+  const double s = 1.0 / pow(density * 0.25, 1.0 / 3.0);
+  const double hs = s * 0.5;
+  const double c = L[0] * 0.5;
+  const int sx = static_cast<int>(L[0] / s), sy = static_cast<int>(L[1] / s), sz = static_cast<int>(L[2] / s);
+  const double e = 0.0000001;
+  long n = 0;
+  auto add = [&](double x, double y, double z) {
+    const double dx = x - c, dy = y - c, dz = z - c;
+    if (dx * dx + dy * dy + dz * dz < radius * radius) put(q3, n, cap, x, y, z);
+  };
+  for (int iz = 0; iz < sz; iz++)
+    for (int iy = 0; iy < sy; iy++)
+      for (int ix = 0; ix < sx; ix++) {
+        const double x = static_cast<double>(ix) * s, y = static_cast<double>(iy) * s, z = static_cast<double>(iz) * s;
+        add(x + e, y + e, z + e);
+        add(x + e, y + hs + e, z + hs + e);
+        add(x + hs + e, y + e, z + hs + e);
+        add(x + hs + e, y + hs + e, z + e);
+      }
+  return n;
+}
+
+long orc_make_collision(const double L[3], double density, double radius, double speed, double *q3, double *p3,
+                        long cap) {
+  const double centre[2][3] = {{L[0] * 0.25, L[1] * 0.5, L[2] * 0.5}, {L[0] * 0.75, L[1] * 0.5, L[2] * 0.5}};
+  const double s = 1.0 / pow(density * 0.25, 1.0 / 3.0);
+  const int is = static_cast<int>(2 * radius / s);
+  const double hs = s * 0.5;
+  long n = 0;
+  for (int b = 0; b < 2; b++) {
+    const double *c = centre[b];
+    const double v = b == 0 ? speed : -speed;
+    auto add = [&](double x, double y, double z) {
+      const double dx = x - c[0], dy = y - c[1], dz = z - c[2];
+      if (dx * dx + dy * dy + dz * dz > radius * radius) return;
+      if (!(0.0 <= x && x < L[0] && 0.0 <= y && y < L[1] && 0.0 <= z && z < L[2])) return;
+      if (p3 && n < cap) {
+        p3[3 * n + 0] = v;
+        p3[3 * n + 1] = 0.0;
+        p3[3 * n + 2] = 0.0;
+      }
+      put(q3, n, cap, x, y, z);
+    };
+    for (int iz = 0; iz < is; iz++)
+      for (int iy = 0; iy < is; iy++)
+        for (int ix = 0; ix < is; ix++) {
+          const double x = ix * s - radius + c[0], y = iy * s - radius + c[1], z = iz * s - radius + c[2];
+          add(x, y, z);
+          add(x + hs, y, z);
+          add(x, y + hs, z);
+          add(x, y, z + hs);
+        }
+  }
   return n;
 }
 

@@ -58,6 +58,11 @@ def _mk():
         lib.orc_make_fcc.argtypes = [dp, ctypes.c_double, dp, ctypes.c_long]
         lib.orc_make_extract.restype = ctypes.c_long
         lib.orc_make_extract.argtypes = [dp, ctypes.c_double, ctypes.c_int, dp, ctypes.c_long]
+        lib.orc_make_droplet.restype = ctypes.c_long
+        lib.orc_make_droplet.argtypes = [dp, ctypes.c_double, ctypes.c_double, dp, ctypes.c_long]
+        lib.orc_make_collision.restype = ctypes.c_long
+        lib.orc_make_collision.argtypes = [dp, ctypes.c_double, ctypes.c_double, ctypes.c_double, dp, dp,
+                                           ctypes.c_long]
         lib.orc_initial_velocity.restype = None
         lib.orc_initial_velocity.argtypes = [dp, ctypes.c_long, ctypes.c_double, ctypes.c_int]
         _makers = lib
@@ -78,6 +83,29 @@ def make_configuration(maker, L, density, unit_id=0):
         q = np.zeros((n, 3))
         lib.orc_make_extract(L3.ctypes.data_as(dp), density, unit_id, q.ctypes.data_as(dp), n)
     return q
+
+
+def make_state(maker, L, density, radius=0.0, v0=0.0, unit_id=0):
+    """(q, p) as the reference sets them up: the maker's positions, then
+    SetInitialVelocity(v0, unit_id) ("fcc", "extract", "droplet" as in
+    Burst::Run), or the collision balls' own velocities +-v0 along x."""
+    L3 = np.ascontiguousarray(np.broadcast_to(np.asarray(L, dtype=np.float64), (3,)))
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib = _mk()
+    if maker == "collision":
+        n = lib.orc_make_collision(L3.ctypes.data_as(dp), density, radius, v0, None, None, 0)
+        q, p = np.zeros((n, 3)), np.zeros((n, 3))
+        lib.orc_make_collision(L3.ctypes.data_as(dp), density, radius, v0, q.ctypes.data_as(dp),
+                               p.ctypes.data_as(dp), n)
+        return q, p
+    if maker == "droplet":
+        n = lib.orc_make_droplet(L3.ctypes.data_as(dp), density, radius, None, 0)
+        q = np.zeros((n, 3))
+        lib.orc_make_droplet(L3.ctypes.data_as(dp), density, radius, q.ctypes.data_as(dp), n)
+    else:
+        q = make_configuration(maker, L3, density, unit_id)
+    p = initial_velocity(len(q), v0, unit_id) if v0 != 0.0 else np.zeros_like(q)
+    return q, p
 
 
 def initial_velocity(n, v0, seed=0):

@@ -11,9 +11,13 @@
 //
 // .cfg keys read here (all other keys are the reference's own):
 //   OracleTask=pairs|force|trace|bench|write|make   what to run
-//   OracleMaker=fcc|extract (task make: ConfigurationMaker or
+//   OracleMaker=fcc|extract|collision|droplet (task make: ConfigurationMaker or
 //     ExtractConfigurationMaker on the empty system, then
-//     MDManager::SetInitialVelocity(InitialVelocity); Density as the reference reads it)
+//     MDManager::SetInitialVelocity(InitialVelocity); Density as the reference
+//     reads it.  collision and droplet run the reference's own Collision::Run
+//     (collision.cc:55-81) and Burst::Run (burst.cc:103-140), whose makers are
+//     local to those files, with TotalLoop=0 (and ThermalizeLoop=0) in the
+//     .cfg so that only their set-up runs)
 //   OracleInput=<file>                    int64 n, then n x {qx qy qz px py pz} doubles
 //   OracleOutput=<prefix>                 output file prefix
 //   OracleBufferLength=<margin>           overrides BufferLength (simulationinfo.cc:6)
@@ -34,6 +38,11 @@
 #include <omp.h>
 #include "projectmanager.h"
 #include "confmaker.h"
+#include "collision.h"
+#include "burst.h"
+
+extern Collision coll;  // collision.cc:6
+extern Burst burst;     // burst.cc:8
 #include "communicator.h"
 #include "mpistream.h"
 
@@ -185,14 +194,20 @@ class OracleProject : public Project {
     }
     if (task == "make") {
       const std::string maker = param->GetStringDef("OracleMaker", "fcc");
-      if (maker == "extract") {
-        ExtractConfigurationMaker c(param);
-        mdm->ExecuteAll(&c);
+      if (maker == "collision") {
+        coll.Run(mdm);
+      } else if (maker == "droplet") {
+        burst.Run(mdm);
       } else {
-        ConfigurationMaker c(param);
-        mdm->ExecuteAll(&c);
+        if (maker == "extract") {
+          ExtractConfigurationMaker c(param);
+          mdm->ExecuteAll(&c);
+        } else {
+          ConfigurationMaker c(param);
+          mdm->ExecuteAll(&c);
+        }
+        if (param->Contains("InitialVelocity")) mdm->SetInitialVelocity(param->GetDouble("InitialVelocity"));
       }
-      if (param->Contains("InitialVelocity")) mdm->SetInitialVelocity(param->GetDouble("InitialVelocity"));
       FILE *f = fopen((out + "_made.bin").c_str(), "wb");
       OrderDumper od(f);
       mdm->ExecuteAllSerial(&od);

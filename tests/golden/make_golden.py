@@ -63,19 +63,30 @@ def io_fixture():
     np.savez_compressed(os.path.join(HERE, "io_small"), q=q, p=p, L=L, **blobs)
 
 
-MAKER_CASES = [("fcc", (10.0, 10.0, 10.0), 0.5), ("fcc", (10.0, 12.0, 11.0), 0.8), ("extract", (10.0,) * 3, 0.5),
-               ("extract", (23.7,) * 3, 0.8), ("extract", (30.0,) * 3, 0.5)]
+# (maker, box, density, radius, v0): v0 is SetInitialVelocity's speed, or the
+# balls' speed for the collision maker (Collision::Run fixes it at 1.0, the
+# radius at L_y / 4 and the density at 0.374, collision.cc:55-63)
+MAKER_CASES = [("fcc", (10.0, 10.0, 10.0), 0.5, 0.0, 1.5), ("fcc", (10.0, 12.0, 11.0), 0.8, 0.0, 1.5),
+               ("extract", (10.0,) * 3, 0.5, 0.0, 1.5), ("extract", (23.7,) * 3, 0.8, 0.0, 1.5),
+               ("extract", (30.0,) * 3, 0.5, 0.0, 1.5),
+               ("collision", (60.0, 30.0, 30.0), 0.374, 7.5, 1.0), ("collision", (50.0, 40.0, 36.0), 0.374, 10.0, 1.0),
+               ("droplet", (20.0,) * 3, 0.6, 6.5, 1.5), ("droplet", (26.0,) * 3, 0.5, 9.0, 1.5)]
 
 
 def makers_fixture():
+    """Positions and velocities the reference's makers produce: its
+    ConfigurationMaker / ExtractConfigurationMaker + SetInitialVelocity, and
+    its Collision::Run / Burst::Run set-up (loops at zero)."""
     out = {}
     dummy = np.zeros((1, 3))
-    for k, (maker, L, rho) in enumerate(MAKER_CASES):
-        o = refrun.run("make", dummy, dummy, np.array(L), rc=RC, margin=MARGIN,
-                       extra={"OracleMaker": maker, "Density": rho, "InitialVelocity": 1.5})
+    for k, (maker, L, rho, radius, v0) in enumerate(MAKER_CASES):
+        extra = {"OracleMaker": maker, "Density": rho, "InitialVelocity": v0, "TotalLoop": 0,
+                 "ThermalizeLoop": 0, "Radius": radius}
+        o = refrun.run("make", dummy, dummy, np.array(L), rc=RC, margin=MARGIN, extra=extra)
         out["q%d" % k], out["p%d" % k] = o["q"], o["p"]
         out["L%d" % k], out["rho%d" % k] = np.array(L), rho
-    np.savez_compressed(os.path.join(HERE, "makers"), makers=np.array([m for m, _, _ in MAKER_CASES]), **out)
+        out["radius%d" % k], out["v0%d" % k] = radius, v0
+    np.savez_compressed(os.path.join(HERE, "makers"), makers=np.array([c[0] for c in MAKER_CASES]), **out)
 
 
 if __name__ == "__main__":

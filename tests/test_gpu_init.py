@@ -3,11 +3,13 @@
 tests/golden/makers.npz holds the states the reference wrote (made by
 tests/golden/make_golden.py): ConfigurationMaker (confmaker.cc:9-44) and
 ExtractConfigurationMaker (confmaker.cc:174-252, mt19937(0) deletions), then
-MDManager::SetInitialVelocity(1.5) (variables.cc:82-108).  Positions must be
-bit-identical in the same order; velocities come from the device's cos/sin
-and a parallel mean, so they agree to rounding.  DropletMaker (burst.cc:10-61)
-is local to the reference's Burst project, so it is checked against a numpy
-restatement of its loop.
+MDManager::SetInitialVelocity(1.5) (variables.cc:82-108); and the set-up of
+the reference's Collision::Run (two BallAdder balls, collision.cc:8-63) and
+Burst::Run (DropletMaker + SetInitialVelocity, burst.cc:10-61,103-109).
+Positions must be bit-identical in the same order; velocities come from the
+device's cos/sin and a parallel mean, so they agree to rounding (the
+collision balls' +-speed exactly).  The droplet is also checked against a
+numpy restatement of its loop.
 """
 import os
 
@@ -32,12 +34,16 @@ def _made(L, maker, rho, v0=1.5, radius=0.0, capacity=None):
 @pytest.mark.parametrize("k", range(len(GOLD["makers"])))
 def test_makers_match_reference(k):
     maker = str(GOLD["makers"][k])
-    q, p = _made(GOLD["L%d" % k], maker, float(GOLD["rho%d" % k]))
+    q, p = _made(GOLD["L%d" % k], maker, float(GOLD["rho%d" % k]), v0=float(GOLD["v0%d" % k]),
+                 radius=float(GOLD["radius%d" % k]))
     qr, pr = GOLD["q%d" % k], GOLD["p%d" % k]
     assert q.shape == qr.shape
     assert np.array_equal(q, qr), np.abs(q - qr).max()
-    np.testing.assert_allclose(p, pr, rtol=0, atol=1e-13)
-    assert np.abs(p.mean(axis=0)).max() < 1e-13
+    if maker == "collision":
+        assert np.array_equal(p, pr)
+    else:
+        np.testing.assert_allclose(p, pr, rtol=0, atol=1e-13)
+        assert np.abs(p.mean(axis=0)).max() < 1e-13
 
 
 def test_droplet_matches_restated_loop():

@@ -107,3 +107,50 @@ def test_benchmark_project_starts_from_the_reference_extract_state(host_bin, tmp
     assert raw.shape[0] == len(q) == int(20.0 ** 3 * 0.6)
     assert np.array_equal(raw[:, :3], q)
     np.testing.assert_allclose(raw[:, 3:], port.initial_velocity(len(q), 1.2, 0), rtol=0, atol=1e-13)
+
+
+@pytest.mark.gpu
+def test_collision_project_matches_oracle(host_bin, tmp_path):
+    # Collision::Run: the two balls made on the device, then NVE steps with a
+    # temperature line every ObserveLoop steps and the initial CDView file
+    from oracle import port
+    text = ("Mode=Collision\nSystemSizeX=60\nSystemSizeY=30\nSystemSizeZ=30\nTimeStep=0.002\nTotalLoop=100\n"
+            "ObserveLoop=20\nCutoffLength=2.5\nBufferLength=0.5\nFinalDumpFile=%s\n" % (tmp_path / "final.dump"))
+    out = subprocess.run([host_bin, _cfg(tmp_path, text)], capture_output=True, text=True, timeout=300,
+                         cwd=str(tmp_path))
+    assert out.returncode == 0, out.stdout + out.stderr
+    rows = np.array([[float(x) for x in l.replace("# observe", "").split()] for l in out.stdout.splitlines()
+                     if l.endswith("# observe")])
+    L = np.array([60.0, 30.0, 30.0])
+    q, p = port.make_state("collision", L, 0.374, 7.5, 1.0)
+    first = np.loadtxt(tmp_path / "conf0000.cd")
+    assert first.shape == (len(q), 8) and np.allclose(first[:, 2:5], q, rtol=1e-5)
+    s = port.System(q, p, L, rc=2.5, margin=0.5, dt=0.002)
+    s.make_pairlist()
+    ref, done = [], 0
+    for c in (1, 21, 41, 61, 81):
+        s.calculate(c - done)
+        done = c
+        ref.append([c * 0.002, s.observe()[0]])
+    np.testing.assert_allclose(rows, np.array(ref), rtol=1e-10, atol=1e-12)
+    s.calculate(100 - done)
+    qf, pf = s.state()
+    dump = np.fromfile(tmp_path / "final.dump", dtype="<f8").reshape(-1, 6)
+    dq = (dump[:, :3] - qf + L / 2) % L - L / 2
+    assert np.abs(dq).max() < 1e-9 and np.abs(dump[:, 3:] - pf).max() < 1e-9
+
+
+@pytest.mark.gpu
+def test_burst_project_runs(host_bin, tmp_path):
+    # Burst::Run: droplet + SetInitialVelocity, heat-bath thermalisation, then free steps
+    text = ("Mode=Burst\nSystemSize=30\nDensity=0.8\nRadius=8\nInitialVelocity=0.9\nAimedTemperature=1.5\n"
+            "HeatbathType=Langevin\nHeatbathGamma=1.0\nThermalizeLoop=200\nTotalLoop=200\nObserveLoop=100\n"
+            "TimeStep=0.005\nCutoffLength=2.5\nBufferLength=0.5\n")
+    out = subprocess.run([host_bin, _cfg(tmp_path, text)], capture_output=True, text=True, timeout=300,
+                         cwd=str(tmp_path))
+    assert out.returncode == 0, out.stdout + out.stderr
+    from oracle import port
+    q, _ = port.make_state("droplet", 30.0, 0.8, 8.0, 0.9)
+    assert re.search(r"# N = %d .* \[MUPS\]" % len(q), out.stdout)
+    assert len([l for l in out.stdout.splitlines() if l.endswith("#observe")]) == 2
+    assert sorted(f for f in os.listdir(tmp_path) if f.endswith(".cd")) == ["conf%04d.cd" % i for i in range(4)]

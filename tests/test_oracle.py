@@ -156,7 +156,7 @@ def test_maker_restatement_matches_reference_fixture():
     # oracle/makers.cc against the states the reference's own makers wrote
     gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "makers.npz"))
     for k, maker in enumerate(gold["makers"]):
-        q = port.make_configuration(str(maker), gold["L%d" % k], float(gold["rho%d" % k]))
-        assert np.array_equal(q, gold["q%d" % k])
-        p = port.initial_velocity(len(q), 1.5, 0)
+        q, p = port.make_state(str(maker), gold["L%d" % k], float(gold["rho%d" % k]), float(gold["radius%d" % k]),
+                               float(gold["v0%d" % k]))
+        assert np.array_equal(q, gold["q%d" % k]), maker
         np.testing.assert_allclose(p, gold["p%d" % k], rtol=0, atol=1e-15)
