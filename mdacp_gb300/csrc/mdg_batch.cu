@@ -337,21 +337,41 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
       sy = fmaf(df, dy, sy);
       sz = fmaf(df, dz, sz);
     };
+    // this lane's entries lane, lane + LPI, ... in batches of four: the next
+    // batch's entries are requested before this batch's positions are used,
+    // and the last full batch requests the remainder
+    const int mine = cnt > lane ? (cnt - lane + LPI - 1) / LPI : 0;
+    const int full = mine - mine % 4;
+    uint32_t en[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int kn = lane + u * LPI;
+      en[u] = kn < cnt ? __ldg(row + (long long)kn * n) : 0u;
+    }
     int k = lane;
-    // four entries' index and position loads in flight per lane
-    for (; k + 3 * LPI < cnt; k += 4 * LPI) {
+    for (int j = 0; j < full; j += 4, k += 4 * LPI) {
       uint32_t e[4];
       float4 l[4];
 #pragma unroll
-      for (int u = 0; u < 4; u++) e[u] = __ldg(row + (long long)(k + u * LPI) * n);
+      for (int u = 0; u < 4; u++) e[u] = en[u];
 #pragma unroll
       for (int u = 0; u < 4; u++) l[u] = __ldg(loc + entry_slot(e[u]));
 #pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int kn = k + (4 + u) * LPI;
+        en[u] = kn < cnt ? __ldg(row + (long long)kn * n) : 0u;
+      }
+#pragma unroll
       for (int u = 0; u < 4; u++) pair(e[u], l[u]);
     }
-    for (; k < cnt; k += LPI) {
-      const uint32_t e = __ldg(row + (long long)k * n);
-      pair(e, __ldg(loc + entry_slot(e)));
+    if (full < mine) {
+      // missing entries get a partner at 1e30: r^2 overflows to +inf, no force
+      float4 l[3];
+#pragma unroll
+      for (int u = 0; u < 3; u++)
+        l[u] = k + u * LPI < cnt ? __ldg(loc + entry_slot(en[u])) : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+#pragma unroll
+      for (int u = 0; u < 3; u++) pair(en[u], l[u]);
     }
     fx = (double)sx;
     fy = (double)sy;

@@ -173,21 +173,39 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
     sz = fmaf(df, dz, sz);
   };
   int k = 0;
-  // kUnroll entries' independent index and position loads in flight per thread
+  // the next batch's list entries are requested before this batch's partner
+  // positions are used, so the entry load (from DRAM) overlaps the gathers;
+  // the last full batch requests the row's remaining (< kUnroll) entries
+  const int full = cnt - cnt % kUnroll;
+  uint32_t en[kUnroll];
+#pragma unroll
+  for (int u = 0; u < kUnroll; u++) en[u] = u < cnt ? __ldg(row + (size_t)u * stride) : 0u;
 #pragma unroll 1
-  for (; k + kUnroll <= cnt; k += kUnroll) {
+  for (; k < full; k += kUnroll) {
     uint32_t e[kUnroll];
     float4 l[kUnroll];
 #pragma unroll
-    for (int u = 0; u < kUnroll; u++) e[u] = __ldg(row + (size_t)(k + u) * stride);
+    for (int u = 0; u < kUnroll; u++) e[u] = en[u];
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) l[u] = __ldg(loc + entry_slot(e[u]));
 #pragma unroll
+    for (int u = 0; u < kUnroll; u++) {
+      const int kn = k + kUnroll + u;
+      en[u] = kn < cnt ? __ldg(row + (size_t)kn * stride) : 0u;
+    }
+#pragma unroll
     for (int u = 0; u < kUnroll; u++) pair(e[u], l[u]);
   }
-  for (; k < cnt; k++) {
-    const uint32_t e = __ldg(row + (size_t)k * stride);
-    pair(e, __ldg(loc + entry_slot(e)));
+  if (k < cnt) {
+    // the remainder as one batch; missing entries get a partner at 1e30,
+    // whose r^2 overflows to +inf and contributes nothing
+    constexpr int kTail = kUnroll > 1 ? kUnroll - 1 : 1;
+    float4 l[kTail];
+#pragma unroll
+    for (int u = 0; u < kTail; u++)
+      l[u] = k + u < cnt ? __ldg(loc + entry_slot(en[u])) : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+#pragma unroll
+    for (int u = 0; u < kTail; u++) pair(en[u], l[u]);
   }
   if (PRUNE) *kept = m;
   return make_double3((double)sx, (double)sy, (double)sz);
