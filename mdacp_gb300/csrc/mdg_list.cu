@@ -47,7 +47,11 @@ __device__ __forceinline__ bool exact_within(const Geom &g, const double4_32a &q
 // a time (independent loads in flight), then tested in order.
 __global__ void __launch_bounds__(kListThreads, MDG_LIST_MIN_BLOCKS) k_build_list(Geom g, Dev d) {
   DevFlags *f = d.flags;
-  if (f->halt != 0 || f->rebuild == 0) return;
+  // one read for the whole block: another block may set the halt meanwhile
+  __shared__ int s_run;
+  if (threadIdx.x == 0) s_run = f->halt == 0 && f->rebuild != 0;
+  __syncthreads();
+  if (!s_run) return;
   unsigned long long tot = 0;
   int mx = 0;
   const float acc_lo = g.acc_lo, acc_hi = g.acc_hi;
