@@ -641,7 +641,8 @@ int mdg_calculate(mdg_handle *h, int32_t nsteps) {
     h->launches += 2;
     h->nh_init = false;
   }
-  if (h->pending == 0) MDG_CK(cudaEventRecord(h->ev0, h->stream));
+  // the call's own steps: ev0 follows any steps still outstanding in the stream
+  MDG_CK(cudaEventRecord(h->ev0, h->stream));
   rc = enqueue_steps(h, nsteps);
   if (rc) return rc;
   MDG_CK(cudaEventRecord(h->ev1, h->stream));

@@ -237,3 +237,18 @@ def test_state_roundtrip_and_bad_state():
         m.make_pairlist()
     m.set_state(q, p)   # the handle stays usable
     m.calculate(5)
+
+
+def test_elapsed_time_is_the_last_calls_steps():
+    # elapsed_ms covers the steps of the last calculate call only, also when
+    # an earlier call's steps were still outstanding
+    q, p, L = liquid_like(0.5, 24, seed=54)
+    m = _gpu(L, len(q), precision="mixed")
+    m.set_state(q, p)
+    m.make_pairlist()
+    m.calculate(300)
+    m.calculate(30)
+    t_short = m.stats()["elapsed_ms"]
+    m.calculate(300)
+    t_long = m.stats()["elapsed_ms"]
+    assert 0 < t_short < 0.5 * t_long
