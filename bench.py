@@ -299,6 +299,7 @@ def run_mine(args):
     me = MDManager(L, capacity=n, cutoff=RC, margin=MARGIN, dt=DT, precision="mixed", device=d.local)
     me.set_state(qh, ph)
     me.calculate(W)
+    me.synchronize()  # the warm-up steps finish before the clock starts
     d.barrier()
     t0 = time.perf_counter()
     me.set_state(qh, ph)

@@ -73,7 +73,9 @@ typedef struct mdg_stats {
   int32_t cells[3];        /* cell grid */
   int32_t particles;
   double zeta;             /* Nose-Hoover friction (Variables::Zeta) */
-  double elapsed_ms;       /* device time of the steps of the last mdg_calculate call */
+  double elapsed_ms;       /* device time of the steps of the last mdg_calculate call with
+                              nsteps > 1; after single-step calls, from the first of them to
+                              their confirmation */
   int64_t kernel_launches; /* kernels this handle has enqueued (graph replays count each node) */
   int64_t inner_pairs;     /* directed pairs in the inner list at the last prune */
   int64_t prunes;          /* inner-list selections since the last mdg_set_state */

@@ -37,11 +37,13 @@ struct mdg_handle {
   int par = 0;
   cudaGraphExec_t gx_pair[2] = {nullptr, nullptr};
   cudaGraphExec_t gx_one[2] = {nullptr, nullptr};
+  int graph_n = -1;  // particle count the graphs were captured for
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
   long long steps_host = 0;  // completed steps as last read from the device
   long long launches = 0;    // kernels enqueued (counting every node of a graph replay)
   long long pending = 0;     // steps enqueued by mdg_calculate and not yet confirmed
+  bool ev1_due = false;      // the timing end event is recorded when the steps are confirmed
 };
 
 // Steps mdg_calculate may leave enqueued before it waits for them.
@@ -69,6 +71,7 @@ void drop_graphs(mdg_handle *h) {
     if (h->gx_one[k]) cudaGraphExecDestroy(h->gx_one[k]);
     h->gx_pair[k] = h->gx_one[k] = nullptr;
   }
+  h->graph_n = -1;
 }
 
 template <class T>
@@ -324,6 +327,7 @@ int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps) {
   if (rc == MDG_OK) {
     cudaError_t e = cudaGraphInstantiate(out, g, 0);
     if (e != cudaSuccess) rc = fail(h, MDG_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    else h->graph_n = h->g.n;
   }
   cudaGraphDestroy(g);
   return rc;
@@ -396,6 +400,8 @@ int settle(mdg_handle *h) {
     if (rc) return rc;
     h->steps_host = (long long)h->hflags->steps - 1;
   }
+  if (h->ev1_due) MDG_CK(cudaEventRecord(h->ev1, h->stream));
+  h->ev1_due = false;
   MDG_CK(cudaEventSynchronize(h->ev1));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, h->ev0, h->ev1);
@@ -552,7 +558,8 @@ static int set_state_common(mdg_handle *h, int32_t n) {
   MDG_CK(cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.nrank * sizeof(int), h->stream));
   MDG_CK(cudaMemcpyAsync(h->d.flags, h->hflags, sizeof(DevFlags), cudaMemcpyHostToDevice, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
-  drop_graphs(h);
+  // the graphs hold the geometry by value; they stay valid for the same count
+  if (h->graph_n != n) drop_graphs(h);
   h->has_state = true;
   h->nh_init = true;
   h->par = 0;
@@ -641,11 +648,16 @@ int mdg_calculate(mdg_handle *h, int32_t nsteps) {
     h->launches += 2;
     h->nh_init = false;
   }
-  // the call's own steps: ev0 follows any steps still outstanding in the stream
-  MDG_CK(cudaEventRecord(h->ev0, h->stream));
+  // A multi-step call is timed on its own: ev0 follows any steps still
+  // outstanding in the stream, ev1 its last step.  A run of single-step calls
+  // (MDManager::Calculate once per step) records no events between the steps
+  // (each record costs about 7 us of device time): it is timed from its first
+  // call to the point where it is confirmed.
+  if (nsteps > 1 || h->pending == 0) MDG_CK(cudaEventRecord(h->ev0, h->stream));
   rc = enqueue_steps(h, nsteps);
   if (rc) return rc;
-  MDG_CK(cudaEventRecord(h->ev1, h->stream));
+  h->ev1_due = nsteps == 1;
+  if (!h->ev1_due) MDG_CK(cudaEventRecord(h->ev1, h->stream));
   h->pending += nsteps;
   if (h->pending >= kMaxPending) return settle(h);
   return MDG_OK;

@@ -252,3 +252,20 @@ def test_elapsed_time_is_the_last_calls_steps():
     m.calculate(300)
     t_long = m.stats()["elapsed_ms"]
     assert 0 < t_short < 0.5 * t_long
+
+
+def test_new_state_of_the_same_size_reuses_graphs_correctly():
+    # the step graphs hold the geometry by value: a new state with the same
+    # particle count keeps them, a different count rebuilds them
+    qa, pa, L = liquid_like(0.5, 10, seed=55)
+    qb, pb, _ = liquid_like(0.5, 10, seed=56)
+    m = _gpu(L, len(qa))
+    m.set_state(qa, pa)
+    m.calculate(20)
+    for q, p in ((qb, pb), (qa[:-7], pa[:-7])):
+        m.set_state(q, p)
+        m.calculate(40)
+        ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+        ref.make_pairlist()
+        ref.calculate(40)
+        np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-10, atol=1e-12)
