@@ -159,6 +159,9 @@ typedef struct mdg_batch_params {
   double dt;
   int32_t list_capacity;  /* neighbour slots per particle; 0 = from the densest box */
   int32_t use_graphs;
+  double prune_buffer;    /* inner-list buffer (one lane per particle): the step walks the listed
+                             pairs within rc + buffer; negative = min(0.1, margin / 2) (default),
+                             0 = walk every listed pair */
 } mdg_batch_params;
 
 typedef struct mdg_batch_stats {
@@ -170,7 +173,7 @@ typedef struct mdg_batch_stats {
   int32_t threads;            /* CTA size of the persistent kernel */
   int32_t lanes_per_particle; /* lanes sharing one particle's row */
   int32_t ctas_per_sm;
-  int32_t reserved;
+  int32_t inner_list;         /* 1: the step walks the inner list (chosen by mdg_batch_tune) */
   double elapsed_ms;          /* device time of the last mdg_batch_calculate */
   int64_t kernel_launches;
 } mdg_batch_stats;

@@ -14,13 +14,13 @@ from . import lattice, native
 class BatchParams(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("device", ctypes.c_int32), ("cutoff", ctypes.c_double),
                 ("margin", ctypes.c_double), ("dt", ctypes.c_double), ("list_capacity", ctypes.c_int32),
-                ("use_graphs", ctypes.c_int32)]
+                ("use_graphs", ctypes.c_int32), ("prune_buffer", ctypes.c_double)]
 
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int64), ("rebuilds", ctypes.c_int64), ("particles", ctypes.c_int64),
                 ("boxes", ctypes.c_int32), ("list_capacity", ctypes.c_int32), ("threads", ctypes.c_int32),
-                ("lanes_per_particle", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("lanes_per_particle", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("inner_list", ctypes.c_int32),
                 ("elapsed_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64)]
 
 
@@ -77,13 +77,15 @@ def make_replicas(nbox, seed=1, n_range=(500, 8000), rho_range=(0.3, 0.9), t_ran
 
 class Batch:
     def __init__(self, boxes, cutoff=2.5, margin=0.4, dt=0.002, precision="fp64", list_capacity=0, device=0,
-                 use_graphs=True):
+                 use_graphs=True, prune_buffer=None):
         self.lib = _lib()
         prm = BatchParams()
         self.lib.mdg_batch_params_default(ctypes.byref(prm))
         prm.precision = {"fp64": native.FP64, "mixed": native.MIXED}[precision]
         prm.device, prm.cutoff, prm.margin, prm.dt = device, cutoff, margin, dt
         prm.list_capacity, prm.use_graphs = list_capacity, 1 if use_graphs else 0
+        if prune_buffer is not None:
+            prm.prune_buffer = prune_buffer
         self.n = np.array([len(b[0]) for b in boxes], dtype=np.int32)
         Ls = np.ascontiguousarray(np.array([np.broadcast_to(b[2], (3,)) for b in boxes], dtype=np.float64))
         self.L = Ls

@@ -60,6 +60,12 @@ struct Params {
   float acc_lo, acc_hi, rc2f, c2x8f;
   int list_cap;
   int nbox;
+  // inner list (one lane per particle): the listed pairs within rc + buffer,
+  // re-selected when a particle of the box moved buffer / 2 since the last
+  // selection, and after every rebuild
+  int inner;
+  float prune_thr2f, half_prune2;
+  double prune_thr2d;
 };
 
 struct Dev {
@@ -68,9 +74,10 @@ struct Dev {
   double4_32a *q_end, *q_mid[2], *p, *q_build, *t_q, *t_p;
   float4 *qf, *loc[2];
   int *id, *cell, *t_id, *t_cell, *order, *cell_start;
-  uint32_t *nl;
-  int *ncount;
-  int *box_rebuild, *box_err, *box_need;
+  uint32_t *nl, *pl;  // outer rows; inner rows in the same layout
+  int *ncount, *pcount;
+  float4 *loc_p;       // local positions at the last inner-list selection
+  int *box_rebuild, *box_err, *box_need, *box_prune;
   long long *box_steps, *box_rebuilds, *goal;
   double *partials;  // per box: KE, PE, virial
   const int *box_of_slot;
@@ -305,14 +312,21 @@ __global__ void __launch_bounds__(128) k_batch_list(Params P, Dev d, int total) 
 }
 
 // Force on local particle a of box b from its row, lanes l = 0..LPI-1 of a group
-// taking every LPI-th entry; returns the group sum on every lane.
-template <int MIXED, int LPI>
-__device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, const BoxDesc &b, int a, int lane, int par) {
+// taking every LPI-th entry; returns the group sum on every lane.  MODE 0 walks
+// the outer row; MODE 1 (one lane per particle) walks the outer row and, when
+// `select` is set, copies the entries within the inner radius to the inner row
+// (*kept: their number); MODE 2 walks the inner row.
+template <int MIXED, int LPI, int MODE>
+__device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, const BoxDesc &b, int a, int lane, int par,
+                                             bool select = false, int *kept = nullptr) {
+  static_assert(MODE == 0 || LPI == 1, "the inner list is kept for one lane per particle");
   const int o = b.atom_off, n = b.n;
   int cx, cy, cz;
   cell_xyz(b, d.cell[o + a], cx, cy, cz);
-  const int cnt = d.ncount[o + a];
-  const uint32_t *row = d.nl + b.list_off + a;
+  const int cnt = MODE == 2 ? d.pcount[o + a] : d.ncount[o + a];
+  const uint32_t *row = (MODE == 2 ? d.pl : d.nl) + b.list_off + a;
+  uint32_t *prow = d.pl + b.list_off + a;
+  int m = 0;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (MIXED) {
     const float4 li = d.loc[par][o + a];
@@ -328,6 +342,7 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
       const float dy = lj.y + fmaf(fmaf(qy.b, ty, qy.a), ty, qy.c);
       const float dz = lj.z + fmaf(fmaf(qz.b, tz, qz.a), tz, qz.c);
       const float r2 = dx * dx + dy * dy + dz * dz;
+      if (MODE == 1 && select && r2 <= P.prune_thr2f) prow[(long long)(m++) * n] = e;
       float inv;
       asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
       const float i6 = inv * inv * inv;
@@ -390,6 +405,7 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
       }
       const double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
       const double r2 = dx * dx + dy * dy + dz * dz;
+      if (MODE == 1 && select && r2 <= P.prune_thr2d) prow[(long long)(m++) * n] = e;
       if (r2 <= P.rc2) {
         const double inv = rcp_hh3(r2);
         const double i6 = inv * inv * inv;
@@ -400,6 +416,7 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
       }
     }
   }
+  if (MODE == 1 && kept) *kept = m;
   if (LPI > 1) {
 #pragma unroll
     for (int off = LPI / 2; off > 0; off >>= 1) {
@@ -420,18 +437,24 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
 #ifndef MDG_BATCH_MIN_BLOCKS
 #define MDG_BATCH_MIN_BLOCKS 2
 #endif
-template <int MIXED, int LPI>
+template <int MIXED, int LPI, int INNER>
 __global__ void __launch_bounds__(512, MIXED ? MDG_BATCH_MIN_BLOCKS : 2) k_batch_step(Params P, Dev d, int par) {
-  __shared__ int s_flag[2];
+  __shared__ int s_flag[3];
   const long long goal = *d.goal;
+  static_assert(INNER == 0 || LPI == 1, "the inner list is kept for one lane per particle");
+  constexpr bool inner = INNER != 0;
   for (int t = d.cta_start[blockIdx.x]; t < d.cta_start[blockIdx.x + 1]; t++) {
     const int bi = d.cta_boxes[t];
     if (threadIdx.x == 0) {
       s_flag[0] = (d.box_err[bi] == 0 && d.box_steps[bi] < goal) ? 1 : 0;
       s_flag[1] = d.box_rebuild[bi];
+      s_flag[2] = d.box_prune[bi];
     }
     __syncthreads();
     const int go = s_flag[0], rb = s_flag[1];
+    // this step re-selects the box's inner rows (after a rebuild, or when a
+    // particle moved half the buffer since the last selection)
+    const bool sel = rb != 0 || s_flag[2] != 0;
     __syncthreads();
     if (!go) continue;
     const BoxDesc b = d.boxes[bi];
@@ -441,11 +464,18 @@ __global__ void __launch_bounds__(512, MIXED ? MDG_BATCH_MIN_BLOCKS : 2) k_batch
     }
     const int o = b.atom_off, n = b.n;
     const int groups = blockDim.x / LPI, lane = threadIdx.x % LPI;
-    bool rebuild = false;
+    bool rebuild = false, reselect = false;
     // all lanes of a group stay together: loop bound rounded to whole groups
     for (int a0 = threadIdx.x / LPI; a0 < ((n + groups - 1) / groups) * groups; a0 += groups) {
       const int a = a0 < n ? a0 : n - 1;
-      const double3 F = box_force<MIXED, LPI>(P, d, b, a, lane, par);
+      double3 F;
+      int kept = 0;
+      if constexpr (INNER != 0) {
+        if (sel) F = box_force<MIXED, 1, 1>(P, d, b, a, lane, par, a0 < n, &kept);
+        else F = box_force<MIXED, 1, 2>(P, d, b, a, lane, par);
+      } else {
+        F = box_force<MIXED, LPI, 0>(P, d, b, a, lane, par);
+      }
       if (lane != 0 || a0 >= n) continue;
       double4_32a p = d.p[o + a];
       p.x += F.x * P.dt;
@@ -479,14 +509,31 @@ __global__ void __launch_bounds__(512, MIXED ? MDG_BATCH_MIN_BLOCKS : 2) k_batch
           rebuild = true;
       }
       const float4 lb = d.qf[o + a];
-      d.loc[par ^ 1][o + a] = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
+      const float4 ln = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
+      d.loc[par ^ 1][o + a] = ln;
+      if (inner) {
+        // inner-list reference: this force evaluation's positions when the
+        // rows were re-selected now, else those of the last selection
+        float4 lp;
+        if (sel) {
+          lp = d.loc[par][o + a];
+          d.loc_p[o + a] = lp;
+          d.pcount[o + a] = kept;
+        } else {
+          lp = d.loc_p[o + a];
+        }
+        const float vx = ln.x - lp.x, vy = ln.y - lp.y, vz = ln.z - lp.z;
+        if (vx * vx + vy * vy + vz * vz > P.half_prune2) reselect = true;
+      }
       d.p[o + a] = p;
       d.q_end[o + a] = qe;
       d.q_mid[par ^ 1][o + a] = q1;
     }
     const int any = __syncthreads_or(rebuild ? 1 : 0);
+    const int anyp = __syncthreads_or(reselect ? 1 : 0);
     if (threadIdx.x == 0) {
       if (any) d.box_rebuild[bi] = 1;
+      if (inner) d.box_prune[bi] = anyp;
       d.box_steps[bi] += 1;
     }
     __syncthreads();
@@ -562,6 +609,7 @@ struct mdg_batch {
   std::string err;
   int nbox = 0, total = 0, num_sms = 0;
   int threads = 256, lpi = 1, ctas_per_sm = 2;
+  int use_inner = 1;  // one lane per particle walks the inner list (when the buffer is > 0)
   cudaStream_t stream = nullptr;
   Params P;
   Dev d;
@@ -629,6 +677,9 @@ int assign(mdg_batch *b) {
   MDG_BCK(cudaMemcpy(b->d.cta_start, start.data(), (G + 1) * sizeof(int), cudaMemcpyHostToDevice));
   MDG_BCK(cudaMemcpy(b->d.cta_boxes, flat.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice));
   b->grid = G;
+  // the inner rows are kept only under one lane per particle: a new shape
+  // starts from a fresh selection
+  MDG_BCK(cudaMemset(b->d.box_prune, 1, b->nbox * sizeof(int)));
   drop_batch_graphs(b);
   return MDG_OK;
 }
@@ -641,7 +692,10 @@ int alloc_batch_list(mdg_batch *b, int cap) {
     off += (long long)bx.n * cap;
   }
   if (b->d.nl) cudaFree(b->d.nl);
+  if (b->d.pl) cudaFree(b->d.pl);
+  b->d.nl = b->d.pl = nullptr;
   MDG_BCK(balloc(&b->d.nl, (size_t)off));
+  if (b->P.inner) MDG_BCK(balloc(&b->d.pl, (size_t)off));
   b->P.list_cap = cap;
   MDG_BCK(cudaMemcpy(b->d.boxes, b->boxes.data(), b->nbox * sizeof(BoxDesc), cudaMemcpyHostToDevice));
   std::vector<int> ones(b->nbox, 1);
@@ -655,11 +709,14 @@ void launch_batch_step(mdg_batch *b, int par) {
   const bool mixed = b->prm.precision == MDG_MIXED;
   k_batch_prep<<<b->nbox, 256, 0, b->stream>>>(b->P, b->d, par);
   k_batch_list<<<(b->total + 127) / 128, 128, 0, b->stream>>>(b->P, b->d, b->total);
-#define MDG_BSTEP(M, L) k_batch_step<M, L><<<b->grid, T, 0, b->stream>>>(b->P, b->d, par)
+#define MDG_BSTEP(M, L, I) k_batch_step<M, L, I><<<b->grid, T, 0, b->stream>>>(b->P, b->d, par)
+  const bool inner = b->P.inner && b->lpi == 1 && b->use_inner;
   if (mixed) {
-    if (b->lpi == 4) MDG_BSTEP(1, 4); else if (b->lpi == 2) MDG_BSTEP(1, 2); else MDG_BSTEP(1, 1);
+    if (b->lpi == 4) MDG_BSTEP(1, 4, 0); else if (b->lpi == 2) MDG_BSTEP(1, 2, 0);
+    else if (inner) MDG_BSTEP(1, 1, 1); else MDG_BSTEP(1, 1, 0);
   } else {
-    if (b->lpi == 4) MDG_BSTEP(0, 4); else if (b->lpi == 2) MDG_BSTEP(0, 2); else MDG_BSTEP(0, 1);
+    if (b->lpi == 4) MDG_BSTEP(0, 4, 0); else if (b->lpi == 2) MDG_BSTEP(0, 2, 0);
+    else if (inner) MDG_BSTEP(0, 1, 1); else MDG_BSTEP(0, 1, 0);
   }
 #undef MDG_BSTEP
   b->launches += 3;
@@ -714,6 +771,7 @@ void mdg_batch_params_default(mdg_batch_params *p) {
   p->dt = 0.002;
   p->list_capacity = 0;
   p->use_graphs = 1;
+  p->prune_buffer = -1.0;
 }
 
 int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_per_box, const double *box_lengths,
@@ -785,6 +843,13 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
   P.dt2 = p->dt * 0.5;
   P.half_margin2 = 0.25 * p->margin * p->margin;
   P.nbox = nbox;
+  // inner-list buffer: negative = min(0.1, margin / 2), as the single-box form
+  const double buffer = p->prune_buffer < 0.0 ? std::fmin(0.1, 0.5 * p->margin) : p->prune_buffer;
+  P.inner = buffer > 0.0 ? 1 : 0;
+  const double rb = p->cutoff + buffer;
+  P.prune_thr2d = rb * rb;
+  P.prune_thr2f = (float)(rb * rb + 1e-4);  // float r2 of local positions is within ~1e-5
+  P.half_prune2 = (float)(0.25 * buffer * buffer * (1.0 - 1e-4));
   int cap = p->list_capacity > 0 ? p->list_capacity : (int)(max_rho * 4.18879020478639 * sl * sl * sl * 1.5 + 24);
   cap = (cap + 7) & ~7;
   cudaError_t e = cudaSetDevice(p->device);
@@ -811,6 +876,9 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
   if (e == cudaSuccess) e = balloc(&d.t_cell, n);
   if (e == cudaSuccess) e = balloc(&d.order, n);
   if (e == cudaSuccess) e = balloc(&d.ncount, n);
+  if (e == cudaSuccess) e = balloc(&d.pcount, n);
+  if (e == cudaSuccess) e = balloc(&d.loc_p, n);
+  if (e == cudaSuccess) e = balloc(&d.box_prune, nbox);
   if (e == cudaSuccess) e = balloc(&d.cell_start, (size_t)cells);
   if (e == cudaSuccess) e = balloc(&d.box_rebuild, nbox);
   if (e == cudaSuccess) e = balloc(&d.box_err, nbox);
@@ -844,6 +912,7 @@ int mdg_batch_destroy(mdg_batch *b) {
   Dev &d = b->d;
   void *ptrs[] = {d.boxes, d.cta_start, d.cta_boxes, d.q_end, d.q_mid[0], d.q_mid[1], d.p, d.q_build, d.t_q, d.t_p,
                   d.qf, d.loc[0], d.loc[1], d.id, d.cell, d.t_id, d.t_cell, d.order, d.cell_start, d.nl, d.ncount,
+                  d.pl, d.pcount, d.loc_p, d.box_prune,
                   d.box_rebuild, d.box_err, d.box_need, d.box_steps, d.box_rebuilds, d.goal, d.partials,
                   b->d_box_of_slot};
   for (void *p : ptrs)
@@ -972,42 +1041,63 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
   std::vector<long long> st0(b->nbox);
   MDG_BCK(cudaMemcpy(st0.data(), b->d.box_steps, b->nbox * sizeof(long long), cudaMemcpyDeviceToHost));
   const long long steps0 = b->steps;
-  const int T0 = b->threads, L0 = b->lpi, C0 = b->ctas_per_sm;
-  double best = 1e300;
-  int bt = T0, bl = L0, bc = C0;
+  // one trial: the shape from the saved state with fresh lists; *ms receives
+  // the device time of `steps` steps after the two that build the lists
+  auto trial = [&](int T, int Lp, int C, int I, int steps, double *ms) -> int {
+    b->threads = T;
+    b->lpi = Lp;
+    b->ctas_per_sm = C;
+    b->use_inner = I;
+    int rc = assign(b);
+    if (rc) return rc;
+    MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
+    MDG_BCK(cudaMemcpyAsync(b->d.p, sp, n * 32, cudaMemcpyDeviceToDevice, b->stream));
+    MDG_BCK(cudaMemcpyAsync(b->d.id, sid, n * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
+    std::vector<int> ones(b->nbox, 1);
+    MDG_BCK(cudaMemcpyAsync(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    MDG_BCK(cudaMemcpyAsync(b->d.box_steps, st0.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+    b->steps = steps0;
+    b->par = 0;
+    rc = mdg_batch_calculate(b, 2);  // builds lists
+    if (rc) return rc;
+    rc = mdg_batch_calculate(b, steps);
+    if (rc) return rc;
+    *ms = b->last_ms;
+    return MDG_OK;
+  };
   const int Ts[] = {128, 256, 512}, Ls[] = {1, 2, 4}, Cs[] = {1, 2, 3, 4};
+  double best = 1e300;
+  int bt = b->threads, bl = b->lpi, bc = b->ctas_per_sm, bi = 0;
   for (int T : Ts)
     for (int Lp : Ls)
       for (int C : Cs) {
         if (T * C > 2048) continue;
-        b->threads = T;
-        b->lpi = Lp;
-        b->ctas_per_sm = C;
-        int rc = assign(b);
+        double ms = 0.0;
+        int rc = trial(T, Lp, C, 0, trial_steps, &ms);
         if (rc) return rc;
-        // every trial starts from the saved state with fresh lists
-        MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
-        MDG_BCK(cudaMemcpyAsync(b->d.p, sp, n * 32, cudaMemcpyDeviceToDevice, b->stream));
-        MDG_BCK(cudaMemcpyAsync(b->d.id, sid, n * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
-        std::vector<int> ones(b->nbox, 1);
-        MDG_BCK(cudaMemcpyAsync(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
-        MDG_BCK(cudaMemcpyAsync(b->d.box_steps, st0.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
-        b->steps = steps0;
-        b->par = 0;
-        rc = mdg_batch_calculate(b, 2);  // builds lists
-        if (rc) return rc;
-        rc = mdg_batch_calculate(b, trial_steps);
-        if (rc) return rc;
-        if (b->last_ms < best) {
-          best = b->last_ms;
+        if (ms < best) {
+          best = ms;
           bt = T;
           bl = Lp;
           bc = C;
         }
       }
+  // the inner list (one lane per particle) on and off over longer trials: it
+  // pays when the boxes re-select their inner rows rarely (small steps,
+  // FP64), which short trials from fresh lists cannot show
+  if (bl == 1 && b->P.inner) {
+    const int longer = std::max((int)trial_steps, 60);
+    double off = 0.0, on = 0.0;
+    int rc = trial(bt, 1, bc, 0, longer, &off);
+    if (rc) return rc;
+    rc = trial(bt, 1, bc, 1, longer, &on);
+    if (rc) return rc;
+    bi = on < off ? 1 : 0;
+  }
   b->threads = bt;
   b->lpi = bl;
   b->ctas_per_sm = bc;
+  b->use_inner = bi;
   int rc = assign(b);
   if (rc) return rc;
   MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
@@ -1052,6 +1142,7 @@ int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s) {
   s->threads = b->threads;
   s->lanes_per_particle = b->lpi;
   s->ctas_per_sm = b->ctas_per_sm;
+  s->inner_list = (b->P.inner && b->lpi == 1 && b->use_inner) ? 1 : 0;
   s->elapsed_ms = b->last_ms;
   s->kernel_launches = b->launches;
   return MDG_OK;

@@ -87,3 +87,23 @@ def test_autotuner_restores_state():
     np.testing.assert_allclose(b.observe_raw(), _oracle_obs([(q, p, L) for (q, p), (_, _, L) in
                                                              zip([(x, y) for x, y in zip(before[0::2], before[1::2])],
                                                                  boxes)], 30), rtol=1e-10, atol=1e-10)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_inner_list_changes_nothing(precision):
+    # the inner rows keep the outer rows' order and drop only pairs beyond rc,
+    # whose terms are exactly zero: the trajectories agree bit for bit, also
+    # when a tiny buffer makes the boxes re-select every few steps
+    from mdacp_gb300.batch import Batch
+    boxes = _boxes(6, seed=13)
+    runs = []
+    for buf in (0.0, None, 0.02):
+        b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision=precision, prune_buffer=buf)
+        b.set_shape(256, 1, 2)
+        b.calculate(80)
+        st = b.stats()
+        assert st["inner_list"] == (0 if buf == 0.0 else 1)
+        runs.append([x.copy() for pair in b.state() for x in pair])
+    for other in runs[1:]:
+        for u, v in zip(runs[0], other):
+            assert np.array_equal(u, v)
