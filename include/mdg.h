@@ -5,7 +5,8 @@
  * periodic box (one MDACP unit spanning the whole system, as `mpirun -np 1`
  * with one OpenMP unit runs it); it owns all device memory and one CUDA
  * stream.  Every call returns MDG_OK (0) or an error code; mdg_last_error()
- * returns the message of the last failure on that handle.  A handle must be
+ * returns the message of the last failure on that handle, and
+ * mdg_last_error(NULL) why the calling thread's last mdg_create failed.  A handle must be
  * used by one host thread at a time.
  *
  * Particle arrays cross the boundary in the reference's layout: `double

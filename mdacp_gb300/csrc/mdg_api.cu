@@ -58,6 +58,14 @@ int fail(mdg_handle *h, int code, const std::string &msg) {
   return code;
 }
 
+// Why the calling thread's last mdg_create failed (mdg_last_error(NULL)).
+thread_local std::string t_create_err;
+
+int create_fail(int code, const std::string &msg) {
+  t_create_err = msg;
+  return code;
+}
+
 #define MDG_CK(call)                                                                                  \
   do {                                                                                                \
     cudaError_t e_ = (call);                                                                          \
@@ -451,20 +459,24 @@ void mdg_params_default(mdg_params *p) {
 }
 
 int mdg_create(const mdg_params *p, mdg_handle **out) {
-  if (!p || !out) return MDG_ERR_INVALID;
+  t_create_err.clear();
+  if (!p || !out) return create_fail(MDG_ERR_INVALID, "null parameters or output");
   *out = nullptr;
-  if (p->capacity <= 0 || p->capacity > mdg::kMaxParticles) return MDG_ERR_INVALID;
-  if (!(p->cutoff > 0.0) || !(p->margin >= 0.0) || !(p->dt > 0.0)) return MDG_ERR_INVALID;
-  if (p->precision != MDG_FP64 && p->precision != MDG_MIXED) return MDG_ERR_INVALID;
-  if (p->thermostat < MDG_NVE || p->thermostat > MDG_NOSEHOOVER) return MDG_ERR_INVALID;
+  if (p->capacity <= 0 || p->capacity > mdg::kMaxParticles)
+    return create_fail(MDG_ERR_INVALID, "capacity must be in 1 .. " + std::to_string(mdg::kMaxParticles));
+  if (!(p->cutoff > 0.0) || !(p->margin >= 0.0) || !(p->dt > 0.0))
+    return create_fail(MDG_ERR_INVALID, "cutoff and dt must be > 0, margin >= 0");
+  if (p->precision != MDG_FP64 && p->precision != MDG_MIXED) return create_fail(MDG_ERR_INVALID, "bad precision");
+  if (p->thermostat < MDG_NVE || p->thermostat > MDG_NOSEHOOVER) return create_fail(MDG_ERR_INVALID, "bad thermostat");
   mdg_handle *h = new mdg_handle();
   h->prm = *p;
   memset(&h->g, 0, sizeof(h->g));
   memset(&h->d, 0, sizeof(h->d));
   int rc = setup_geometry(h);
   if (rc) {
+    const std::string msg = h->err;
     delete h;
-    return rc;
+    return create_fail(rc, msg);
   }
   cudaError_t e = cudaSetDevice(p->device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, p->device);
@@ -515,8 +527,7 @@ int mdg_create(const mdg_params *p, mdg_handle **out) {
   if (e != cudaSuccess) {
     std::string msg = cudaGetErrorString(e);
     mdg_destroy(h);
-    fprintf(stderr, "mdg_create: %s\n", msg.c_str());
-    return MDG_ERR_CUDA;
+    return create_fail(MDG_ERR_CUDA, msg);
   }
   *out = h;
   return MDG_OK;
@@ -537,7 +548,10 @@ int mdg_destroy(mdg_handle *h) {
   return MDG_OK;
 }
 
-const char *mdg_last_error(const mdg_handle *h) { return h ? h->err.c_str() : "null handle"; }
+const char *mdg_last_error(const mdg_handle *h) {
+  if (h) return h->err.c_str();
+  return t_create_err.empty() ? "null handle" : t_create_err.c_str();
+}
 
 static int set_state_common(mdg_handle *h, int32_t n) {
   h->g.n = n;

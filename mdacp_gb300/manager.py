@@ -54,7 +54,7 @@ class MDManager:
         self.params = prm
         self.L = np.array(prm.box[:])
         h = ctypes.c_void_p()
-        native.check(self.lib.mdg_create(ctypes.byref(prm), ctypes.byref(h)))
+        native.check(self.lib.mdg_create(ctypes.byref(prm), ctypes.byref(h)), create=True)
         self._h = h
         self.n = 0
 

@@ -100,11 +100,13 @@ class MDGError(RuntimeError):
     pass
 
 
-def check(rc, handle=None):
+def check(rc, handle=None, create=False):
+    """Raises MDGError for a failed call, with the handle's message (or, for
+    create=True, the calling thread's last mdg_create failure)."""
     if rc != MDG_OK:
         msg = ERRORS.get(rc, "error %d" % rc)
-        if handle:
-            detail = load().mdg_last_error(handle)
+        if handle or create:
+            detail = load().mdg_last_error(handle if handle else None)
             if detail:
                 msg += ": " + detail.decode()
         raise MDGError(msg)

@@ -134,3 +134,25 @@ def test_capacity_limits():
         m.set_state(np.vstack([q, q[:1] + 0.5]), np.vstack([p, p[:1]]))
     m.set_state(q, p)
     m.calculate(3)
+
+
+def test_box_below_two_search_lengths_is_refused():
+    # the 27-cell stencil needs at least two cells per side (side > 2 (rc + margin))
+    from mdacp_gb300 import native
+    with pytest.raises(native.MDGError, match="twice the search length"):
+        _gpu(5.9, 10)
+    with pytest.raises(native.MDGError):
+        _gpu(np.array([12.0, 12.0, 6.0]), 10)
+    m = _gpu(6.2, 10)   # two cells per side: accepted
+    m.close()
+
+
+def test_empty_state_is_refused_and_the_handle_stays_usable():
+    from mdacp_gb300 import native
+    q, p, L = liquid_like(0.5, 4, seed=93)
+    m = _gpu(L, len(q))
+    with pytest.raises(native.MDGError):
+        m.set_state(np.zeros((0, 3)), np.zeros((0, 3)))
+    m.set_state(q, p)
+    m.calculate(5)
+    assert m.stats()["steps"] == 5
