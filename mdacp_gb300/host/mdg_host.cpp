@@ -96,7 +96,8 @@ MDManager::MDManager(const Parameter &param, int capacity) : sinfo_(param) {
   p.seed = (uint64_t)param.GetIntegerDef("Seed", 1);
   p.device = param.GetIntegerDef("GpuDevice", 0);
   const int rc = mdg_create(&p, &h_);
-  if (rc != MDG_OK) throw std::runtime_error("mdg_create failed (" + std::to_string(rc) + ")");
+  if (rc != MDG_OK)
+    throw std::runtime_error("mdg_create failed (" + std::to_string(rc) + "): " + mdg_last_error(nullptr));
 }
 
 MDManager::~MDManager() { mdg_destroy(h_); }
