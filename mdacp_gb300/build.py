@@ -14,6 +14,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmdg.so")
+# bounds-checked build (-DMDG_CHECK=1): the same sources, every gather and
+# scatter index of the single-box path checked on the device
+OBJ_CHECK = os.path.join(HERE, "_build_check")
+LIB_CHECK = os.path.join(HERE, "libmdg_check.so")
 SOURCES = ["mdg_cells.cu", "mdg_list.cu", "mdg_step.cu", "mdg_batch.cu", "mdg_api.cu", "mdg_adjoint.cu", "mdg_noalloc.cu",
            "mdg_io.cu", "mdg_init.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -38,13 +42,17 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    """Compiles and links libmdg.so if any source is newer; returns its path."""
-    os.makedirs(OBJ, exist_ok=True)
+def build(force=False, verbose=False, extra_flags=(), check=False):
+    """Compiles and links libmdg.so (libmdg_check.so with check=True) if any
+    source is newer; returns its path."""
+    obj_dir, lib_path = (OBJ_CHECK, LIB_CHECK) if check else (OBJ, LIB)
+    if check:
+        extra_flags = tuple(extra_flags) + ("-DMDG_CHECK=1",)
+    os.makedirs(obj_dir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "mdg.h"))
     srcs = [os.path.join(CSRC, s) for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
-    objs = [os.path.join(OBJ, os.path.basename(s).replace(".cu", ".o")) for s in srcs]
+    objs = [os.path.join(obj_dir, os.path.basename(s).replace(".cu", ".o")) for s in srcs]
     cc = nvcc()
 
     def compile_one(src, obj):
@@ -63,14 +71,14 @@ def build(force=False, verbose=False, extra_flags=()):
         for o in outs:
             if o:
                 sys.stderr.write(o)
-    if force or _stale(LIB, objs):
-        tmp = LIB + ".tmp%d" % os.getpid()
+    if force or _stale(lib_path, objs):
+        tmp = lib_path + ".tmp%d" % os.getpid()
         cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 HOST = os.path.join(HERE, "host")

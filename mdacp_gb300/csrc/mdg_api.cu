@@ -224,6 +224,11 @@ int halt_error(mdg_handle *h) {
   cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.nrank * sizeof(int), h->stream);
   cudaStreamSynchronize(h->stream);
   char buf[160];
+  if (h->hflags->halt == mdg::kHaltCheck) {
+    snprintf(buf, sizeof buf, "bounds check failed (site %d, index %d)", h->hflags->check_site,
+             h->hflags->bad_slot);
+    return fail(h, MDG_ERR_STATE, buf);
+  }
   snprintf(buf, sizeof buf, "particle coordinate non-finite or outside the box at a rebuild (slot %d)",
            h->hflags->bad_slot);
   return fail(h, MDG_ERR_STATE, buf);

@@ -160,7 +160,8 @@ __global__ void k_scatter(Geom g, Dev d) {
     int cx, cy, cz;
     cell_unkey(d.cell[i], cx, cy, cz);
     const int c = cell_rank(g, cx, cy, cz);
-    d.order[d.cell_start[c] + atomicAdd(&d.cell_fill[c], 1)] = i;
+    const int dst = d.cell_start[c] + atomicAdd(&d.cell_fill[c], 1);
+    if (MDG_IN_RANGE(d.flags, kCheckScatter, dst, g.n)) d.order[dst] = i;
   }
 }
 

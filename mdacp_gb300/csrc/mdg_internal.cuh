@@ -45,6 +45,7 @@ __device__ __forceinline__ int entry_sz(uint32_t e) { return (int)((e >> 4) & 3u
 // halt codes
 constexpr int kHaltOverflow = 1;
 constexpr int kHaltBadState = 2;
+constexpr int kHaltCheck = 3;  // checked builds: a bounds check failed
 
 struct DevFlags {
   int rebuild;                  // rebuild the list at the start of the next step
@@ -56,7 +57,7 @@ struct DevFlags {
   unsigned long long rebuilds;  // completed list builds
   unsigned long long pairs;     // directed pairs at the last build
   int bad_slot;
-  int pad0;
+  int check_site;               // checked builds: which bounds check failed
   double zeta;                  // Nose-Hoover zeta (Variables::Zeta) after the last step
   double zeta_a;                // zeta after the first update of the coming step
   double exp1;                  // exp(-dt/2 * zeta_a)
@@ -197,5 +198,34 @@ __device__ __forceinline__ float step_float(uint32_t e, uint32_t mask, float bia
 
 // device helpers
 __device__ __forceinline__ void halt_with(DevFlags *f, int code) { atomicCAS(&f->halt, 0, code); }
+
+// Checked builds (-DMDG_CHECK=1, libmdg_check.so): index checks on the
+// gathers and scatters of the single-box path.  A failed check stops the run
+// like any other halt (every later kernel is a no-op), records the site and
+// the index, and the access is skipped; nothing traps.  Sites:
+enum CheckSite {
+  kCheckStepSlot = 1,    // step / force: list entry slot >= n
+  kCheckStepRow = 2,     // step / force: row length > list capacity
+  kCheckBuildCell = 3,   // list build: stencil cell rank >= cell count
+  kCheckBuildRange = 4,  // list build: a cell's slot range outside 0..n
+  kCheckScatter = 5,     // binning: destination slot >= n
+  kCheckObserve = 6,     // observers: list entry slot >= n
+};
+#ifndef MDG_CHECK
+#define MDG_CHECK 0
+#endif
+constexpr bool kCheck = MDG_CHECK != 0;
+
+__device__ __noinline__ inline bool check_failed(DevFlags *f, int site, long long index) {
+  if (atomicCAS(&f->halt, 0, kHaltCheck) == 0) {
+    f->check_site = site;
+    f->bad_slot = index > 0x7fffffffLL ? 0x7fffffff : (int)index;
+  }
+  return false;
+}
+// true when 0 <= v < n (always in unchecked builds)
+#define MDG_IN_RANGE(flags, site, v, n) \
+  (!mdg::kCheck || (unsigned long long)(long long)(v) < (unsigned long long)(long long)(n) || \
+   mdg::check_failed((flags), (site), (long long)(v)))
 
 }  // namespace mdg

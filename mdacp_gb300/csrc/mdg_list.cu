@@ -77,7 +77,9 @@ __global__ void __launch_bounds__(kListThreads, MDG_LIST_MIN_BLOCKS) k_build_lis
           if (nx < 0) { nx += g.nc[0]; sx = -1; } else if (nx >= g.nc[0]) { nx -= g.nc[0]; sx = 1; }
           const float fx = (float)ox * g.w32[0] + (float)sx * g.dl32[0] - fi.x;
           const int cc = cell_rank(g, nx, ny, nz);
-          const int a = d.cell_start[cc], b = d.cell_start[cc + 1];
+          if (!MDG_IN_RANGE(f, kCheckBuildCell, cc, g.nrank)) continue;
+          int a = d.cell_start[cc], b = d.cell_start[cc + 1];
+          if (!MDG_IN_RANGE(f, kCheckBuildRange, b, g.n + 1) || !MDG_IN_RANGE(f, kCheckBuildRange, a, b + 1)) a = b = 0;
           const uint32_t code = entry_pack(0, ox, oy, oz);
           for (int j0 = a; j0 < b; j0 += kListUnroll) {
             float4 fj[kListUnroll];

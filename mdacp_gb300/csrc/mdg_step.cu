@@ -119,13 +119,15 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
                                               const CellPos &cp, const uint32_t *__restrict__ list,
                                               const int *__restrict__ counts, int *kept) {
   const double4_32a qi = pos[i];
-  const int cnt = counts[i];
+  int cnt = counts[i];
+  if (!MDG_IN_RANGE(d.flags, kCheckStepRow, cnt, g.list_cap + 1)) cnt = 0;
   const uint32_t *row = list + i;
   const double thr = (double)g.prune_thr2;
   int m = 0;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int k = 0; k < cnt; k++) {
     const uint32_t e = __ldg(row + (size_t)k * g.stride);
+    if (!MDG_IN_RANGE(d.flags, kCheckStepSlot, entry_slot(e), g.n)) continue;
     double4_32a qj = ldg4(pos + entry_slot(e));
     if (cp.edge) apply_image(g, cp, e, qj);
     const double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
@@ -155,10 +157,18 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
   const AxisQuad qx = axis_quad(g.w32[0], g.dl32[0], cp.cx == 0, cp.cx == g.nc[0] - 1, li.x, 1.0f);
   const AxisQuad qy = axis_quad(g.w32[1], g.dl32[1], cp.cy == 0, cp.cy == g.nc[1] - 1, li.y, 0.25f);
   const AxisQuad qz = axis_quad(g.w32[2], g.dl32[2], cp.cz == 0, cp.cz == g.nc[2] - 1, li.z, 0.0625f);
-  const int cnt = counts[i];
+  int cnt = counts[i];
+  if (!MDG_IN_RANGE(d.flags, kCheckStepRow, cnt, g.list_cap + 1)) cnt = 0;
   const uint32_t *row = list + i;
   const size_t stride = (size_t)g.stride;
   float sx = 0.f, sy = 0.f, sz = 0.f;
+  // a partner position (a far one, contributing nothing, for an entry a
+  // checked build rejects)
+  auto gather = [&](uint32_t e) -> float4 {
+    const int j = entry_slot(e);
+    if (!MDG_IN_RANGE(d.flags, kCheckStepSlot, j, g.n)) return make_float4(1e30f, 1e30f, 1e30f, 0.f);
+    return __ldg(loc + j);
+  };
   const float rc2 = g.rc2f, c2x8 = g.c2x8f, thr = g.prune_thr2;
   int m = 0;
   auto pair = [&](uint32_t e, const float4 &lj) {
@@ -195,7 +205,7 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) e[u] = en[u];
 #pragma unroll
-    for (int u = 0; u < kUnroll; u++) l[u] = __ldg(loc + entry_slot(e[u]));
+    for (int u = 0; u < kUnroll; u++) l[u] = gather(e[u]);
 #pragma unroll
     for (int u = 0; u < kUnroll; u++) {
       const int kn = k + kUnroll + u;
@@ -218,7 +228,7 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
     float4 l[kTail];
 #pragma unroll
     for (int u = 0; u < kTail; u++)
-      l[u] = k + u < cnt ? __ldg(loc + entry_slot(en[u])) : make_float4(1e30f, 1e30f, 1e30f, 0.f);
+      l[u] = k + u < cnt ? gather(en[u]) : make_float4(1e30f, 1e30f, 1e30f, 0.f);
 #pragma unroll
     for (int u = 0; u < kTail; u++) pair(en[u], l[u]);
   }
@@ -432,6 +442,7 @@ __global__ void __launch_bounds__(kStepThreads) k_observe(Geom g, Dev d) {
     const int cnt = d.ncount[i];
     for (int k = 0; k < cnt; k++) {
       const uint32_t e = d.nl[(size_t)k * g.stride + i];
+      if (!MDG_IN_RANGE(d.flags, kCheckObserve, entry_slot(e), g.n)) continue;
       double4_32a qj = d.q_end[entry_slot(e)];
       if (cp.edge) apply_image(g, cp, e, qj);
       const double dx = __dsub_rn(qi.x, qj.x), dy = __dsub_rn(qi.y, qj.y), dz = __dsub_rn(qi.z, qj.z);
@@ -476,6 +487,7 @@ __global__ void __launch_bounds__(kStepThreads) k_observe_mixed(Geom g, Dev d, c
     const int cnt = d.ncount[i];
     for (int k = 0; k < cnt; k++) {
       const uint32_t e = __ldg(d.nl + (size_t)k * g.stride + i);
+      if (!MDG_IN_RANGE(d.flags, kCheckObserve, entry_slot(e), g.n)) continue;
       const float4 lj = __ldg(loc + entry_slot(e));
       const float tx = step_float(e, 0x03u, 8388609.0f), ty = step_float(e, 0x0Cu, 8388612.0f),
                   tz = step_float(e, 0x30u, 8388624.0f);

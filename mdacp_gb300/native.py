@@ -9,6 +9,7 @@ import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmdg.so")
+CHECK_LIB_PATH = os.path.join(HERE, "libmdg_check.so")
 
 MDG_OK = 0
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "capacity", 4: "bad particle state", 5: "no state"}
@@ -79,11 +80,14 @@ _lib = None
 
 
 def load(path=None):
-    """Loads libmdg.so and declares every entry point; raises if it is missing."""
+    """Loads libmdg.so and declares every entry point; raises if it is missing.
+
+    MDG_LIBRARY=check selects the bounds-checked build (libmdg_check.so, made
+    by build.build(check=True)) for the whole process."""
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = path or LIB_PATH
+    p = path or (CHECK_LIB_PATH if os.environ.get("MDG_LIBRARY") == "check" else LIB_PATH)
     if not os.path.exists(p):
         raise RuntimeError("libmdg.so not built (%s); run __graft_entry__.build()" % p)
     lib = ctypes.CDLL(p)
