@@ -405,8 +405,10 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
       }
       const double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
       const double r2 = dx * dx + dy * dy + dz * dz;
-      if (MODE == 1 && select && r2 <= P.prune_thr2d) prow[(long long)(m++) * n] = e;
-      if (r2 <= P.rc2) {
+      // bit-pattern comparisons of r2 >= +0: the integer pipe, not the FP64 one
+      const long long r2_bits = __double_as_longlong(r2);
+      if (MODE == 1 && select && r2_bits <= __double_as_longlong(P.prune_thr2d)) prow[(long long)(m++) * n] = e;
+      if (r2_bits <= __double_as_longlong(P.rc2)) {
         const double inv = rcp_hh3(r2);
         const double i6 = inv * inv * inv;
         const double df = (i6 * inv) * fma(-48.0, i6, 24.0) + P.c2x8;

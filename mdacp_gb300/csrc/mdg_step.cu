@@ -123,6 +123,10 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
   if (!MDG_IN_RANGE(d.flags, kCheckStepRow, cnt, g.list_cap + 1)) cnt = 0;
   const uint32_t *row = list + i;
   const double thr = (double)g.prune_thr2;
+  // r2 >= +0, so its bit pattern orders like the value (a NaN compares above
+  // every finite bound): the cutoff tests run on the integer pipe instead of
+  // the FP64 pipe (1/64 of the FP32 rate; 6 % of the FP64 step at 4M atoms)
+  const long long rc2_bits = __double_as_longlong(g.rc2), thr_bits = __double_as_longlong(thr);
   int m = 0;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   for (int k = 0; k < cnt; k++) {
@@ -132,8 +136,8 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
     if (cp.edge) apply_image(g, cp, e, qj);
     const double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
     const double r2 = dx * dx + dy * dy + dz * dz;
-    if (PRUNE && r2 <= thr) d.pl[(size_t)(m++) * g.stride + i] = e;
-    if (r2 <= g.rc2) {
+    if (PRUNE && __double_as_longlong(r2) <= thr_bits) d.pl[(size_t)(m++) * g.stride + i] = e;
+    if (__double_as_longlong(r2) <= rc2_bits) {
       const double inv = rcp_hh3(r2);
       const double i6 = inv * inv * inv;
       const double df = (i6 * inv) * fma(-48.0, i6, 24.0) + g.c2x8;
