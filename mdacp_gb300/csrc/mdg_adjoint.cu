@@ -70,6 +70,7 @@ struct D {
   double *part;              // block partials
   double *acc;               // running sums: J, g_eps, g_sig
   int *flag;
+  unsigned int *done;        // blocks of the current reduction that wrote their partials
 };
 
 __device__ __forceinline__ void min_image(const P &c, double &dx, double &dy, double &dz) {
@@ -101,7 +102,8 @@ struct PairTerms {
 
 __device__ __forceinline__ bool pair_terms(const P &c, double r2, PairTerms &t) {
   const double x2 = r2 * c.inv_s2;
-  if (x2 > c.xc2) return false;
+  // x2 >= +0: compared as bit patterns, on the integer pipe (same order)
+  if (__double_as_longlong(x2) > __double_as_longlong(c.xc2)) return false;
   const double ix2 = recip(x2), ix6 = ix2 * ix2 * ix2, ix8 = ix6 * ix2, ix12 = ix6 * ix6, ix14 = ix12 * ix2;
   const double ix10 = ix8 * ix2, ix16 = ix14 * ix2;
   // psi(x) = phi'(x)/x, chi(x) = x^2 psi(x)
@@ -133,6 +135,37 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   return t;
 }
 
+// Writes this block's three partials; the last block of the grid to do so
+// adds w times their sums (blocks in a fixed order, so the result does not
+// depend on which block finished last) to acc[0..2] and rearms the counter.
+// No block waits for another.
+__device__ void partials_accumulate(const D &d, double A, double B, double E, double w) {
+  __shared__ int last;
+  __shared__ double sh2[32];
+  if (threadIdx.x == 0) {
+    d.part[3 * blockIdx.x + 0] = A;
+    d.part[3 * blockIdx.x + 1] = B;
+    d.part[3 * blockIdx.x + 2] = E;
+    __threadfence();
+    last = atomicAdd(d.done, 1u) == gridDim.x - 1 ? 1 : 0;
+  }
+  __syncthreads();
+  if (!last) return;
+  double a = 0, b = 0, e = 0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+    a += __ldcg(d.part + 3 * k);
+    b += __ldcg(d.part + 3 * k + 1);
+    e += __ldcg(d.part + 3 * k + 2);
+  }
+  const double ta = block_sum(a, sh2), tb = block_sum(b, sh2), te = block_sum(e, sh2);
+  if (threadIdx.x == 0) {
+    d.acc[0] += w * ta;
+    d.acc[1] += w * tb;
+    d.acc[2] += w * te;
+    *d.done = 0;
+  }
+}
+
 // Sum over the kLanes lanes that share a particle (all lanes hold the total).
 __device__ __forceinline__ double lane_sum(double v) {
 #pragma unroll
@@ -141,58 +174,74 @@ __device__ __forceinline__ double lane_sum(double v) {
 }
 
 // Pair list at positions q: every partner within the list radius, minimum
-// image, ascending j.  The test runs in float on block-wide tiles of
-// positions against a radius widened by 1e-3 (float positions of a box of
-// tens of sigma are within 1e-5), so every pair within the exact radius is
-// listed; a few more do no harm (the pair terms cut at rc).
+// image.  kLanes lanes share a particle: lane l tests partners j = l, l +
+// kLanes, ... (a particle's lanes read neighbouring positions together), first
+// counting, then writing at its offset in the row (a prefix sum over the
+// lanes), so the row order is fixed: lane 0's partners, then lane 1's, ...
+// The test runs in float against a radius widened by 1e-3 (float positions of
+// a box of tens of sigma are within 1e-5), so every pair within the exact
+// radius is listed; a few more do no harm (the pair terms cut at rc).
 __global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
-  __shared__ float4 tile[kT];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  float4 qi = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (i < c.n) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tid / kLanes, lane = tid % kLanes;
+  const bool active = i < c.n;
+  float qx = 0.f, qy = 0.f, qz = 0.f;
+  if (active) {
     const double4_32a v = q[i];
-    qi = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+    qx = (float)v.x;
+    qy = (float)v.y;
+    qz = (float)v.z;
   }
   const float lx = (float)c.L[0], ly = (float)c.L[1], lz = (float)c.L[2];
   const float ilx = (float)c.inv_L[0], ily = (float)c.inv_L[1], ilz = (float)c.inv_L[2];
   const float sl2f = (float)c.sl2f;
+  auto within = [&](int j) {
+    const double4_32a v = q[j];
+    float dx = (float)v.x - qx, dy = (float)v.y - qy, dz = (float)v.z - qz;
+    dx -= lx * rintf(dx * ilx);
+    dy -= ly * rintf(dy * ily);
+    dz -= lz * rintf(dz * ilz);
+    return dx * dx + dy * dy + dz * dz <= sl2f && j != i;
+  };
   int m = 0;
-  for (int base = 0; base < c.n; base += kT) {
-    const int jl = base + threadIdx.x;
-    if (jl < c.n) {
-      const double4_32a v = q[jl];
-      tile[threadIdx.x] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
-    }
-    __syncthreads();
-    const int lim = min(kT, c.n - base);
-    if (i < c.n) {
-      for (int t = 0; t < lim; t++) {
-        const float4 qj = tile[t];
-        float dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-        dx -= lx * rintf(dx * ilx);
-        dy -= ly * rintf(dy * ily);
-        dz -= lz * rintf(dz * ilz);
-        const int j = base + t;
-        if (dx * dx + dy * dy + dz * dz <= sl2f && j != i) {
-          if (m < c.cap) d.nbr[(size_t)i * c.cap + m] = j;
-          m++;
-        }
-      }
-    }
-    __syncthreads();
+  if (active)
+    for (int j = lane; j < c.n; j += kLanes) m += within(j) ? 1 : 0;
+  // offsets of the lanes' partners in the row
+  int incl = m;
+#pragma unroll
+  for (int o = 1; o < kLanes; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o, kLanes);
+    if (lane >= o) incl += v;
   }
-  if (i < c.n) {
-    d.cnt[i] = m < c.cap ? m : c.cap;
-    if (m > c.cap) atomicMax(d.flag, m);
+  const int total = __shfl_sync(0xffffffffu, incl, kLanes - 1, kLanes);
+  if (active) {
+    int w = incl - m;
+    int *row = d.nbr + (size_t)i * c.cap;
+    for (int j = lane; j < c.n; j += kLanes)
+      if (within(j)) {
+        if (w < c.cap) row[w] = j;
+        w++;
+      }
+    if (lane == 0) {
+      d.cnt[i] = total < c.cap ? total : c.cap;
+      if (total > c.cap) atomicMax(d.flag, total);
+    }
   }
 }
 
+// Forces at the half-step positions q; also the segment's displacement check
+// (a particle more than margin/2 from where the segment's list was built).
 __global__ void k_force(P c, D d, const double4_32a *q, double4_32a *F) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
   double fx = 0, fy = 0, fz = 0;
   if (i < c.n) {
     const double4_32a qi = q[i];
+    if (lane == 0) {
+      const double4_32a z = d.q0[i];
+      const double ux = qi.x - z.x, uy = qi.y - z.y, uz = qi.z - z.z;
+      if (ux * ux + uy * uy + uz * uz > c.half_margin2) atomicMax(d.flag + 1, 1);
+    }
     for (int k = lane; k < d.cnt[i]; k += kLanes) {
       const double4_32a qj = q[d.nbr[(size_t)i * c.cap + k]];
       double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
@@ -210,8 +259,8 @@ __global__ void k_force(P c, D d, const double4_32a *q, double4_32a *F) {
   if (i < c.n && lane == 0) F[i] = make_double4_32a(fx, fy, fz, 0.0);
 }
 
-// qh = q + p dt/2 (also records the displacement check against q0)
-__global__ void k_drift(P c, D d, const double4_32a *q, const double4_32a *p, double4_32a *out) {
+// qh = q + p dt/2: the first half-drift of a trajectory or segment
+__global__ void k_drift(P c, const double4_32a *q, const double4_32a *p, double4_32a *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
   double4_32a a = q[i];
@@ -220,31 +269,43 @@ __global__ void k_drift(P c, D d, const double4_32a *q, const double4_32a *p, do
   a.y += b.y * c.dt2;
   a.z += b.z * c.dt2;
   out[i] = a;
-  const double4_32a z = d.q0[i];
-  const double ux = a.x - z.x, uy = a.y - z.y, uz = a.z - z.z;
-  if (ux * ux + uy * uy + uz * uz > c.half_margin2) atomicMax(d.flag + 1, 1);
 }
 
-// p += F dt; q = qh + p dt/2
-__global__ void k_kick_drift(P c, const double4_32a *qh, const double4_32a *F, double4_32a *q, double4_32a *p) {
+// p_out = p_in + F dt; q_out = qh + p_out dt/2; and, when qh_next is given,
+// the next step's first half-drift qh_next = q_out + p_out dt/2 (the same
+// operations k_drift performs).  Out of place, so a recomputed segment writes
+// step k from step k - 1 without copies; qh_next may alias qh.
+__global__ void k_kick_drift(P c, const double4_32a *qh, const double4_32a *F, const double4_32a *p_in,
+                             double4_32a *q_out, double4_32a *p_out, double4_32a *qh_next) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= c.n) return;
-  double4_32a b = p[i];
+  double4_32a b = p_in[i];
   const double4_32a f = F[i];
   b.x += f.x * c.dt;
   b.y += f.y * c.dt;
   b.z += f.z * c.dt;
-  p[i] = b;
+  p_out[i] = b;
   double4_32a a = qh[i];
   a.x += b.x * c.dt2;
   a.y += b.y * c.dt2;
   a.z += b.z * c.dt2;
-  q[i] = a;
+  q_out[i] = a;
+  if (qh_next) {
+    a.x += b.x * c.dt2;
+    a.y += b.y * c.dt2;
+    a.z += b.z * c.dt2;
+    qh_next[i] = a;
+  }
 }
 
-// Objective j at (q, p) into partials (value, d/deps, d/dsigma); with grad,
-// also adds w * dj/dq to aq and w * dj/dp to ap (w = 1/Ns).
-__global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p, int grad, double w) {
+// Objective j at (q, p) into partials (value, d/deps, d/dsigma); with GRAD,
+// also adds w * dj/dq to aq and w * dj/dp to ap (w = 1/Ns).  OBJ and GRAD are
+// template parameters so that each pass computes only the pair terms it uses
+// (the forward pass of the potential-energy objective needs phi and its sigma
+// derivative alone).
+template <int OBJ, int GRAD>
+__global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p, double w) {
+  constexpr bool grad = GRAD != 0;
   __shared__ double sh[32];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
@@ -258,25 +319,31 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
       min_image(c, dx, dy, dz);
       PairTerms t;
       if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
-      if (c.objective == 0) {
+      if (OBJ == 0) {
         u += 0.5 * t.phi;
         us += 0.5 * t.dphis;
-        gx -= t.f * dx;  // dU/dq_i = -F_i
-        gy -= t.f * dy;
-        gz -= t.f * dz;
+        if (grad) {
+          gx -= t.f * dx;  // dU/dq_i = -F_i
+          gy -= t.f * dy;
+          gz -= t.f * dz;
+        }
       } else {
         G += 0.5 * t.g;
         Gs += 0.5 * t.gs;
-        gx += t.gpr * dx;  // dG/dq_i = -sum g'(r) d/r;  dP/dq_i = -(1/3V) dG/dq_i
-        gy += t.gpr * dy;
-        gz += t.gpr * dz;
+        if (grad) {
+          gx += t.gpr * dx;  // dG/dq_i = -sum g'(r) d/r;  dP/dq_i = -(1/3V) dG/dq_i
+          gy += t.gpr * dy;
+          gz += t.gpr * dz;
+        }
       }
     }
   }
-  gx = lane_sum(gx);
-  gy = lane_sum(gy);
-  gz = lane_sum(gz);
-  if (c.objective == 0) {
+  if (grad) {
+    gx = lane_sum(gx);
+    gy = lane_sum(gy);
+    gz = lane_sum(gz);
+  }
+  if (OBJ == 0) {
     u = lane_sum(u);
     us = lane_sum(us);
   } else {
@@ -286,7 +353,7 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
   if (i < c.n && lane == 0) {
     const double4_32a pi = p[i];
     const double ke = 0.5 * (pi.x * pi.x + pi.y * pi.y + pi.z * pi.z);
-    if (c.objective == 0) {
+    if (OBJ == 0) {
       const double inv_n = 1.0 / (double)c.n;
       val = u * inv_n;
       ge = u / c.eps * inv_n;
@@ -317,28 +384,7 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
     }
   }
   const double A = block_sum(val, sh), B = block_sum(ge, sh), E = block_sum(gs, sh);
-  if (threadIdx.x == 0) {
-    d.part[3 * blockIdx.x + 0] = A;
-    d.part[3 * blockIdx.x + 1] = B;
-    d.part[3 * blockIdx.x + 2] = E;
-  }
-}
-
-// acc[0..2] += w * (sum of partials), fixed order.
-__global__ void k_accumulate(D d, int nparts, double w) {
-  __shared__ double sh[32];
-  double a = 0, b = 0, e = 0;
-  for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
-    a += d.part[3 * k];
-    b += d.part[3 * k + 1];
-    e += d.part[3 * k + 2];
-  }
-  const double ta = block_sum(a, sh), tb = block_sum(b, sh), te = block_sum(e, sh);
-  if (threadIdx.x == 0) {
-    d.acc[0] += w * ta;
-    d.acc[1] += w * tb;
-    d.acc[2] += w * te;
-  }
+  partials_accumulate(d, A, B, E, w);
 }
 
 // Reverse of one step at half-step positions qh.  In: aq, ap adjoints of
@@ -406,12 +452,8 @@ __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
     d.aq[i] = a;
     d.ap[i] = pb;
   }
-  const double A = block_sum(0.0, sh), B = block_sum(te, sh), E = block_sum(ts, sh);
-  if (threadIdx.x == 0) {
-    d.part[3 * blockIdx.x + 0] = A;
-    d.part[3 * blockIdx.x + 1] = B;
-    d.part[3 * blockIdx.x + 2] = E;
-  }
+  const double B = block_sum(te, sh), E = block_sum(ts, sh);
+  partials_accumulate(d, 0.0, B, E, 1.0);
 }
 
 }  // namespace adj
@@ -453,11 +495,20 @@ cudaError_t aalloc(T **p, size_t n) {
   return cudaMalloc((void **)p, (n ? n : 1) * sizeof(T));
 }
 
-// One forward step from (q, p): qh_out, then (q, p) updated in place.
-void fwd_step(mdg_adjoint *a, double4_32a *q, double4_32a *p, double4_32a *qh) {
-  k_drift<<<a->grid, kT, 0, a->s>>>(a->c, a->d, q, p, qh);
+void launch_objective(mdg_adjoint *a, const double4_32a *q, const double4_32a *p, bool grad, double w) {
+  const int obj = a->c.objective;
+  if (obj == 0 && !grad) k_objective<0, 0><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w);
+  else if (obj == 0) k_objective<0, 1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w);
+  else if (!grad) k_objective<1, 0><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w);
+  else k_objective<1, 1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w);
+}
+
+// One step from the half-step positions qh (already drifted from step k - 1)
+// and p_in: forces, then q_out, p_out and, when given, the next step's qh.
+void fwd_step(mdg_adjoint *a, const double4_32a *qh, const double4_32a *p_in, double4_32a *q_out,
+              double4_32a *p_out, double4_32a *qh_next) {
   k_force<<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, a->d.F);
-  k_kick_drift<<<a->grid, kT, 0, a->s>>>(a->c, qh, a->d.F, q, p);
+  k_kick_drift<<<a->grid, kT, 0, a->s>>>(a->c, qh, a->d.F, p_in, q_out, p_out, qh_next);
 }
 
 // The horizon from the state in d.q, d.p: per segment its list, per step the
@@ -471,14 +522,14 @@ int enqueue_forward(mdg_adjoint *a) {
   const double w = 1.0 / Ns;
   MDG_ACK(cudaMemcpyAsync(d.ckq, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
   MDG_ACK(cudaMemcpyAsync(d.ckp, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
+  k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.p, d.qh);
   for (int n = 1; n <= Ns; n++) {
     if ((n - 1) % K == 0) {  // a checkpoint segment starts: its own list
       MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
-      k_build<<<a->grid, kT, 0, a->s>>>(a->c, d, d.q);
+      k_build<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.q);
     }
-    fwd_step(a, d.q, d.p, d.qh);
-    k_objective<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.q, d.p, 0, w);
-    k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, w);
+    fwd_step(a, d.qh, d.p, d.q, d.p, n < Ns ? d.qh : nullptr);
+    launch_objective(a, d.q, d.p, false, w);
     if (n % K == 0) {
       MDG_ACK(cudaMemcpyAsync(d.ckq + N * (n / K), d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
       MDG_ACK(cudaMemcpyAsync(d.ckp + N * (n / K), d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
@@ -505,20 +556,17 @@ int enqueue_backward(mdg_adjoint *a) {
     MDG_ACK(cudaMemcpyAsync(d.segp, d.ckp + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
     // the segment's list, built from the same state as in the forward pass
     MDG_ACK(cudaMemcpyAsync(d.q0, d.segq, bytes, cudaMemcpyDeviceToDevice, a->s));
-    k_build<<<a->grid, kT, 0, a->s>>>(a->c, d, d.segq);
-    for (int k = 1; k <= len; k++) {
-      MDG_ACK(cudaMemcpyAsync(d.segq + N * k, d.segq + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
-      MDG_ACK(cudaMemcpyAsync(d.segp + N * k, d.segp + N * (k - 1), bytes, cudaMemcpyDeviceToDevice, a->s));
-      fwd_step(a, d.segq + N * k, d.segp + N * k, d.segqh + N * k);
-    }
+    k_build<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segq);
+    k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.segq, d.segp, d.segqh + N);
+    for (int k = 1; k <= len; k++)
+      fwd_step(a, d.segqh + N * k, d.segp + N * (k - 1), d.segq + N * k, d.segp + N * k,
+               k < len ? d.segqh + N * (k + 1) : nullptr);
     for (int k = len; k >= 1; k--) {
       // objective terms of state (seg_start + k)
-      k_objective<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segq + N * k, d.segp + N * k, 1, w);
-      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, w);
+      launch_objective(a, d.segq + N * k, d.segp + N * k, true, w);
       // reverse the step that produced it
       k_reverse<<<a->grid, kT, 0, a->s>>>(a->c, d);
       k_reverse_hvp<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segqh + N * k);
-      k_accumulate<<<1, 1024, 0, a->s>>>(d, a->gridp, 1.0);
     }
     seg_end = seg_start;
   }
@@ -619,6 +667,8 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   if (e == cudaSuccess) e = aalloc(&d.part, 3 * (size_t)a->gridp);
   if (e == cudaSuccess) e = aalloc(&d.acc, 3);
   if (e == cudaSuccess) e = aalloc(&d.flag, 2);
+  if (e == cudaSuccess) e = aalloc(&d.done, 1);
+  if (e == cudaSuccess) e = cudaMemset(d.done, 0, sizeof(unsigned int));
   if (e != cudaSuccess) {
     fprintf(stderr, "mdg_adjoint_create: %s\n", cudaGetErrorString(e));
     mdg_adjoint_destroy(a);
@@ -636,7 +686,7 @@ int mdg_adjoint_destroy(mdg_adjoint *a) {
   if (a->gx_backward) cudaGraphExecDestroy(a->gx_backward);
   D &d = a->d;
   void *ptrs[] = {d.q, d.p, d.qh, d.F, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
-                  d.nbr, d.cnt, d.part, d.acc, d.flag};
+                  d.nbr, d.cnt, d.part, d.acc, d.flag, d.done};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (a->s) cudaStreamDestroy(a->s);
