@@ -1,5 +1,5 @@
 // C ABI of libmdg.so (include/mdg.h): handle life cycle, state exchange and
-// the step driver that stands in for MDManager::Calculate.
+// the step sequencing that stands in for MDManager::Calculate.
 //
 // A step is enqueued as the rebuild sequence (a no-op unless the device flag
 // says the list expired) followed by the fused step kernel.  Steps are

@@ -8,7 +8,7 @@
 //                 lines through an ostream with default formatting;
 //   configuration Variables::SaveConfiguration (variables.cc:45-56): "qx qy qz
 //                 px py pz" lines (the reference also writes its ghost copies,
-//                 which this build does not have: real particles only);
+//                 which the engine does not keep: real particles only);
 //   stream        Variables::SaveToStream (variables.cc:111-118): per particle,
 //                 for d = 0..3, q[d] then p[d]; Variables::LoadFromStream
 //                 (variables.cc:121-131) reads an int particle count, the

@@ -2,7 +2,7 @@
 // allocate device memory.
 //
 // Who needs it: code that runs where cudaMalloc is unavailable or unsafe --
-// inside a memory-pool-managed host application that forbids driver
+// inside a memory-pool-managed host application that forbids CUDA
 // allocations, inside a host callback or a stream-ordered section that must
 // not synchronise the device, or a caller that already owns its particle
 // arrays on the device and has no mdg handle (creating one allocates the
