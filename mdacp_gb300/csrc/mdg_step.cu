@@ -48,26 +48,6 @@ constexpr int kStepThreads = 128;
 #define MDG_STEP_UNROLL 4
 #endif
 constexpr int kUnroll = MDG_STEP_UNROLL;
-// 0: none; 1: prefetch the per-particle state into L2; 2: into L1.
-#ifndef MDG_STATE_PREFETCH
-#define MDG_STATE_PREFETCH 0
-#endif
-// List rows requested into L2 this many entries ahead of the pair loop (0:
-// none).  16 measured best at 4M atoms (step kernel 0.476 -> 0.440 ms; 8: 0.472,
-// 12: 0.472, 20: 0.442, 24: 0.445, 32: 0.452, 64: 0.458).
-#ifndef MDG_ENTRY_L2_AHEAD
-#define MDG_ENTRY_L2_AHEAD 16
-#endif
-constexpr int kEntryAhead = MDG_ENTRY_L2_AHEAD;
-
-template <class T>
-__device__ __forceinline__ void prefetch_state(const T *p) {
-#if MDG_STATE_PREFETCH == 2
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-#else
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-#endif
-}
 
 __device__ __forceinline__ double rcp_hh3(double x) {
   double y;
@@ -298,14 +278,6 @@ __global__ void __launch_bounds__(kStepThreads, PMODE == 1 ? MDG_STEP_MIN_BLOCKS
     // build-time local position; its w word holds the home-cell coordinates
     const float4 lb = d.qf[i];
     const CellPos cp = cell_pos_packed(g, lb.w);
-#if MDG_STATE_PREFETCH
-    // the per-particle state read after the pair loop, requested now so its
-    // latency overlaps the loop
-    prefetch_state(d.p + i);
-    prefetch_state(qm + i);
-    prefetch_state(d.q_build + i);
-    if (!prune) prefetch_state(d.loc_p + i);
-#endif
     double3 F;
     if (prune)
       F = MIXED ? force_mixed<true>(g, d, d.loc[par], i, cp, d.nl, d.ncount, &kept)
