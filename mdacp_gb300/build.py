@@ -39,7 +39,9 @@ def _stale(target, deps):
     if not os.path.exists(target):
         return True
     t = os.path.getmtime(target)
-    return any(os.path.getmtime(d) > t for d in deps)
+    # an equal time counts as newer: a source saved in the same clock tick as
+    # the last build is rebuilt
+    return any(os.path.getmtime(d) >= t for d in deps)
 
 
 def build(force=False, verbose=False, extra_flags=(), check=False):
