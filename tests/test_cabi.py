@@ -64,3 +64,16 @@ def test_invalid_parameters_rejected_before_device_use(lib):
     assert L.mdg_create(ctypes.byref(p), ctypes.byref(h)) == 1
     assert not h.value
     assert L.mdg_destroy(None) == 0
+    # the reason stays readable after the failed create, per calling thread
+    assert b"capacity" in L.mdg_last_error(None)
+    p.capacity = 100
+    p.dt = 0.0
+    assert L.mdg_create(ctypes.byref(p), ctypes.byref(h)) == 1
+    assert b"dt" in L.mdg_last_error(None)
+
+
+def test_python_manager_reports_the_create_reason():
+    from mdacp_gb300 import native
+    from mdacp_gb300.manager import MDManager
+    with pytest.raises(native.MDGError, match="dt must be"):
+        MDManager(20.0, capacity=100, dt=0.0)
