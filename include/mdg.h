@@ -119,6 +119,12 @@ int mdg_synchronize(mdg_handle *h);
  * stream around every launch of the fused step kernel; *step_kernel_ms receives
  * the summed device time of those launches (for roofline accounting). */
 int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms);
+/* The phase times of the reference's StopWatch objects (mdmanager.cc:117-147,
+ * stopwatch.h:8-37) for nsteps steps run as in mdg_calculate_profiled:
+ * phase_ms[0] = the fused step kernels (force, kick, drifts; "force"),
+ * phase_ms[1] = the rebuild sequences (wrap, bin, sort, list build; "pair"),
+ * phase_ms[2] = the whole run ("all"), device milliseconds. */
+int mdg_calculate_phases(mdg_handle *h, int32_t nsteps, double phase_ms[3]);
 /* Replaces KineticEnergyObserver, PotentialEnergyObserver and VirialObserver
  * (observer.cc:5-79) at the current positions: out[0] = sum p^2/2,
  * out[1] = sum of pair energies, out[2] = sum of pair virials / 3. */

@@ -684,36 +684,45 @@ int mdg_calculate(mdg_handle *h, int32_t nsteps) {
 
 int mdg_synchronize(mdg_handle *h) { return check_handle(h, false); }
 
-int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms) {
-  int rc = check_handle(h, true);
-  if (rc) return rc;
-  if (nsteps < 0 || !step_kernel_ms) return fail(h, MDG_ERR_INVALID, "bad arguments");
-  *step_kernel_ms = 0.0;
+}  // extern "C"
+
+namespace {
+
+// Steps as plain launches with three events per step on the handle's stream:
+// before the rebuild sequence, before the step kernel, after it.  Sums the
+// device time of the step kernels (force, kick, drifts), of the rebuild
+// sequences (wrap, bin, sort, list build; empty launches when none is due)
+// and of the whole run.
+int profiled_run(mdg_handle *h, int32_t nsteps, double *step_ms, double *rebuild_ms, double *all_ms) {
   if (h->prm.thermostat == MDG_NOSEHOOVER && h->nh_init) {
     mdg::launch_nh_init(h->g, h->d, h->stream);
     h->launches += 2;
     h->nh_init = false;
   }
   constexpr int kChunk = 64;
-  cudaEvent_t ev[2 * kChunk];
-  for (int k = 0; k < 2 * kChunk; k++) MDG_CK(cudaEventCreate(&ev[k]));
+  cudaEvent_t ev[3 * kChunk];
+  for (int k = 0; k < 3 * kChunk; k++) MDG_CK(cudaEventCreate(&ev[k]));
   long long done = 0;
-  double total = 0.0;
+  double t_step = 0.0, t_rebuild = 0.0, t_all = 0.0;
   int status = MDG_OK;
   for (int guard = 0; guard < 1000000 && done < nsteps && status == MDG_OK; guard++) {
     const unsigned long long before = (unsigned long long)h->steps_host;
     const int m = (int)((nsteps - done) < kChunk ? (nsteps - done) : kChunk);
     for (int k = 0; k < m; k++) {
-      enqueue_step(h, h->par, 3, ev[2 * k], ev[2 * k + 1]);
+      cudaEventRecord(ev[3 * k], h->stream);
+      enqueue_step(h, h->par, 3, ev[3 * k + 1], ev[3 * k + 2]);
       h->launches += kernels_per_step(h) + 1;
       h->par ^= 1;
     }
     status = read_flags(h);
     if (status) break;
     for (int k = 0; k < m; k++) {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]) == cudaSuccess) total += ms;
+      float a = 0.f, b = 0.f;
+      if (cudaEventElapsedTime(&a, ev[3 * k], ev[3 * k + 1]) == cudaSuccess) t_rebuild += a;
+      if (cudaEventElapsedTime(&b, ev[3 * k + 1], ev[3 * k + 2]) == cudaSuccess) t_step += b;
     }
+    float w = 0.f;
+    if (cudaEventElapsedTime(&w, ev[0], ev[3 * (m - 1) + 2]) == cudaSuccess) t_all += w;
     long long completed = (long long)(h->hflags->steps - before);
     if (h->hflags->halt == 0) {
       done += completed;
@@ -726,9 +735,31 @@ int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms
       status = halt_error(h);
     }
   }
-  for (int k = 0; k < 2 * kChunk; k++) cudaEventDestroy(ev[k]);
-  *step_kernel_ms = total;
+  for (int k = 0; k < 3 * kChunk; k++) cudaEventDestroy(ev[k]);
+  if (step_ms) *step_ms = t_step;
+  if (rebuild_ms) *rebuild_ms = t_rebuild;
+  if (all_ms) *all_ms = t_all;
   return status;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  if (nsteps < 0 || !step_kernel_ms) return fail(h, MDG_ERR_INVALID, "bad arguments");
+  *step_kernel_ms = 0.0;
+  return profiled_run(h, nsteps, step_kernel_ms, nullptr, nullptr);
+}
+
+int mdg_calculate_phases(mdg_handle *h, int32_t nsteps, double phase_ms[3]) {
+  int rc = check_handle(h, true);
+  if (rc) return rc;
+  if (nsteps < 0 || !phase_ms) return fail(h, MDG_ERR_INVALID, "bad arguments");
+  phase_ms[0] = phase_ms[1] = phase_ms[2] = 0.0;
+  return profiled_run(h, nsteps, &phase_ms[0], &phase_ms[1], &phase_ms[2]);
 }
 
 int mdg_observe(mdg_handle *h, double out[3]) {

@@ -142,6 +142,13 @@ class MDManager:
         self._ck(self.lib.mdg_calculate_profiled(self._h, int(nsteps), ctypes.byref(ms)))
         return ms.value
 
+    def calculate_phases(self, nsteps):
+        """Steps without graph replay; device ms per phase as the reference's
+        StopWatch objects split Calculate: {"force", "pair", "all"}."""
+        out = np.zeros(3)
+        self._ck(self.lib.mdg_calculate_phases(self._h, int(nsteps), _dp(out)))
+        return {"force": out[0], "pair": out[1], "all": out[2]}
+
     def forces(self):
         f4 = np.zeros((self.n, 4))
         self._ck(self.lib.mdg_forces(self._h, _dp(f4)))

@@ -49,6 +49,7 @@ SIGNATURES = {
     "mdg_calculate": (ctypes.c_int, [_P, ctypes.c_int32]),
     "mdg_synchronize": (ctypes.c_int, [_P]),
     "mdg_calculate_profiled": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
+    "mdg_calculate_phases": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
     "mdg_observe": (ctypes.c_int, [_P, _D]),
     "mdg_forces": (ctypes.c_int, [_P, _D]),
     "mdg_pairs": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.c_int64,

@@ -269,3 +269,19 @@ def test_new_state_of_the_same_size_reuses_graphs_correctly():
         ref.make_pairlist()
         ref.calculate(40)
         np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-10, atol=1e-12)
+
+
+def test_phase_times_split_the_run():
+    # StopWatch-like split: step kernels ("force"), rebuild sequences ("pair")
+    # and the whole run; the first step after set_state rebuilds
+    q, p, L = liquid_like(0.5, 12, seed=57)
+    m = _gpu(L, len(q), precision="mixed")
+    m.set_state(q, p)
+    ph = m.calculate_phases(60)
+    assert ph["force"] > 0 and ph["pair"] > 0
+    assert ph["force"] + ph["pair"] <= ph["all"] * 1.001
+    assert m.stats()["steps"] == 60
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN)
+    ref.make_pairlist()
+    ref.calculate(60)
+    np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-5, atol=1e-6)
