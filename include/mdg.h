@@ -204,6 +204,9 @@ int mdg_batch_observe(mdg_batch *b, double *out);
 int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t *lanes_per_particle,
                    int32_t *ctas_per_sm);
 int mdg_batch_set_shape(mdg_batch *b, int32_t threads, int32_t lanes_per_particle, int32_t ctas_per_sm);
+/* Whether one lane per particle walks the inner list (1, the default when the
+ * buffer is > 0) or every listed pair (0); mdg_batch_tune chooses it too. */
+int mdg_batch_set_inner(mdg_batch *b, int32_t on);
 int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s);
 
 /* ------------------------------------------------------------------------
@@ -235,6 +238,7 @@ typedef struct mdg_adjoint_params {
 typedef struct mdg_adjoint mdg_adjoint;
 
 void mdg_adjoint_params_default(mdg_adjoint_params *p);
+/* n particles, 2 <= n < 2^26; every box edge > 2 (cutoff * sigma + margin). */
 int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out);
 int mdg_adjoint_destroy(mdg_adjoint *a);
 const char *mdg_adjoint_last_error(const mdg_adjoint *a);

@@ -38,6 +38,7 @@ SIGNATURES = {
     "mdg_batch_observe": (ctypes.c_int, [_P, _D]),
     "mdg_batch_tune": (ctypes.c_int, [_P, ctypes.c_int32, _I, _I, _I]),
     "mdg_batch_set_shape": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "mdg_batch_set_inner": (ctypes.c_int, [_P, ctypes.c_int32]),
     "mdg_batch_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(BatchStats)]),
 }
 
@@ -136,6 +137,10 @@ class Batch:
         self._ck(self.lib.mdg_batch_tune(self._h, int(trial_steps), ctypes.byref(t), ctypes.byref(lp),
                                          ctypes.byref(c)))
         return t.value, lp.value, c.value
+
+    def set_inner(self, on):
+        """One lane per particle walks the inner list (True) or every listed pair."""
+        self._ck(self.lib.mdg_batch_set_inner(self._h, 1 if on else 0))
 
     def set_shape(self, threads, lanes, ctas_per_sm):
         self._ck(self.lib.mdg_batch_set_shape(self._h, threads, lanes, ctas_per_sm))

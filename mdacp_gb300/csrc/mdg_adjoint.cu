@@ -19,12 +19,18 @@
 // H v is the Hessian-vector product over the same pair list.  States are
 // checkpointed every K steps in the forward pass; the backward pass recomputes
 // each segment from its checkpoint (storing its K half-step positions and
-// states) and then reverses it.  Each checkpoint segment has its own pair
-// list (every pair within cutoff*sigma + margin at the segment's first state,
-// minimum image), built from the same state in both passes; the forward pass
-// verifies that no particle moves more than margin/2 within a segment.  The
-// pair kernels give each particle kLanes lanes and evaluate the pair terms
-// without divisions (GB300's FP64 rate is 1/64 of FP32).
+// states) and then reverses it.  Each checkpoint segment starts by wrapping
+// the positions into the box (a shift by whole box lengths: forces, objectives
+// and adjoints are unchanged) and has its own pair list (every pair within
+// cutoff*sigma + margin at the segment's first state, minimum image), built
+// from the same state in both passes; the forward pass verifies that no
+// particle moves more than margin/2 within a segment.  A list entry keeps the
+// pair's image at the segment's first state, which stays the minimum image of
+// every pair within the cut-off for the whole segment (box > 2 (rc + margin)),
+// so the pair kernels form the separation with one subtraction per axis
+// (from q_i, q_i - L or q_i + L, held per lane) instead of a rounding.  The pair kernels give each particle kLanes lanes and evaluate
+// the pair terms in Horner form, without divisions (GB300's FP64 rate is 1/64
+// of FP32).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -59,24 +65,50 @@ struct P {
   double volume;
   // eps / sigma^k products used per pair (no division in the pair terms)
   double inv_s2, e_s, e_s2, e_s3, e_s4;
+  // coefficients of the pair terms in Horner form (pair_terms)
+  double kf6, kf0, kfc, kp6, kp0, ke6, ke0, kec2, kec0, kd6, kd0, kdc, ks6, ks0, ksc;
+  double kg6, kg0, kgc, kr6, kr0, krc, kq6, kq0, kqc;
   int n, cap, objective, pad;
 };
+
+// A list entry: partner index << kImageBits | per axis two bits r + 1, the
+// pair's image being q_j - r L (r in {-1, 0, 1}).
+constexpr int kImageBits = 6;
+constexpr int kMaxAdjointParticles = 1 << (32 - kImageBits);
 
 struct D {
   double4_32a *q, *p, *qh, *F, *aq, *ap, *aqh, *tmp, *q0;
   double4_32a *ckq, *ckp;    // checkpoints
+  float4 *qf;                // float copy of the segment's first state (the list test)
   double4_32a *segq, *segp, *segqh;  // recomputed segment
-  int *nbr, *cnt;            // the current segment's list, row-major [n][cap]
+  uint32_t *nbr;             // the current segment's list, row-major [n][cap]
+  int *cnt;
   double *part;              // block partials
   double *acc;               // running sums: J, g_eps, g_sig
   int *flag;
   unsigned int *done;        // blocks of the current reduction that wrote their partials
 };
 
-__device__ __forceinline__ void min_image(const P &c, double &dx, double &dy, double &dz) {
-  dx -= c.L[0] * rint(dx * c.inv_L[0]);
-  dy -= c.L[1] * rint(dy * c.inv_L[1]);
-  dz -= c.L[2] * rint(dz * c.inv_L[2]);
+// Particle i's position and its images q_i - L, q_i + L per axis.
+struct Home {
+  double x, y, z, xm, ym, zm, xp, yp, zp;
+};
+
+__device__ __forceinline__ Home make_home(const P &c, const double4_32a &q) {
+  return Home{q.x, q.y, q.z, q.x - c.L[0], q.y - c.L[1], q.z - c.L[2], q.x + c.L[0], q.y + c.L[1], q.z + c.L[2]};
+}
+
+// The partner of entry e and the separation d = q_j - r L - q_i in the
+// entry's image, formed as q_j - (q_i + r L).
+__device__ __forceinline__ int pair_sep(uint32_t e, const double4_32a *q, const Home &h, double &dx, double &dy,
+                                        double &dz) {
+  const int j = (int)(e >> kImageBits);
+  const double4_32a qj = q[j];
+  const uint32_t ix = e & 3u, iy = (e >> 2) & 3u, iz = (e >> 4) & 3u;
+  dx = qj.x - (ix == 1u ? h.x : (ix == 0u ? h.xm : h.xp));
+  dy = qj.y - (iy == 1u ? h.y : (iy == 0u ? h.ym : h.yp));
+  dz = qj.z - (iz == 1u ? h.z : (iz == 0u ? h.zm : h.zp));
+  return j;
 }
 
 // 1/x from the hardware estimate refined by one cubic Householder step
@@ -100,39 +132,70 @@ struct PairTerms {
   double gs;     // d g / d sigma
 };
 
+// With x^2 = r^2 / sigma^2, psi(x) = phi'(x)/x = -48 x^-14 + 24 x^-8 + 8 C2,
+// chi(x) = x^2 psi(x):
+//   f     = eps/s^2 psi              = x^-8 (kf6 x^-6 + kf0) + kfc
+//   fpr   = eps/s^4 psi'(x)/x        = x^-10 (kp6 x^-6 + kp0)
+//   phi   = eps phi(x)               = x^-6 (ke6 x^-6 + ke0) + (kec2 x^2 + kec0)
+//   dphis = -eps/s x phi'(x)         = x^-6 (kd6 x^-6 + kd0) + kdc x^2
+//   fs    = -eps/s^3 (2 psi + x psi'(x))  = x^-8 (ks6 x^-6 + ks0) + ksc
+//   g     = eps chi(x)               = x^-6 (kg6 x^-6 + kg0) + kgc x^2
+//   gpr   = eps/s^2 chi'(x)/x        = x^-8 (kr6 x^-6 + kr0) + krc
+//   gs    = -eps/s x chi'(x)         = x^-6 (kq6 x^-6 + kq0) + kqc x^2
+// (coefficients set in mdg_adjoint_create; the kernels keep the terms they use).
 __device__ __forceinline__ bool pair_terms(const P &c, double r2, PairTerms &t) {
   const double x2 = r2 * c.inv_s2;
   // x2 >= +0: compared as bit patterns, on the integer pipe (same order)
   if (__double_as_longlong(x2) > __double_as_longlong(c.xc2)) return false;
-  const double ix2 = recip(x2), ix6 = ix2 * ix2 * ix2, ix8 = ix6 * ix2, ix12 = ix6 * ix6, ix14 = ix12 * ix2;
-  const double ix10 = ix8 * ix2, ix16 = ix14 * ix2;
-  // psi(x) = phi'(x)/x, chi(x) = x^2 psi(x)
-  const double psi = -48.0 * ix14 + 24.0 * ix8 + 8.0 * c.c2;
-  const double dpsi_x = 672.0 * ix16 - 192.0 * ix10;      // psi'(x)/x
-  const double phi = 4.0 * (ix12 - ix6 + c.c2 * x2 + c.c0);
-  const double xdphi = 4.0 * (-12.0 * ix12 + 6.0 * ix6 + 2.0 * c.c2 * x2);  // x phi'(x)
-  const double chi = x2 * psi;                               // -48 x^-12 + 24 x^-6 + 8 C2 x^2
-  const double xdchi = 576.0 * ix12 - 144.0 * ix6 + 16.0 * c.c2 * x2;  // x chi'(x)
-  t.f = c.e_s2 * psi;
-  t.fpr = c.e_s4 * dpsi_x;
-  t.phi = c.eps * phi;
-  t.fs = -c.e_s3 * (2.0 * psi + x2 * dpsi_x);
-  t.dphis = -c.e_s * xdphi;
-  t.g = c.eps * chi;
-  t.gpr = c.e_s2 * (xdchi * ix2);
-  t.gs = -c.e_s * xdchi;
+  const double ix2 = recip(x2), ix4 = ix2 * ix2, ix6 = ix4 * ix2, ix8 = ix4 * ix4, ix10 = ix8 * ix2;
+  t.f = fma(ix8, fma(c.kf6, ix6, c.kf0), c.kfc);
+  t.fpr = ix10 * fma(c.kp6, ix6, c.kp0);
+  t.phi = fma(ix6, fma(c.ke6, ix6, c.ke0), fma(c.kec2, x2, c.kec0));
+  t.dphis = fma(ix6, fma(c.kd6, ix6, c.kd0), c.kdc * x2);
+  t.fs = fma(ix8, fma(c.ks6, ix6, c.ks0), c.ksc);
+  t.g = fma(ix6, fma(c.kg6, ix6, c.kg0), c.kgc * x2);
+  t.gpr = fma(ix8, fma(c.kr6, ix6, c.kr0), c.krc);
+  t.gs = fma(ix6, fma(c.kq6, ix6, c.kq0), c.kqc * x2);
   return true;
 }
 
-__device__ __forceinline__ double block_sum(double v, double *sh) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+// Row i's entries k = lane, lane + kLanes, ...: body(t, dx, dy, dz, j) for
+// each pair within the cut-off, in the row's order.
+template <class Body>
+__device__ __forceinline__ void for_pairs(const P &c, const D &d, int i, int lane, const double4_32a *q,
+                                          const Home &h, Body body) {
+  const int cnt = d.cnt[i];
+  const uint32_t *row = d.nbr + (size_t)i * c.cap;
+  for (int k = lane; k < cnt; k += kLanes) {
+    double dx, dy, dz;
+    const int j = pair_sep(row[k], q, h, dx, dy, dz);
+    PairTerms t;
+    if (pair_terms(c, dx * dx + dy * dy + dz * dz, t)) body(t, dx, dy, dz, j);
+  }
+}
+
+// Block sums of three values at once (thread 0 holds them).
+__device__ __forceinline__ void block_sum3(double &a, double &b, double &e, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    e += __shfl_down_sync(0xffffffffu, e, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sh[3 * (threadIdx.x >> 5)] = a;
+    sh[3 * (threadIdx.x >> 5) + 1] = b;
+    sh[3 * (threadIdx.x >> 5) + 2] = e;
+  }
   __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+  if (threadIdx.x == 0) {
+    a = b = e = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      a += sh[3 * w];
+      b += sh[3 * w + 1];
+      e += sh[3 * w + 2];
+    }
+  }
   __syncthreads();
-  return t;
 }
 
 // Writes this block's three partials; the last block of the grid to do so
@@ -141,7 +204,7 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // No block waits for another.
 __device__ void partials_accumulate(const D &d, double A, double B, double E, double w) {
   __shared__ int last;
-  __shared__ double sh2[32];
+  __shared__ double sh2[96];
   if (threadIdx.x == 0) {
     d.part[3 * blockIdx.x + 0] = A;
     d.part[3 * blockIdx.x + 1] = B;
@@ -157,11 +220,11 @@ __device__ void partials_accumulate(const D &d, double A, double B, double E, do
     b += __ldcg(d.part + 3 * k + 1);
     e += __ldcg(d.part + 3 * k + 2);
   }
-  const double ta = block_sum(a, sh2), tb = block_sum(b, sh2), te = block_sum(e, sh2);
+  block_sum3(a, b, e, sh2);
   if (threadIdx.x == 0) {
-    d.acc[0] += w * ta;
-    d.acc[1] += w * tb;
-    d.acc[2] += w * te;
+    d.acc[0] += w * a;
+    d.acc[1] += w * b;
+    d.acc[2] += w * e;
     *d.done = 0;
   }
 }
@@ -173,31 +236,35 @@ __device__ __forceinline__ double lane_sum(double v) {
   return v;
 }
 
-// Pair list at positions q: every partner within the list radius, minimum
-// image.  kLanes lanes share a particle: lane l tests partners j = l, l +
-// kLanes, ... (a particle's lanes read neighbouring positions together), first
-// counting, then writing at its offset in the row (a prefix sum over the
-// lanes), so the row order is fixed: lane 0's partners, then lane 1's, ...
-// The test runs in float against a radius widened by 1e-3 (float positions of
-// a box of tens of sigma are within 1e-5), so every pair within the exact
-// radius is listed; a few more do no harm (the pair terms cut at rc).
+// Pair list at positions q (wrapped into the box): every partner within the
+// list radius, minimum image.  kLanes lanes share a particle: lane l tests
+// partners j = l, l + kLanes, ... (a particle's lanes read neighbouring
+// positions together), first counting, then writing at its offset in the row
+// (a prefix sum over the lanes), so the row order is fixed: lane 0's partners,
+// then lane 1's, ...  The test runs in float against a radius widened by 1e-3
+// (float positions of a box of tens of sigma are within 1e-5), so every pair
+// within the exact radius is listed; a few more do no harm (the pair terms cut
+// at rc).  The float positions come from d.qf (k_wrap writes them), so a
+// candidate costs one 16-byte load and no conversions.  The recorded image is
+// the double-precision minimum image, r = rint((q_j - q_i) / L) per axis, in
+// {-1, 0, 1} for wrapped positions.
 __global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
   const bool active = i < c.n;
   float qx = 0.f, qy = 0.f, qz = 0.f;
   if (active) {
-    const double4_32a v = q[i];
-    qx = (float)v.x;
-    qy = (float)v.y;
-    qz = (float)v.z;
+    const float4 v = d.qf[i];
+    qx = v.x;
+    qy = v.y;
+    qz = v.z;
   }
   const float lx = (float)c.L[0], ly = (float)c.L[1], lz = (float)c.L[2];
   const float ilx = (float)c.inv_L[0], ily = (float)c.inv_L[1], ilz = (float)c.inv_L[2];
   const float sl2f = (float)c.sl2f;
   auto within = [&](int j) {
-    const double4_32a v = q[j];
-    float dx = (float)v.x - qx, dy = (float)v.y - qy, dz = (float)v.z - qz;
+    const float4 v = d.qf[j];
+    float dx = v.x - qx, dy = v.y - qy, dz = v.z - qz;
     dx -= lx * rintf(dx * ilx);
     dy -= ly * rintf(dy * ily);
     dz -= lz * rintf(dz * ilz);
@@ -216,10 +283,17 @@ __global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
   const int total = __shfl_sync(0xffffffffu, incl, kLanes - 1, kLanes);
   if (active) {
     int w = incl - m;
-    int *row = d.nbr + (size_t)i * c.cap;
+    uint32_t *row = d.nbr + (size_t)i * c.cap;
+    const double4_32a qi = q[i];
     for (int j = lane; j < c.n; j += kLanes)
       if (within(j)) {
-        if (w < c.cap) row[w] = j;
+        if (w < c.cap) {
+          const double4_32a v = q[j];
+          const int rx = (int)rint((v.x - qi.x) * c.inv_L[0]), ry = (int)rint((v.y - qi.y) * c.inv_L[1]),
+                    rz = (int)rint((v.z - qi.z) * c.inv_L[2]);
+          row[w] = ((uint32_t)j << kImageBits) | (uint32_t)(rx + 1) | ((uint32_t)(ry + 1) << 2) |
+                   ((uint32_t)(rz + 1) << 4);
+        }
         w++;
       }
     if (lane == 0) {
@@ -242,16 +316,12 @@ __global__ void k_force(P c, D d, const double4_32a *q, double4_32a *F) {
       const double ux = qi.x - z.x, uy = qi.y - z.y, uz = qi.z - z.z;
       if (ux * ux + uy * uy + uz * uz > c.half_margin2) atomicMax(d.flag + 1, 1);
     }
-    for (int k = lane; k < d.cnt[i]; k += kLanes) {
-      const double4_32a qj = q[d.nbr[(size_t)i * c.cap + k]];
-      double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-      min_image(c, dx, dy, dz);
-      PairTerms t;
-      if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
+    const Home h = make_home(c, qi);
+    for_pairs(c, d, i, lane, q, h, [&](const PairTerms &t, double dx, double dy, double dz, int) {
       fx += t.f * dx;
       fy += t.f * dy;
       fz += t.f * dz;
-    }
+    });
   }
   fx = lane_sum(fx);
   fy = lane_sum(fy);
@@ -269,6 +339,24 @@ __global__ void k_drift(P c, const double4_32a *q, const double4_32a *p, double4
   a.y += b.y * c.dt2;
   a.z += b.z * c.dt2;
   out[i] = a;
+}
+
+// A segment's first state: with wrap, positions into the box, q - k L per
+// axis with k = floor(q / L) (particles already inside keep their bits); then
+// the float copy for the list test.  The backward pass calls it without wrap
+// on the checkpoint the forward pass wrapped.
+__global__ void k_wrap(P c, double4_32a *q, float4 *qf, int wrap) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= c.n) return;
+  double4_32a a = q[i];
+  if (wrap) {
+    const double kx = floor(a.x * c.inv_L[0]), ky = floor(a.y * c.inv_L[1]), kz = floor(a.z * c.inv_L[2]);
+    if (kx != 0.0) a.x = fma(-kx, c.L[0], a.x);
+    if (ky != 0.0) a.y = fma(-ky, c.L[1], a.y);
+    if (kz != 0.0) a.z = fma(-kz, c.L[2], a.z);
+    q[i] = a;
+  }
+  qf[i] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.f);
 }
 
 // p_out = p_in + F dt; q_out = qh + p_out dt/2; and, when qh_next is given,
@@ -306,19 +394,15 @@ __global__ void k_kick_drift(P c, const double4_32a *qh, const double4_32a *F, c
 template <int OBJ, int GRAD>
 __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p, double w) {
   constexpr bool grad = GRAD != 0;
-  __shared__ double sh[32];
+  __shared__ double sh[96];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
   double val = 0, ge = 0, gs = 0;
   double gx = 0, gy = 0, gz = 0, u = 0, us = 0, G = 0, Gs = 0;
   if (i < c.n) {
     const double4_32a qi = q[i];
-    for (int k = lane; k < d.cnt[i]; k += kLanes) {
-      const double4_32a qj = q[d.nbr[(size_t)i * c.cap + k]];
-      double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-      min_image(c, dx, dy, dz);
-      PairTerms t;
-      if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
+    const Home h = make_home(c, qi);
+    for_pairs(c, d, i, lane, q, h, [&](const PairTerms &t, double dx, double dy, double dz, int) {
       if (OBJ == 0) {
         u += 0.5 * t.phi;
         us += 0.5 * t.dphis;
@@ -336,7 +420,7 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
           gz += t.gpr * dz;
         }
       }
-    }
+    });
   }
   if (grad) {
     gx = lane_sum(gx);
@@ -383,8 +467,8 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
       }
     }
   }
-  const double A = block_sum(val, sh), B = block_sum(ge, sh), E = block_sum(gs, sh);
-  partials_accumulate(d, A, B, E, w);
+  block_sum3(val, ge, gs, sh);
+  partials_accumulate(d, val, ge, gs, w);
 }
 
 // Reverse of one step at half-step positions qh.  In: aq, ap adjoints of
@@ -404,20 +488,16 @@ __global__ void k_reverse(P c, D d) {
 }
 
 __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
-  __shared__ double sh[32];
+  __shared__ double sh[96];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
   double te = 0, ts = 0;
   double hx = 0, hy = 0, hz = 0, fx = 0, fy = 0, fz = 0, sx = 0, sy = 0, sz = 0;
   if (i < c.n) {
     const double4_32a qi = qh[i], vi = d.tmp[i];
-    for (int k = lane; k < d.cnt[i]; k += kLanes) {
-      const int j = d.nbr[(size_t)i * c.cap + k];
-      const double4_32a qj = qh[j], vj = d.tmp[j];
-      double dx = qj.x - qi.x, dy = qj.y - qi.y, dz = qj.z - qi.z;
-      min_image(c, dx, dy, dz);
-      PairTerms t;
-      if (!pair_terms(c, dx * dx + dy * dy + dz * dz, t)) continue;
+    const Home h = make_home(c, qi);
+    for_pairs(c, d, i, lane, qh, h, [&](const PairTerms &t, double dx, double dy, double dz, int j) {
+      const double4_32a vj = d.tmp[j];
       const double wx = vi.x - vj.x, wy = vi.y - vj.y, wz = vi.z - vj.z;
       const double dw = dx * wx + dy * wy + dz * wz;
       // (H v)_i = sum_j f (v_i - v_j) + (f'/r) d (d . (v_i - v_j))
@@ -430,7 +510,7 @@ __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
       sx += t.fs * dx;
       sy += t.fs * dy;
       sz += t.fs * dz;
-    }
+    });
   }
   hx = lane_sum(hx); hy = lane_sum(hy); hz = lane_sum(hz);
   fx = lane_sum(fx); fy = lane_sum(fy); fz = lane_sum(fz);
@@ -452,8 +532,9 @@ __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
     d.aq[i] = a;
     d.ap[i] = pb;
   }
-  const double B = block_sum(te, sh), E = block_sum(ts, sh);
-  partials_accumulate(d, 0.0, B, E, 1.0);
+  double none = 0.0;
+  block_sum3(none, te, ts, sh);
+  partials_accumulate(d, 0.0, te, ts, 1.0);
 }
 
 }  // namespace adj
@@ -520,20 +601,20 @@ int enqueue_forward(mdg_adjoint *a) {
   MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
   const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
   const double w = 1.0 / Ns;
-  MDG_ACK(cudaMemcpyAsync(d.ckq, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
-  MDG_ACK(cudaMemcpyAsync(d.ckp, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
-  k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.p, d.qh);
   for (int n = 1; n <= Ns; n++) {
-    if ((n - 1) % K == 0) {  // a checkpoint segment starts: its own list
+    if ((n - 1) % K == 0) {  // a checkpoint segment starts: wrapped state, checkpoint, its own list
+      const size_t ck = (size_t)((n - 1) / K);
+      k_wrap<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.qf, 1);
+      MDG_ACK(cudaMemcpyAsync(d.ckq + N * ck, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+      MDG_ACK(cudaMemcpyAsync(d.ckp + N * ck, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
       MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
       k_build<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.q);
+      k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.p, d.qh);
     }
-    fwd_step(a, d.qh, d.p, d.q, d.p, n < Ns ? d.qh : nullptr);
+    // the next step's half-drift here unless a segment starts there (as the
+    // backward pass recomputes it: from the wrapped checkpoint)
+    fwd_step(a, d.qh, d.p, d.q, d.p, n < Ns && n % K != 0 ? d.qh : nullptr);
     launch_objective(a, d.q, d.p, false, w);
-    if (n % K == 0) {
-      MDG_ACK(cudaMemcpyAsync(d.ckq + N * (n / K), d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
-      MDG_ACK(cudaMemcpyAsync(d.ckp + N * (n / K), d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
-    }
   }
   return cudaGetLastError() == cudaSuccess ? MDG_OK : afail(a, MDG_ERR_CUDA, "adjoint forward launch failed");
 }
@@ -556,6 +637,7 @@ int enqueue_backward(mdg_adjoint *a) {
     MDG_ACK(cudaMemcpyAsync(d.segp, d.ckp + N * (seg_start / K), bytes, cudaMemcpyDeviceToDevice, a->s));
     // the segment's list, built from the same state as in the forward pass
     MDG_ACK(cudaMemcpyAsync(d.q0, d.segq, bytes, cudaMemcpyDeviceToDevice, a->s));
+    k_wrap<<<a->grid, kT, 0, a->s>>>(a->c, d.segq, d.qf, 0);
     k_build<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segq);
     k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.segq, d.segp, d.segqh + N);
     for (int k = 1; k <= len; k++)
@@ -615,6 +697,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
       !(p->sigma > 0) || (p->objective != MDG_OBJ_POTENTIAL && p->objective != MDG_OBJ_PRESSURE))
     return MDG_ERR_INVALID;
   *out = nullptr;
+  if (n >= kMaxAdjointParticles) return MDG_ERR_INVALID;
   const double sl = p->cutoff * p->sigma + p->margin;
   for (int k = 0; k < 3; k++)
     if (!(p->box[k] > 2.0 * sl)) return MDG_ERR_INVALID;
@@ -639,6 +722,15 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   const double s2 = 1.0 / c.xc2, s6 = s2 * s2 * s2, s8 = s6 * s2, s12 = s6 * s6, s14 = s12 * s2;
   c.c2 = 6.0 * s14 - 3.0 * s8;  // variables.cc:16-28 in sigma units
   c.c0 = -s12 + s6 - c.c2 / s2;
+  const double ep = c.eps;
+  c.kf6 = -48.0 * c.e_s2; c.kf0 = 24.0 * c.e_s2; c.kfc = 8.0 * c.c2 * c.e_s2;
+  c.kp6 = 672.0 * c.e_s4; c.kp0 = -192.0 * c.e_s4;
+  c.ke6 = 4.0 * ep; c.ke0 = -4.0 * ep; c.kec2 = 4.0 * ep * c.c2; c.kec0 = 4.0 * ep * c.c0;
+  c.kd6 = 48.0 * c.e_s; c.kd0 = -24.0 * c.e_s; c.kdc = -8.0 * c.c2 * c.e_s;
+  c.ks6 = -576.0 * c.e_s3; c.ks0 = 144.0 * c.e_s3; c.ksc = -16.0 * c.c2 * c.e_s3;
+  c.kg6 = -48.0 * ep; c.kg0 = 24.0 * ep; c.kgc = 8.0 * ep * c.c2;
+  c.kr6 = 576.0 * c.e_s2; c.kr0 = -144.0 * c.e_s2; c.krc = 16.0 * c.c2 * c.e_s2;
+  c.kq6 = -576.0 * c.e_s; c.kq0 = 144.0 * c.e_s; c.kqc = -16.0 * c.c2 * c.e_s;
   c.sl2 = sl * sl;
   c.sl2f = (sl + 1e-3) * (sl + 1e-3);
   c.half_margin2 = 0.25 * p->margin * p->margin;
@@ -664,6 +756,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   if (e == cudaSuccess) e = aalloc(&d.segqh, N * (K + 1));
   if (e == cudaSuccess) e = aalloc(&d.nbr, N * (size_t)c.cap);
   if (e == cudaSuccess) e = aalloc(&d.cnt, N);
+  if (e == cudaSuccess) e = aalloc(&d.qf, N);
   if (e == cudaSuccess) e = aalloc(&d.part, 3 * (size_t)a->gridp);
   if (e == cudaSuccess) e = aalloc(&d.acc, 3);
   if (e == cudaSuccess) e = aalloc(&d.flag, 2);
@@ -686,7 +779,7 @@ int mdg_adjoint_destroy(mdg_adjoint *a) {
   if (a->gx_backward) cudaGraphExecDestroy(a->gx_backward);
   D &d = a->d;
   void *ptrs[] = {d.q, d.p, d.qh, d.F, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
-                  d.nbr, d.cnt, d.part, d.acc, d.flag, d.done};
+                  d.nbr, d.cnt, d.qf, d.part, d.acc, d.flag, d.done};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (a->s) cudaStreamDestroy(a->s);

@@ -1204,6 +1204,12 @@ int mdg_batch_set_shape(mdg_batch *b, int32_t threads, int32_t lanes_per_particl
   return assign(b);
 }
 
+int mdg_batch_set_inner(mdg_batch *b, int32_t on) {
+  if (!b) return MDG_ERR_INVALID;
+  b->use_inner = on ? 1 : 0;
+  return assign(b);  // fresh selections, graphs captured again
+}
+
 int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s) {
   if (!b || !s) return MDG_ERR_INVALID;
   memset(s, 0, sizeof(*s));

@@ -104,6 +104,13 @@ def test_inner_list_changes_nothing(precision):
         st = b.stats()
         assert st["inner_list"] == (0 if buf == 0.0 else 1)
         runs.append([x.copy() for pair in b.state() for x in pair])
+    # the inner list switched off by hand walks every listed pair
+    b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision=precision)
+    b.set_shape(256, 1, 2)
+    b.set_inner(False)
+    b.calculate(80)
+    assert b.stats()["inner_list"] == 0
+    runs.append([x.copy() for pair in b.state() for x in pair])
     for other in runs[1:]:
         for u, v in zip(runs[0], other):
             assert np.array_equal(u, v)
