@@ -181,25 +181,28 @@ __device__ void prep_box(const Params &P, const Dev &d, const BoxDesc &b, int bi
     return;
   }
   cta_scan(s_cnt, s_start, b.ncell);
+  // each cell's particles in arbitrary order (slot and id side by side in
+  // the temporaries, which the gather below rewrites) ...
   for (int a = threadIdx.x; a < n; a += blockDim.x) {
     const int c = d.cell[o + a];
-    d.order[o + s_start[c] + atomicAdd(&s_cnt[c], 1)] = a;
+    const int k = o + s_start[c] + atomicAdd(&s_cnt[c], 1);
+    d.t_cell[k] = a;
+    d.t_id[k] = d.id[o + a];
   }
-  __syncthreads();
-  for (int c = threadIdx.x; c < b.ncell; c += blockDim.x) {
-    const int lo = s_start[c], hi = s_start[c + 1];
-    d.cell_start[b.cell_off + c] = lo;
-    for (int k = lo + 1; k < hi; k++) {
-      const int v = d.order[o + k], key = d.id[o + v];
-      int m = k - 1;
-      while (m >= lo && d.id[o + d.order[o + m]] > key) {
-        d.order[o + m + 1] = d.order[o + m];
-        m--;
-      }
-      d.order[o + m + 1] = v;
-    }
-  }
+  for (int c = threadIdx.x; c < b.ncell; c += blockDim.x) d.cell_start[b.cell_off + c] = s_start[c];
   if (threadIdx.x == 0) d.cell_start[b.cell_off + b.ncell] = n;
+  __syncthreads();
+  // ... then in id order (ids are distinct): a particle's place in its cell
+  // is the number of the cell's particles with a smaller id, counted by one
+  // thread per particle with independent loads
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int v = d.t_cell[o + k], key = d.t_id[o + k];
+    const int c = d.cell[o + v];
+    const int lo = s_start[c], hi = s_start[c + 1];
+    int r = 0;
+    for (int m = lo; m < hi; m++) r += d.t_id[o + m] < key ? 1 : 0;
+    d.order[o + lo + r] = v;
+  }
   __syncthreads();
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
     const int src = o + d.order[o + k];
