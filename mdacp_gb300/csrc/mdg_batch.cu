@@ -10,12 +10,15 @@
 //   * a CTA advances each of its boxes by one step (the fused force/kick/
 //     drift over the box);
 //   * a box whose displacement test fired is rebuilt at the start of the next
-//     step by two kernels ahead of the persistent one: k_batch_prep (one CTA
-//     per rebuilding box: counting sort with the cell counters in shared
-//     memory, stable by particle index) and k_batch_list (one thread per
-//     particle of every rebuilding box, same float-first exact acceptance test
-//     as the single-box path), so a rebuild is spread over the whole GPU
-//     instead of stalling the CTA that steps the box;
+//     step by kernels ahead of the persistent one: k_batch_rebuild_set (the
+//     rebuilding boxes and their slot prefix), k_batch_bin (one thread per
+//     particle of every rebuilding box: wrap and home cell), k_batch_sort (one
+//     CTA per rebuilding box: counting sort with the cell counters in shared
+//     memory, each cell in id order), k_batch_place (one thread per particle:
+//     the reordered state and its float positions) and k_batch_list (one
+//     thread per particle, same float-first exact acceptance test as the
+//     single-box path), so a rebuild is spread over the whole GPU instead of
+//     stalling the CTA that steps the box;
 //   * lanes-per-particle (1, 2 or 4 lanes share one particle's row and reduce
 //     with shuffles), threads per CTA and CTAs per SM are chosen by the
 //     autotuner (mdg_batch_tune);
@@ -144,45 +147,54 @@ __device__ void cta_scan(int *cnt, int *out, int m) {
   __syncthreads();
 }
 
-// Rebuild of one box by the whole CTA, up to the pair list: wrap (one +-L
-// per component), bin, stable reorder by (cell, particle index), cell starts,
-// build-time and mid-step positions.
-__device__ void prep_box(const Params &P, const Dev &d, const BoxDesc &b, int bi, int par, int *s_cnt, int *s_start,
-                         int *s_err) {
+// Slot t of this step's rebuilding boxes (their particles side by side):
+// the index k into rb_boxes / rb_start with rb_start[k] <= t < rb_start[k + 1].
+__device__ __forceinline__ int rb_find(const Dev &d, int nb, int t) {
+  int lo = 0, hi = nb - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (d.rb_start[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Rebuild part 1, one thread per particle of every rebuilding box (the FP64
+// work of a rebuild spread over the GPU: at 1/64 of the FP32 rate one SM
+// per box would take ~100 us for 8,000 particles): wrap (one +-L per
+// component) and home cell.  A particle outside [-L, 2L) fails its box.
+__device__ void bin_particle(const Dev &d, const BoxDesc &b, int bi, int a) {
+  const int o = b.atom_off;
+  double4_32a q = d.q_end[o + a];
+  double x[3] = {q.x, q.y, q.z};
+  int ci[3];
+  bool bad = false;
+  for (int k = 0; k < 3; k++) {
+    double v = x[k];
+    if (v < 0.0) v += b.L[k];
+    else if (v > b.L[k]) v -= b.L[k];
+    if (!(v >= 0.0 && v <= b.L[k])) bad = true;
+    x[k] = v;
+    int c = bad ? 0 : (int)(v * b.inv_w[k]);
+    ci[k] = c < 0 ? 0 : (c >= b.nc[k] ? b.nc[k] - 1 : c);
+  }
+  if (bad) atomicExch(&d.box_err[bi], kErrBadState);
+  q.x = x[0]; q.y = x[1]; q.z = x[2];
+  d.q_end[o + a] = q;
+  d.cell[o + a] = (ci[2] * b.nc[1] + ci[1]) * b.nc[0] + ci[0];
+}
+
+// Rebuild part 2, one CTA per rebuilding box: the integer reorder.  Cell
+// counts in shared memory, their scan, then each cell's particles in id order
+// (slots and ids scattered per cell, then one thread per particle counting
+// the cell's smaller ids: ids are distinct), cell starts, and the particles
+// gathered in the new order into the temporaries.
+__device__ void sort_box(const Dev &d, const BoxDesc &b, int *s_cnt, int *s_start) {
   const int n = b.n, o = b.atom_off;
   for (int c = threadIdx.x; c < b.ncell; c += blockDim.x) s_cnt[c] = 0;
-  if (threadIdx.x == 0) *s_err = 0;
   __syncthreads();
-  for (int a = threadIdx.x; a < n; a += blockDim.x) {
-    double4_32a q = d.q_end[o + a];
-    double x[3] = {q.x, q.y, q.z};
-    int ci[3];
-    bool bad = false;
-    for (int k = 0; k < 3; k++) {
-      double v = x[k];
-      if (v < 0.0) v += b.L[k];
-      else if (v > b.L[k]) v -= b.L[k];
-      if (!(v >= 0.0 && v <= b.L[k])) bad = true;
-      x[k] = v;
-      int c = bad ? 0 : (int)(v * b.inv_w[k]);
-      ci[k] = c < 0 ? 0 : (c >= b.nc[k] ? b.nc[k] - 1 : c);
-    }
-    if (bad) *s_err = kErrBadState;
-    q.x = x[0]; q.y = x[1]; q.z = x[2];
-    d.q_end[o + a] = q;
-    const int cc = (ci[2] * b.nc[1] + ci[1]) * b.nc[0] + ci[0];
-    d.cell[o + a] = cc;
-    atomicAdd(&s_cnt[cc], 1);
-  }
+  for (int a = threadIdx.x; a < n; a += blockDim.x) atomicAdd(&s_cnt[d.cell[o + a]], 1);
   __syncthreads();
-  if (*s_err) {
-    if (threadIdx.x == 0) d.box_err[bi] = kErrBadState;
-    __syncthreads();
-    return;
-  }
   cta_scan(s_cnt, s_start, b.ncell);
-  // each cell's particles in arbitrary order (slot and id side by side in
-  // the temporaries, which the gather below rewrites) ...
   for (int a = threadIdx.x; a < n; a += blockDim.x) {
     const int c = d.cell[o + a];
     const int k = o + s_start[c] + atomicAdd(&s_cnt[c], 1);
@@ -192,9 +204,6 @@ __device__ void prep_box(const Params &P, const Dev &d, const BoxDesc &b, int bi
   for (int c = threadIdx.x; c < b.ncell; c += blockDim.x) d.cell_start[b.cell_off + c] = s_start[c];
   if (threadIdx.x == 0) d.cell_start[b.cell_off + b.ncell] = n;
   __syncthreads();
-  // ... then in id order (ids are distinct): a particle's place in its cell
-  // is the number of the cell's particles with a smaller id, counted by one
-  // thread per particle with independent loads
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
     const int v = d.t_cell[o + k], key = d.t_id[o + k];
     const int c = d.cell[o + v];
@@ -211,28 +220,30 @@ __device__ void prep_box(const Params &P, const Dev &d, const BoxDesc &b, int bi
     d.t_id[o + k] = d.id[src];
     d.t_cell[o + k] = d.cell[src];
   }
-  __syncthreads();
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const double4_32a q = d.t_q[o + k], p = d.t_p[o + k];
-    const int c = d.t_cell[o + k];
-    d.q_end[o + k] = q;
-    d.p[o + k] = p;
-    d.id[o + k] = d.t_id[o + k];
-    d.cell[o + k] = c;
-    d.q_build[o + k] = q;
-    int cx, cy, cz;
-    cell_xyz(b, c, cx, cy, cz);
-    const double ox = ((double)cx + 0.5) * (double)b.w32[0], oy = ((double)cy + 0.5) * (double)b.w32[1],
-                 oz = ((double)cz + 0.5) * (double)b.w32[2];
-    d.qf[o + k] = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), 0.0f);
-    double4_32a m = q;
-    m.x = __dadd_rn(q.x, __dmul_rn(p.x, P.dt2));
-    m.y = __dadd_rn(q.y, __dmul_rn(p.y, P.dt2));
-    m.z = __dadd_rn(q.z, __dmul_rn(p.z, P.dt2));
-    d.q_mid[par][o + k] = m;
-    d.loc[par][o + k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), 0.0f);
-  }
-  __syncthreads();
+}
+
+// Rebuild part 3, one thread per particle of every rebuilding box: the
+// reordered state back in place, with the build-time and mid-step positions.
+__device__ void place_particle(const Params &P, const Dev &d, const BoxDesc &b, int k, int par) {
+  const int o = b.atom_off;
+  const double4_32a q = d.t_q[o + k], p = d.t_p[o + k];
+  const int c = d.t_cell[o + k];
+  d.q_end[o + k] = q;
+  d.p[o + k] = p;
+  d.id[o + k] = d.t_id[o + k];
+  d.cell[o + k] = c;
+  d.q_build[o + k] = q;
+  int cx, cy, cz;
+  cell_xyz(b, c, cx, cy, cz);
+  const double ox = ((double)cx + 0.5) * (double)b.w32[0], oy = ((double)cy + 0.5) * (double)b.w32[1],
+               oz = ((double)cz + 0.5) * (double)b.w32[2];
+  d.qf[o + k] = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), 0.0f);
+  double4_32a m = q;
+  m.x = __dadd_rn(q.x, __dmul_rn(p.x, P.dt2));
+  m.y = __dadd_rn(q.y, __dmul_rn(p.y, P.dt2));
+  m.z = __dadd_rn(q.z, __dmul_rn(p.z, P.dt2));
+  d.q_mid[par][o + k] = m;
+  d.loc[par][o + k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), 0.0f);
 }
 
 // Pair-list row of local particle a of box b (the box's cell starts and
@@ -299,20 +310,40 @@ __device__ int build_row(const Params &P, const Dev &d, const BoxDesc &b, int bi
 #define MDG_BATCH_PREP_THREADS 1024
 #endif
 constexpr int kPrepThreads = MDG_BATCH_PREP_THREADS;
+constexpr int kBatchKernelsPerStep = 6;  // rebuild set, bin, sort, place, list, step
 
-__global__ void __launch_bounds__(kPrepThreads) k_batch_prep(Params P, Dev d, int par) {
-  __shared__ int s_cnt[kMaxCellsPerBox];
-  __shared__ int s_start[kMaxCellsPerBox + 1];
-  __shared__ int s_err;
-  const int bi = blockIdx.x;
-  if (!rebuilding(d, bi, *d.goal)) return;  // uniform over the CTA
-  const BoxDesc b = d.boxes[bi];
-  prep_box(P, d, b, bi, par, s_cnt, s_start, &s_err);
+__global__ void __launch_bounds__(128) k_batch_bin(Dev d) {
+  const int nb = *d.rb_count;
+  if (nb == 0) return;
+  const int total = d.rb_start[nb];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int k = rb_find(d, nb, t), bi = d.rb_boxes[k];
+    bin_particle(d, d.boxes[bi], bi, t - d.rb_start[k]);
+  }
 }
 
-// Between the two rebuild parts: the boxes that rebuild this step (after the
-// prep, which may have failed a box) in box order, and the prefix of their
-// particle counts.  One CTA of 1,024 threads.
+__global__ void __launch_bounds__(kPrepThreads) k_batch_sort(Dev d) {
+  __shared__ int s_cnt[kMaxCellsPerBox];
+  __shared__ int s_start[kMaxCellsPerBox + 1];
+  const int bi = blockIdx.x;
+  if (!rebuilding(d, bi, *d.goal)) return;  // uniform over the CTA; a box failed by k_batch_bin stops here
+  const BoxDesc b = d.boxes[bi];
+  sort_box(d, b, s_cnt, s_start);
+}
+
+__global__ void __launch_bounds__(128) k_batch_place(Params P, Dev d, int par) {
+  const int nb = *d.rb_count;
+  if (nb == 0) return;
+  const int total = d.rb_start[nb];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int k = rb_find(d, nb, t), bi = d.rb_boxes[k];
+    if (d.box_err[bi] == 0) place_particle(P, d, d.boxes[bi], t - d.rb_start[k], par);
+  }
+}
+
+// Ahead of the rebuild parts: the boxes that rebuild this step, in box order,
+// and the prefix of their particle counts (a box the rebuild then fails stays
+// in the set; the later parts skip it).  One CTA of 1,024 threads.
 __global__ void __launch_bounds__(1024) k_batch_rebuild_set(Params P, Dev d) {
   __shared__ int carry_n, carry_k;
   __shared__ long long wsum[32];
@@ -368,12 +399,8 @@ __global__ void __launch_bounds__(128) k_batch_list(Params P, Dev d) {
   if (nb == 0) return;
   const int total = d.rb_start[nb];
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-    int lo = 0, hi = nb - 1;  // the box whose slots hold t: rb_start[k] <= t < rb_start[k + 1]
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (d.rb_start[mid] <= t) lo = mid; else hi = mid - 1;
-    }
-    const int bi = d.rb_boxes[lo];
+    const int lo = rb_find(d, nb, t), bi = d.rb_boxes[lo];
+    if (d.box_err[bi] == kErrBadState) continue;
     const BoxDesc &b = d.boxes[bi];
     const int cnt = build_row(P, d, b, bi, t - d.rb_start[lo]);
     if (cnt > P.list_cap) {
@@ -504,7 +531,7 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
 
 // The advance of every box by one step, one persistent kernel: each CTA
 // steps its boxes in turn.  The lists of the boxes that rebuilt this step
-// were made by k_batch_prep and k_batch_list just before.
+// were made by the rebuild kernels just before.
 // Resident 512-thread blocks per SM the mixed step is compiled for: 2 (64
 // registers) measured 9 % faster on 1,024 boxes than 3 (40 registers); the
 // FP64 form stays at 2 (it spills at 40 registers).
@@ -781,8 +808,10 @@ int alloc_batch_list(mdg_batch *b, int cap) {
 void launch_batch_step(mdg_batch *b, int par) {
   const int T = b->threads;
   const bool mixed = b->prm.precision == MDG_MIXED;
-  k_batch_prep<<<b->nbox, kPrepThreads, 0, b->stream>>>(b->P, b->d, par);
   k_batch_rebuild_set<<<1, 1024, 0, b->stream>>>(b->P, b->d);
+  k_batch_bin<<<b->num_sms * 16, 128, 0, b->stream>>>(b->d);
+  k_batch_sort<<<b->nbox, kPrepThreads, 0, b->stream>>>(b->d);
+  k_batch_place<<<b->num_sms * 16, 128, 0, b->stream>>>(b->P, b->d, par);
   k_batch_list<<<b->num_sms * 16, 128, 0, b->stream>>>(b->P, b->d);
 #define MDG_BSTEP(M, L, I) k_batch_step<M, L, I><<<b->grid, T, 0, b->stream>>>(b->P, b->d, par)
   const bool inner = b->P.inner && b->lpi == 1 && b->use_inner;
@@ -794,7 +823,7 @@ void launch_batch_step(mdg_batch *b, int par) {
     else if (inner) MDG_BSTEP(0, 1, 1); else MDG_BSTEP(0, 1, 0);
   }
 #undef MDG_BSTEP
-  b->launches += 4;
+  b->launches += kBatchKernelsPerStep;
 }
 
 int run_steps(mdg_batch *b, int nsteps) {
@@ -822,7 +851,7 @@ int run_steps(mdg_batch *b, int nsteps) {
         if (e != cudaSuccess) return bfail(b, MDG_ERR_CUDA, cudaGetErrorString(e));
       }
       MDG_BCK(cudaGraphLaunch(b->gx[par], b->stream));
-      b->launches += 8;
+      b->launches += 2 * kBatchKernelsPerStep;
       left -= 2;
     } else {
       launch_batch_step(b, par);
