@@ -52,6 +52,9 @@ constexpr int kT = 128;
 #define MDG_ADJ_LANES 8
 #endif
 constexpr int kLanes = MDG_ADJ_LANES;
+// Lanes sharing one particle in the list build (a warp: the build's float
+// test is light, so it needs many warps per SM to hide its load latency).
+constexpr int kBuildLanes = 32;
 
 struct P {
   double L[3];
@@ -237,11 +240,11 @@ __device__ __forceinline__ double lane_sum(double v) {
 }
 
 // Pair list at positions q (wrapped into the box): every partner within the
-// list radius, minimum image.  kLanes lanes share a particle: lane l tests
-// partners j = l, l + kLanes, ... (a particle's lanes read neighbouring
-// positions together), first counting, then writing at its offset in the row
-// (a prefix sum over the lanes), so the row order is fixed: lane 0's partners,
-// then lane 1's, ...  The test runs in float against a radius widened by 1e-3
+// list radius, minimum image.  kBuildLanes lanes share a particle: lane l
+// tests partners j = l, l + kBuildLanes, ... (a particle's lanes read
+// neighbouring positions together), first counting, then writing at its
+// offset in the row (a prefix sum over the lanes), so the row order is fixed:
+// lane 0's partners, then lane 1's, ...  The test runs in float against a radius widened by 1e-3
 // (float positions of a box of tens of sigma are within 1e-5), so every pair
 // within the exact radius is listed; a few more do no harm (the pair terms cut
 // at rc).  The float positions come from d.qf (k_wrap writes them), so a
@@ -250,7 +253,7 @@ __device__ __forceinline__ double lane_sum(double v) {
 // {-1, 0, 1} for wrapped positions.
 __global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = tid / kLanes, lane = tid % kLanes;
+  const int i = tid / kBuildLanes, lane = tid % kBuildLanes;
   const bool active = i < c.n;
   float qx = 0.f, qy = 0.f, qz = 0.f;
   if (active) {
@@ -272,20 +275,20 @@ __global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
   };
   int m = 0;
   if (active)
-    for (int j = lane; j < c.n; j += kLanes) m += within(j) ? 1 : 0;
+    for (int j = lane; j < c.n; j += kBuildLanes) m += within(j) ? 1 : 0;
   // offsets of the lanes' partners in the row
   int incl = m;
 #pragma unroll
-  for (int o = 1; o < kLanes; o <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, incl, o, kLanes);
+  for (int o = 1; o < kBuildLanes; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o, kBuildLanes);
     if (lane >= o) incl += v;
   }
-  const int total = __shfl_sync(0xffffffffu, incl, kLanes - 1, kLanes);
+  const int total = __shfl_sync(0xffffffffu, incl, kBuildLanes - 1, kBuildLanes);
   if (active) {
     int w = incl - m;
     uint32_t *row = d.nbr + (size_t)i * c.cap;
     const double4_32a qi = q[i];
-    for (int j = lane; j < c.n; j += kLanes)
+    for (int j = lane; j < c.n; j += kBuildLanes)
       if (within(j)) {
         if (w < c.cap) {
           const double4_32a v = q[j];
@@ -550,6 +553,7 @@ struct mdg_adjoint {
   cudaStream_t s = nullptr;
   int grid = 1;    // one thread per particle
   int gridp = 1;   // kLanes threads per particle (pair kernels)
+  int gridb = 1;   // kBuildLanes threads per particle (list build)
   int nck = 0;
   bool forward_done = false;
   // the device work of a forward and of a backward pass, captured once and
@@ -608,7 +612,7 @@ int enqueue_forward(mdg_adjoint *a) {
       MDG_ACK(cudaMemcpyAsync(d.ckq + N * ck, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
       MDG_ACK(cudaMemcpyAsync(d.ckp + N * ck, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
       MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
-      k_build<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.q);
+      k_build<<<a->gridb, kT, 0, a->s>>>(a->c, d, d.q);
       k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.p, d.qh);
     }
     // the next step's half-drift here unless a segment starts there (as the
@@ -638,7 +642,7 @@ int enqueue_backward(mdg_adjoint *a) {
     // the segment's list, built from the same state as in the forward pass
     MDG_ACK(cudaMemcpyAsync(d.q0, d.segq, bytes, cudaMemcpyDeviceToDevice, a->s));
     k_wrap<<<a->grid, kT, 0, a->s>>>(a->c, d.segq, d.qf, 0);
-    k_build<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segq);
+    k_build<<<a->gridb, kT, 0, a->s>>>(a->c, d, d.segq);
     k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.segq, d.segp, d.segqh + N);
     for (int k = 1; k <= len; k++)
       fwd_step(a, d.segqh + N * k, d.segp + N * (k - 1), d.segq + N * k, d.segp + N * k,
@@ -741,6 +745,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   c.cap = ((int)(rho * 4.18879020478639 * sl * sl * sl * 1.5 + 32) + 7) & ~7;
   a->grid = (n + kT - 1) / kT;
   a->gridp = (int)(((long long)n * kLanes + kT - 1) / kT);
+  a->gridb = (int)(((long long)n * kBuildLanes + kT - 1) / kT);
   a->nck = p->steps / p->checkpoint_every + 1;
   const size_t N = (size_t)n, K = (size_t)p->checkpoint_every;
   D &d = a->d;
