@@ -37,6 +37,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "mdg_internal.cuh"
@@ -80,7 +81,7 @@ constexpr int kImageBits = 6;
 constexpr int kMaxAdjointParticles = 1 << (32 - kImageBits);
 
 struct D {
-  double4_32a *q, *p, *qh, *F, *aq, *ap, *aqh, *tmp, *q0;
+  double4_32a *q, *p, *qh, *qh2, *aq, *ap, *aqh, *tmp, *q0;
   double4_32a *ckq, *ckp;    // checkpoints
   float4 *qf;                // float copy of the segment's first state (the list test)
   double4_32a *segq, *segp, *segqh;  // recomputed segment
@@ -306,14 +307,21 @@ __global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
   }
 }
 
-// Forces at the half-step positions q; also the segment's displacement check
+// One step from the half-step positions q: the forces F there (the lanes of
+// a particle), then, by its lane 0, p_out = p_in + F dt, q_out = q + p_out dt/2
+// and, when qh_next is given, the next step's first half-drift
+// qh_next = q_out + p_out dt/2 (the operations k_drift performs).  Out of
+// place: q_out and qh_next must not alias q, which other particles' lanes
+// still read; p_out may alias p_in.  Also the segment's displacement check
 // (a particle more than margin/2 from where the segment's list was built).
-__global__ void k_force(P c, D d, const double4_32a *q, double4_32a *F) {
+__global__ void k_step(P c, D d, const double4_32a *q, const double4_32a *p_in, double4_32a *q_out,
+                       double4_32a *p_out, double4_32a *qh_next) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
   double fx = 0, fy = 0, fz = 0;
+  double4_32a qi = make_double4_32a(0.0, 0.0, 0.0, 0.0);
   if (i < c.n) {
-    const double4_32a qi = q[i];
+    qi = q[i];
     if (lane == 0) {
       const double4_32a z = d.q0[i];
       const double ux = qi.x - z.x, uy = qi.y - z.y, uz = qi.z - z.z;
@@ -329,7 +337,24 @@ __global__ void k_force(P c, D d, const double4_32a *q, double4_32a *F) {
   fx = lane_sum(fx);
   fy = lane_sum(fy);
   fz = lane_sum(fz);
-  if (i < c.n && lane == 0) F[i] = make_double4_32a(fx, fy, fz, 0.0);
+  if (i < c.n && lane == 0) {
+    double4_32a b = p_in[i];
+    b.x += fx * c.dt;
+    b.y += fy * c.dt;
+    b.z += fz * c.dt;
+    p_out[i] = b;
+    double4_32a a = qi;
+    a.x += b.x * c.dt2;
+    a.y += b.y * c.dt2;
+    a.z += b.z * c.dt2;
+    q_out[i] = a;
+    if (qh_next) {
+      a.x += b.x * c.dt2;
+      a.y += b.y * c.dt2;
+      a.z += b.z * c.dt2;
+      qh_next[i] = a;
+    }
+  }
 }
 
 // qh = q + p dt/2: the first half-drift of a trajectory or segment
@@ -362,38 +387,12 @@ __global__ void k_wrap(P c, double4_32a *q, float4 *qf, int wrap) {
   qf[i] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.f);
 }
 
-// p_out = p_in + F dt; q_out = qh + p_out dt/2; and, when qh_next is given,
-// the next step's first half-drift qh_next = q_out + p_out dt/2 (the same
-// operations k_drift performs).  Out of place, so a recomputed segment writes
-// step k from step k - 1 without copies; qh_next may alias qh.
-__global__ void k_kick_drift(P c, const double4_32a *qh, const double4_32a *F, const double4_32a *p_in,
-                             double4_32a *q_out, double4_32a *p_out, double4_32a *qh_next) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= c.n) return;
-  double4_32a b = p_in[i];
-  const double4_32a f = F[i];
-  b.x += f.x * c.dt;
-  b.y += f.y * c.dt;
-  b.z += f.z * c.dt;
-  p_out[i] = b;
-  double4_32a a = qh[i];
-  a.x += b.x * c.dt2;
-  a.y += b.y * c.dt2;
-  a.z += b.z * c.dt2;
-  q_out[i] = a;
-  if (qh_next) {
-    a.x += b.x * c.dt2;
-    a.y += b.y * c.dt2;
-    a.z += b.z * c.dt2;
-    qh_next[i] = a;
-  }
-}
-
 // Objective j at (q, p) into partials (value, d/deps, d/dsigma); with GRAD,
 // also adds w * dj/dq to aq and w * dj/dp to ap (w = 1/Ns).  OBJ and GRAD are
-// template parameters so that each pass computes only the pair terms it uses
-// (the forward pass of the potential-energy objective needs phi and its sigma
-// derivative alone).
+// template parameters so that each pass computes only the pair terms it uses:
+// the forward pass returns J alone (the parameter terms of the gradient are
+// summed in the backward pass), so without GRAD the sigma derivative is left
+// out and its partial is zero.
 template <int OBJ, int GRAD>
 __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p, double w) {
   constexpr bool grad = GRAD != 0;
@@ -408,7 +407,7 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
     for_pairs(c, d, i, lane, q, h, [&](const PairTerms &t, double dx, double dy, double dz, int) {
       if (OBJ == 0) {
         u += 0.5 * t.phi;
-        us += 0.5 * t.dphis;
+        if (grad) us += 0.5 * t.dphis;
         if (grad) {
           gx -= t.f * dx;  // dU/dq_i = -F_i
           gy -= t.f * dy;
@@ -416,7 +415,7 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
         }
       } else {
         G += 0.5 * t.g;
-        Gs += 0.5 * t.gs;
+        if (grad) Gs += 0.5 * t.gs;
         if (grad) {
           gx += t.gpr * dx;  // dG/dq_i = -sum g'(r) d/r;  dP/dq_i = -(1/3V) dG/dq_i
           gy += t.gpr * dy;
@@ -589,11 +588,10 @@ void launch_objective(mdg_adjoint *a, const double4_32a *q, const double4_32a *p
 }
 
 // One step from the half-step positions qh (already drifted from step k - 1)
-// and p_in: forces, then q_out, p_out and, when given, the next step's qh.
+// and p_in: q_out, p_out and, when given, the next step's qh (not qh itself).
 void fwd_step(mdg_adjoint *a, const double4_32a *qh, const double4_32a *p_in, double4_32a *q_out,
               double4_32a *p_out, double4_32a *qh_next) {
-  k_force<<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, a->d.F);
-  k_kick_drift<<<a->grid, kT, 0, a->s>>>(a->c, qh, a->d.F, p_in, q_out, p_out, qh_next);
+  k_step<<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, p_in, q_out, p_out, qh_next);
 }
 
 // The horizon from the state in d.q, d.p: per segment its list, per step the
@@ -605,6 +603,7 @@ int enqueue_forward(mdg_adjoint *a) {
   MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
   const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
   const double w = 1.0 / Ns;
+  double4_32a *qh = d.qh, *qh_alt = d.qh2;  // half-step positions, written out of place
   for (int n = 1; n <= Ns; n++) {
     if ((n - 1) % K == 0) {  // a checkpoint segment starts: wrapped state, checkpoint, its own list
       const size_t ck = (size_t)((n - 1) / K);
@@ -613,11 +612,13 @@ int enqueue_forward(mdg_adjoint *a) {
       MDG_ACK(cudaMemcpyAsync(d.ckp + N * ck, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
       MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
       k_build<<<a->gridb, kT, 0, a->s>>>(a->c, d, d.q);
-      k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.p, d.qh);
+      k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.p, qh);
     }
     // the next step's half-drift here unless a segment starts there (as the
     // backward pass recomputes it: from the wrapped checkpoint)
-    fwd_step(a, d.qh, d.p, d.q, d.p, n < Ns && n % K != 0 ? d.qh : nullptr);
+    double4_32a *next = n < Ns && n % K != 0 ? qh_alt : nullptr;
+    fwd_step(a, qh, d.p, d.q, d.p, next);
+    if (next) std::swap(qh, qh_alt);
     launch_objective(a, d.q, d.p, false, w);
   }
   return cudaGetLastError() == cudaSuccess ? MDG_OK : afail(a, MDG_ERR_CUDA, "adjoint forward launch failed");
@@ -751,7 +752,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   D &d = a->d;
   cudaError_t e = cudaSetDevice(p->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->s, cudaStreamNonBlocking);
-  double4_32a **vecs[] = {&d.q, &d.p, &d.qh, &d.F, &d.aq, &d.ap, &d.aqh, &d.tmp, &d.q0};
+  double4_32a **vecs[] = {&d.q, &d.p, &d.qh, &d.qh2, &d.aq, &d.ap, &d.aqh, &d.tmp, &d.q0};
   for (auto v : vecs)
     if (e == cudaSuccess) e = aalloc(v, N);
   if (e == cudaSuccess) e = aalloc(&d.ckq, N * a->nck);
@@ -783,7 +784,7 @@ int mdg_adjoint_destroy(mdg_adjoint *a) {
   if (a->gx_forward) cudaGraphExecDestroy(a->gx_forward);
   if (a->gx_backward) cudaGraphExecDestroy(a->gx_backward);
   D &d = a->d;
-  void *ptrs[] = {d.q, d.p, d.qh, d.F, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
+  void *ptrs[] = {d.q, d.p, d.qh, d.qh2, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
                   d.nbr, d.cnt, d.qf, d.part, d.acc, d.flag, d.done};
   for (void *p : ptrs)
     if (p) cudaFree(p);
