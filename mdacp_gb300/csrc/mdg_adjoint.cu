@@ -387,8 +387,21 @@ __global__ void k_wrap(P c, double4_32a *q, float4 *qf, int wrap) {
   qf[i] = make_float4((float)a.x, (float)a.y, (float)a.z, 0.f);
 }
 
+// The reverse of a step's second half-drift q_n = qh + dt/2 p_n for particle
+// i, from the adjoints a, b of (q_n, p_n): a_p += dt/2 a_q.  tmp receives the
+// adjoint of p after the kick (the neighbours' H v reads it), aqh that of qh.
+__device__ __forceinline__ void reverse_drift(const P &c, const D &d, int i, const double4_32a &a, double4_32a b) {
+  b.x += c.dt2 * a.x;
+  b.y += c.dt2 * a.y;
+  b.z += c.dt2 * a.z;
+  d.tmp[i] = b;
+  d.aqh[i] = a;
+}
+
 // Objective j at (q, p) into partials (value, d/deps, d/dsigma); with GRAD,
-// also adds w * dj/dq to aq and w * dj/dp to ap (w = 1/Ns).  OBJ and GRAD are
+// also adds w * dj/dq and w * dj/dp (w = 1/Ns) to the adjoints aq, ap of
+// state n and applies the reverse of step n's second half-drift (into tmp
+// and aqh, which k_reverse_hvp takes up).  OBJ and GRAD are
 // template parameters so that each pass computes only the pair terms it uses:
 // the forward pass returns J alone (the parameter terms of the gradient are
 // summed in the backward pass), so without GRAD the sigma derivative is left
@@ -449,7 +462,7 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
         a.x += w * gx * inv_n;
         a.y += w * gy * inv_n;
         a.z += w * gz * inv_n;
-        d.aq[i] = a;
+        reverse_drift(c, d, i, a, d.ap[i]);
       }
     } else {
       const double inv3v = 1.0 / (3.0 * c.volume);
@@ -464,8 +477,7 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
         b.x += w * 2.0 * pi.x * inv3v;
         b.y += w * 2.0 * pi.y * inv3v;
         b.z += w * 2.0 * pi.z * inv3v;
-        d.aq[i] = a;
-        d.ap[i] = b;
+        reverse_drift(c, d, i, a, b);
       }
     }
   }
@@ -473,22 +485,10 @@ __global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p
   partials_accumulate(d, val, ge, gs, w);
 }
 
-// Reverse of one step at half-step positions qh.  In: aq, ap adjoints of
-// (q_{n}, p_{n}).  Out: aq, ap adjoints of (q_{n-1}, p_{n-1}); parameter terms
+// The rest of the reverse of one step at half-step positions qh (kick and
+// first half-drift).  In: tmp, aqh from the reverse of its second half-drift
+// (k_objective).  Out: aq, ap adjoints of (q_{n-1}, p_{n-1}); parameter terms
 // dt * ap . dF/dtheta into partials (slots 1, 2).
-__global__ void k_reverse(P c, D d) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < c.n) {
-    double4_32a a = d.aq[i], b = d.ap[i];
-    // drift q_n = qh + dt/2 p_n : a_p += dt/2 a_q  (done per particle, a_q unchanged)
-    b.x += c.dt2 * a.x;
-    b.y += c.dt2 * a.y;
-    b.z += c.dt2 * a.z;
-    d.tmp[i] = b;  // adjoint of p after the kick, needed by the neighbours' H v
-    d.aqh[i] = a;
-  }
-}
-
 __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
   __shared__ double sh[96];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -649,10 +649,10 @@ int enqueue_backward(mdg_adjoint *a) {
       fwd_step(a, d.segqh + N * k, d.segp + N * (k - 1), d.segq + N * k, d.segp + N * k,
                k < len ? d.segqh + N * (k + 1) : nullptr);
     for (int k = len; k >= 1; k--) {
-      // objective terms of state (seg_start + k)
+      // objective terms of state (seg_start + k) and the reverse of the
+      // second half-drift of the step that produced it, then the rest of
+      // that step's reverse
       launch_objective(a, d.segq + N * k, d.segp + N * k, true, w);
-      // reverse the step that produced it
-      k_reverse<<<a->grid, kT, 0, a->s>>>(a->c, d);
       k_reverse_hvp<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segqh + N * k);
     }
     seg_end = seg_start;
