@@ -77,3 +77,25 @@ def test_python_manager_reports_the_create_reason():
     from mdacp_gb300.manager import MDManager
     with pytest.raises(native.MDGError, match="dt must be"):
         MDManager(20.0, capacity=100, dt=0.0)
+
+
+def test_adjoint_create_checks_before_device_use(lib):
+    # particle count (list entries hold the index in 26 bits), box size
+    # against 2 (cutoff sigma + margin) and the step parameters are checked
+    # before any device call
+    import mdacp_gb300.adjoint as adj
+    L = adj._lib()
+    p = adj.AdjointParams()
+    L.mdg_adjoint_params_default(ctypes.byref(p))
+    p.box[:] = [20.0, 20.0, 20.0]
+    p.margin = 0.5
+    h = ctypes.c_void_p()
+    for n in (1, 1 << 26):
+        assert L.mdg_adjoint_create(ctypes.byref(p), n, ctypes.byref(h)) == 1
+        assert not h.value
+    p.box[:] = [5.9, 20.0, 20.0]  # below 2 (2.5 + 0.5)
+    assert L.mdg_adjoint_create(ctypes.byref(p), 4000, ctypes.byref(h)) == 1
+    p.box[:] = [20.0, 20.0, 20.0]
+    p.checkpoint_every = 0
+    assert L.mdg_adjoint_create(ctypes.byref(p), 4000, ctypes.byref(h)) == 1
+    assert not h.value
