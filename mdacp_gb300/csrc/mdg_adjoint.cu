@@ -81,7 +81,7 @@ constexpr int kImageBits = 6;
 constexpr int kMaxAdjointParticles = 1 << (32 - kImageBits);
 
 struct D {
-  double4_32a *q, *p, *qh, *qh2, *aq, *ap, *aqh, *tmp, *q0;
+  double4_32a *q, *q2, *p, *qh, *qh2, *aq, *ap, *aqh, *tmp, *q0;
   double4_32a *ckq, *ckp;    // checkpoints
   float4 *qf;                // float copy of the segment's first state (the list test)
   double4_32a *segq, *segp, *segqh;  // recomputed segment
@@ -314,11 +314,18 @@ __global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
 // place: q_out and qh_next must not alias q, which other particles' lanes
 // still read; p_out may alias p_in.  Also the segment's displacement check
 // (a particle more than margin/2 from where the segment's list was built).
+// With VAL = 0 or 1 (the potential-energy or pressure objective) the kernel
+// also adds w times the objective's value at the previous whole-step state
+// (q_obj, p_in) to acc[0], as k_objective<VAL, 0> does (same row walk, lanes
+// and reductions, so the same bits); q_obj must be in this step's segment.
+template <int VAL>
 __global__ void k_step(P c, D d, const double4_32a *q, const double4_32a *p_in, double4_32a *q_out,
-                       double4_32a *p_out, double4_32a *qh_next) {
+                       double4_32a *p_out, double4_32a *qh_next, const double4_32a *q_obj, double w) {
+  __shared__ double sh[96];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
   double fx = 0, fy = 0, fz = 0;
+  double u = 0, G = 0;
   double4_32a qi = make_double4_32a(0.0, 0.0, 0.0, 0.0);
   if (i < c.n) {
     qi = q[i];
@@ -333,12 +340,24 @@ __global__ void k_step(P c, D d, const double4_32a *q, const double4_32a *p_in, 
       fy += t.f * dy;
       fz += t.f * dz;
     });
+    if (VAL >= 0) {
+      const Home ho = make_home(c, q_obj[i]);
+      for_pairs(c, d, i, lane, q_obj, ho, [&](const PairTerms &t, double, double, double, int) {
+        if (VAL == 0) u += 0.5 * t.phi;
+        else G += 0.5 * t.g;
+      });
+    }
   }
   fx = lane_sum(fx);
   fy = lane_sum(fy);
   fz = lane_sum(fz);
+  double val = 0.0;
+  if (VAL == 0) u = lane_sum(u);
+  if (VAL == 1) G = lane_sum(G);
   if (i < c.n && lane == 0) {
     double4_32a b = p_in[i];
+    if (VAL == 0) val = u * (1.0 / (double)c.n);
+    if (VAL == 1) val = (2.0 * (0.5 * (b.x * b.x + b.y * b.y + b.z * b.z)) - G) * (1.0 / (3.0 * c.volume));
     b.x += fx * c.dt;
     b.y += fy * c.dt;
     b.z += fz * c.dt;
@@ -354,6 +373,11 @@ __global__ void k_step(P c, D d, const double4_32a *q, const double4_32a *p_in, 
       a.z += b.z * c.dt2;
       qh_next[i] = a;
     }
+  }
+  if (VAL >= 0) {
+    double none1 = 0.0, none2 = 0.0;
+    block_sum3(val, none1, none2, sh);
+    partials_accumulate(d, val, 0.0, 0.0, w);
   }
 }
 
@@ -588,10 +612,16 @@ void launch_objective(mdg_adjoint *a, const double4_32a *q, const double4_32a *p
 }
 
 // One step from the half-step positions qh (already drifted from step k - 1)
-// and p_in: q_out, p_out and, when given, the next step's qh (not qh itself).
+// and p_in: q_out, p_out and, when given, the next step's qh (not qh itself);
+// with q_obj, also w times the objective's value at (q_obj, p_in).
 void fwd_step(mdg_adjoint *a, const double4_32a *qh, const double4_32a *p_in, double4_32a *q_out,
-              double4_32a *p_out, double4_32a *qh_next) {
-  k_step<<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, p_in, q_out, p_out, qh_next);
+              double4_32a *p_out, double4_32a *qh_next, const double4_32a *q_obj = nullptr, double w = 0.0) {
+  if (!q_obj)
+    k_step<-1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, p_in, q_out, p_out, qh_next, nullptr, 0.0);
+  else if (a->c.objective == 0)
+    k_step<0><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, p_in, q_out, p_out, qh_next, q_obj, w);
+  else
+    k_step<1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, p_in, q_out, p_out, qh_next, q_obj, w);
 }
 
 // The horizon from the state in d.q, d.p: per segment its list, per step the
@@ -603,23 +633,28 @@ int enqueue_forward(mdg_adjoint *a) {
   MDG_ACK(cudaMemsetAsync(d.acc, 0, 3 * sizeof(double), a->s));
   const int Ns = a->prm.steps, K = a->prm.checkpoint_every;
   const double w = 1.0 / Ns;
-  double4_32a *qh = d.qh, *qh_alt = d.qh2;  // half-step positions, written out of place
+  // half-step and whole-step positions, both written out of place
+  double4_32a *qh = d.qh, *qh_alt = d.qh2, *q = d.q, *q_alt = d.q2;
   for (int n = 1; n <= Ns; n++) {
     if ((n - 1) % K == 0) {  // a checkpoint segment starts: wrapped state, checkpoint, its own list
       const size_t ck = (size_t)((n - 1) / K);
-      k_wrap<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.qf, 1);
-      MDG_ACK(cudaMemcpyAsync(d.ckq + N * ck, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
+      k_wrap<<<a->grid, kT, 0, a->s>>>(a->c, q, d.qf, 1);
+      MDG_ACK(cudaMemcpyAsync(d.ckq + N * ck, q, bytes, cudaMemcpyDeviceToDevice, a->s));
       MDG_ACK(cudaMemcpyAsync(d.ckp + N * ck, d.p, bytes, cudaMemcpyDeviceToDevice, a->s));
-      MDG_ACK(cudaMemcpyAsync(d.q0, d.q, bytes, cudaMemcpyDeviceToDevice, a->s));
-      k_build<<<a->gridb, kT, 0, a->s>>>(a->c, d, d.q);
-      k_drift<<<a->grid, kT, 0, a->s>>>(a->c, d.q, d.p, qh);
+      MDG_ACK(cudaMemcpyAsync(d.q0, q, bytes, cudaMemcpyDeviceToDevice, a->s));
+      k_build<<<a->gridb, kT, 0, a->s>>>(a->c, d, q);
+      k_drift<<<a->grid, kT, 0, a->s>>>(a->c, q, d.p, qh);
     }
     // the next step's half-drift here unless a segment starts there (as the
-    // backward pass recomputes it: from the wrapped checkpoint)
+    // backward pass recomputes it: from the wrapped checkpoint); the
+    // objective of state n - 1 rides along when that state is in this
+    // step's segment (the states are summed in order either way)
     double4_32a *next = n < Ns && n % K != 0 ? qh_alt : nullptr;
-    fwd_step(a, qh, d.p, d.q, d.p, next);
+    fwd_step(a, qh, d.p, q_alt, d.p, next, n > 1 && (n - 1) % K != 0 ? q : nullptr, w);
+    std::swap(q, q_alt);
     if (next) std::swap(qh, qh_alt);
-    launch_objective(a, d.q, d.p, false, w);
+    // the last state of a segment (or of the horizon) with its own list
+    if (n % K == 0 || n == Ns) launch_objective(a, q, d.p, false, w);
   }
   return cudaGetLastError() == cudaSuccess ? MDG_OK : afail(a, MDG_ERR_CUDA, "adjoint forward launch failed");
 }
@@ -752,7 +787,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   D &d = a->d;
   cudaError_t e = cudaSetDevice(p->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->s, cudaStreamNonBlocking);
-  double4_32a **vecs[] = {&d.q, &d.p, &d.qh, &d.qh2, &d.aq, &d.ap, &d.aqh, &d.tmp, &d.q0};
+  double4_32a **vecs[] = {&d.q, &d.q2, &d.p, &d.qh, &d.qh2, &d.aq, &d.ap, &d.aqh, &d.tmp, &d.q0};
   for (auto v : vecs)
     if (e == cudaSuccess) e = aalloc(v, N);
   if (e == cudaSuccess) e = aalloc(&d.ckq, N * a->nck);
@@ -784,7 +819,7 @@ int mdg_adjoint_destroy(mdg_adjoint *a) {
   if (a->gx_forward) cudaGraphExecDestroy(a->gx_forward);
   if (a->gx_backward) cudaGraphExecDestroy(a->gx_backward);
   D &d = a->d;
-  void *ptrs[] = {d.q, d.p, d.qh, d.qh2, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
+  void *ptrs[] = {d.q, d.q2, d.p, d.qh, d.qh2, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
                   d.nbr, d.cnt, d.qf, d.part, d.acc, d.flag, d.done};
   for (void *p : ptrs)
     if (p) cudaFree(p);
