@@ -81,7 +81,7 @@ constexpr int kImageBits = 6;
 constexpr int kMaxAdjointParticles = 1 << (32 - kImageBits);
 
 struct D {
-  double4_32a *q, *q2, *p, *qh, *qh2, *aq, *ap, *aqh, *tmp, *q0;
+  double4_32a *q, *q2, *p, *qh, *qh2, *aq, *ap, *aqh, *tmp, *tmp2, *q0;
   double4_32a *ckq, *ckp;    // checkpoints
   float4 *qf;                // float copy of the segment's first state (the list test)
   double4_32a *segq, *segp, *segqh;  // recomputed segment
@@ -414,12 +414,93 @@ __global__ void k_wrap(P c, double4_32a *q, float4 *qf, int wrap) {
 // The reverse of a step's second half-drift q_n = qh + dt/2 p_n for particle
 // i, from the adjoints a, b of (q_n, p_n): a_p += dt/2 a_q.  tmp receives the
 // adjoint of p after the kick (the neighbours' H v reads it), aqh that of qh.
-__device__ __forceinline__ void reverse_drift(const P &c, const D &d, int i, const double4_32a &a, double4_32a b) {
+__device__ __forceinline__ void reverse_drift(const P &c, const D &d, int i, const double4_32a &a, double4_32a b,
+                                              double4_32a *tmp) {
   b.x += c.dt2 * a.x;
   b.y += c.dt2 * a.y;
   b.z += c.dt2 * a.z;
-  d.tmp[i] = b;
+  tmp[i] = b;
   d.aqh[i] = a;
+}
+
+// Particle i's pair sums of the objective at positions q (every lane holds
+// them after the lane sums; all threads of the block call it).
+struct ObjSums {
+  double u, us, G, Gs, gx, gy, gz;
+};
+
+template <int OBJ, bool GRAD>
+__device__ __forceinline__ ObjSums objective_sums(const P &c, const D &d, int i, int lane, const double4_32a *q) {
+  ObjSums r{0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (i < c.n) {
+    const Home h = make_home(c, q[i]);
+    for_pairs(c, d, i, lane, q, h, [&](const PairTerms &t, double dx, double dy, double dz, int) {
+      if (OBJ == 0) {
+        r.u += 0.5 * t.phi;
+        if (GRAD) {
+          r.us += 0.5 * t.dphis;
+          r.gx -= t.f * dx;  // dU/dq_i = -F_i
+          r.gy -= t.f * dy;
+          r.gz -= t.f * dz;
+        }
+      } else {
+        r.G += 0.5 * t.g;
+        if (GRAD) {
+          r.Gs += 0.5 * t.gs;
+          r.gx += t.gpr * dx;  // dG/dq_i = -sum g'(r) d/r;  dP/dq_i = -(1/3V) dG/dq_i
+          r.gy += t.gpr * dy;
+          r.gz += t.gpr * dz;
+        }
+      }
+    });
+  }
+  if (GRAD) {
+    r.gx = lane_sum(r.gx);
+    r.gy = lane_sum(r.gy);
+    r.gz = lane_sum(r.gz);
+  }
+  if (OBJ == 0) {
+    r.u = lane_sum(r.u);
+    if (GRAD) r.us = lane_sum(r.us);
+  } else {
+    r.G = lane_sum(r.G);
+    if (GRAD) r.Gs = lane_sum(r.Gs);
+  }
+  return r;
+}
+
+// Particle i's objective terms from its sums (lane 0): the value and its
+// epsilon and sigma derivatives; with GRAD, w dj/dq added to a and w dj/dp
+// to b (the adjoints of the state's q and p).
+template <int OBJ, bool GRAD>
+__device__ __forceinline__ void objective_finish(const P &c, const ObjSums &r, const double4_32a &pi, double w,
+                                                 double &val, double &ge, double &gs, double4_32a &a,
+                                                 double4_32a &b) {
+  if (OBJ == 0) {
+    const double inv_n = 1.0 / (double)c.n;
+    val = r.u * inv_n;
+    ge = r.u / c.eps * inv_n;
+    gs = r.us * inv_n;
+    if (GRAD) {
+      a.x += w * r.gx * inv_n;
+      a.y += w * r.gy * inv_n;
+      a.z += w * r.gz * inv_n;
+    }
+  } else {
+    const double ke = 0.5 * (pi.x * pi.x + pi.y * pi.y + pi.z * pi.z);
+    const double inv3v = 1.0 / (3.0 * c.volume);
+    val = (2.0 * ke - r.G) * inv3v;
+    ge = -r.G / c.eps * inv3v;
+    gs = -r.Gs * inv3v;
+    if (GRAD) {
+      a.x += w * r.gx * inv3v;
+      a.y += w * r.gy * inv3v;
+      a.z += w * r.gz * inv3v;
+      b.x += w * 2.0 * pi.x * inv3v;
+      b.y += w * 2.0 * pi.y * inv3v;
+      b.z += w * 2.0 * pi.z * inv3v;
+    }
+  }
 }
 
 // Objective j at (q, p) into partials (value, d/deps, d/dsigma); with GRAD,
@@ -431,99 +512,48 @@ __device__ __forceinline__ void reverse_drift(const P &c, const D &d, int i, con
 // summed in the backward pass), so without GRAD the sigma derivative is left
 // out and its partial is zero.
 template <int OBJ, int GRAD>
-__global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p, double w) {
+__global__ void k_objective(P c, D d, const double4_32a *q, const double4_32a *p, double w, double4_32a *tmp) {
   constexpr bool grad = GRAD != 0;
   __shared__ double sh[96];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
   double val = 0, ge = 0, gs = 0;
-  double gx = 0, gy = 0, gz = 0, u = 0, us = 0, G = 0, Gs = 0;
-  if (i < c.n) {
-    const double4_32a qi = q[i];
-    const Home h = make_home(c, qi);
-    for_pairs(c, d, i, lane, q, h, [&](const PairTerms &t, double dx, double dy, double dz, int) {
-      if (OBJ == 0) {
-        u += 0.5 * t.phi;
-        if (grad) us += 0.5 * t.dphis;
-        if (grad) {
-          gx -= t.f * dx;  // dU/dq_i = -F_i
-          gy -= t.f * dy;
-          gz -= t.f * dz;
-        }
-      } else {
-        G += 0.5 * t.g;
-        if (grad) Gs += 0.5 * t.gs;
-        if (grad) {
-          gx += t.gpr * dx;  // dG/dq_i = -sum g'(r) d/r;  dP/dq_i = -(1/3V) dG/dq_i
-          gy += t.gpr * dy;
-          gz += t.gpr * dz;
-        }
-      }
-    });
-  }
-  if (grad) {
-    gx = lane_sum(gx);
-    gy = lane_sum(gy);
-    gz = lane_sum(gz);
-  }
-  if (OBJ == 0) {
-    u = lane_sum(u);
-    us = lane_sum(us);
-  } else {
-    G = lane_sum(G);
-    Gs = lane_sum(Gs);
-  }
+  const ObjSums r = objective_sums<OBJ, grad>(c, d, i, lane, q);
   if (i < c.n && lane == 0) {
-    const double4_32a pi = p[i];
-    const double ke = 0.5 * (pi.x * pi.x + pi.y * pi.y + pi.z * pi.z);
-    if (OBJ == 0) {
-      const double inv_n = 1.0 / (double)c.n;
-      val = u * inv_n;
-      ge = u / c.eps * inv_n;
-      gs = us * inv_n;
-      if (grad) {
-        double4_32a a = d.aq[i];
-        a.x += w * gx * inv_n;
-        a.y += w * gy * inv_n;
-        a.z += w * gz * inv_n;
-        reverse_drift(c, d, i, a, d.ap[i]);
-      }
-    } else {
-      const double inv3v = 1.0 / (3.0 * c.volume);
-      val = (2.0 * ke - G) * inv3v;
-      ge = -G / c.eps * inv3v;
-      gs = -Gs * inv3v;
-      if (grad) {
-        double4_32a a = d.aq[i], b = d.ap[i];
-        a.x += w * gx * inv3v;
-        a.y += w * gy * inv3v;
-        a.z += w * gz * inv3v;
-        b.x += w * 2.0 * pi.x * inv3v;
-        b.y += w * 2.0 * pi.y * inv3v;
-        b.z += w * 2.0 * pi.z * inv3v;
-        reverse_drift(c, d, i, a, b);
-      }
+    double4_32a a = make_double4_32a(0.0, 0.0, 0.0, 0.0), b = a;
+    if (grad) {
+      a = d.aq[i];
+      b = d.ap[i];
     }
+    objective_finish<OBJ, grad>(c, r, p[i], w, val, ge, gs, a, b);
+    if (grad) reverse_drift(c, d, i, a, b, tmp);
   }
   block_sum3(val, ge, gs, sh);
   partials_accumulate(d, val, ge, gs, w);
 }
 
-// The rest of the reverse of one step at half-step positions qh (kick and
-// first half-drift).  In: tmp, aqh from the reverse of its second half-drift
-// (k_objective).  Out: aq, ap adjoints of (q_{n-1}, p_{n-1}); parameter terms
-// dt * ap . dF/dtheta into partials (slots 1, 2).
-__global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
+// The rest of the reverse of step n at half-step positions qh (kick and
+// first half-drift).  In: tmp (read by the neighbours too) and aqh from the
+// reverse of its second half-drift.  Out: aq, ap adjoints of (q_{n-1},
+// p_{n-1}); parameter terms dt * ap . dF/dtheta into partials (slots 1, 2).
+// With OBJ = 0 or 1 the kernel goes on with state n - 1 (in the same
+// segment): its objective terms at (q_obj, p_obj), as k_objective<OBJ, 1>
+// computes them, and the reverse of step n - 1's second half-drift, into
+// tmp_out (not tmp: other particles' lanes still read it) and aqh instead of
+// aq, ap.
+template <int OBJ>
+__global__ void k_reverse_hvp(P c, D d, const double4_32a *qh, const double4_32a *tmp, const double4_32a *q_obj,
+                              const double4_32a *p_obj, double w, double4_32a *tmp_out) {
   __shared__ double sh[96];
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = tid / kLanes, lane = tid % kLanes;
   double te = 0, ts = 0;
   double hx = 0, hy = 0, hz = 0, fx = 0, fy = 0, fz = 0, sx = 0, sy = 0, sz = 0;
   if (i < c.n) {
-    const double4_32a qi = qh[i], vi = d.tmp[i];
+    const double4_32a qi = qh[i], vi = tmp[i];
     const Home h = make_home(c, qi);
     for_pairs(c, d, i, lane, qh, h, [&](const PairTerms &t, double dx, double dy, double dz, int j) {
-      const double4_32a vj = d.tmp[j];
+      const double4_32a vj = tmp[j];
       const double wx = vi.x - vj.x, wy = vi.y - vj.y, wz = vi.z - vj.z;
       const double dw = dx * wx + dy * wy + dz * wz;
       // (H v)_i = sum_j f (v_i - v_j) + (f'/r) d (d . (v_i - v_j))
@@ -541,8 +571,11 @@ __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
   hx = lane_sum(hx); hy = lane_sum(hy); hz = lane_sum(hz);
   fx = lane_sum(fx); fy = lane_sum(fy); fz = lane_sum(fz);
   sx = lane_sum(sx); sy = lane_sum(sy); sz = lane_sum(sz);
+  ObjSums r{};
+  if (OBJ >= 0) r = objective_sums<(OBJ >= 0 ? OBJ : 0), true>(c, d, i, lane, q_obj);
+  double val = 0, ge = 0, gs = 0;
   if (i < c.n && lane == 0) {
-    const double4_32a b = d.tmp[i];
+    const double4_32a b = tmp[i];
     // parameter terms: dt * a_p . dF_i/deps (= F_i/eps), dt * a_p . dF_i/dsigma
     te = c.dt * (b.x * fx + b.y * fy + b.z * fz) / c.eps;
     ts = c.dt * (b.x * sx + b.y * sy + b.z * sz);
@@ -555,12 +588,18 @@ __global__ void k_reverse_hvp(P c, D d, const double4_32a *qh) {
     pb.x += c.dt2 * a.x;
     pb.y += c.dt2 * a.y;
     pb.z += c.dt2 * a.z;
-    d.aq[i] = a;
-    d.ap[i] = pb;
+    if (OBJ >= 0) {
+      objective_finish<(OBJ >= 0 ? OBJ : 0), true>(c, r, p_obj[i], w, val, ge, gs, a, pb);
+      reverse_drift(c, d, i, a, pb, tmp_out);
+    } else {
+      d.aq[i] = a;
+      d.ap[i] = pb;
+    }
   }
-  double none = 0.0;
-  block_sum3(none, te, ts, sh);
-  partials_accumulate(d, 0.0, te, ts, 1.0);
+  // the objective's partials carry the weight w, the kick terms 1
+  double A = w * val, B = te + w * ge, E = ts + w * gs;
+  block_sum3(A, B, E, sh);
+  partials_accumulate(d, A, B, E, 1.0);
 }
 
 }  // namespace adj
@@ -603,12 +642,24 @@ cudaError_t aalloc(T **p, size_t n) {
   return cudaMalloc((void **)p, (n ? n : 1) * sizeof(T));
 }
 
-void launch_objective(mdg_adjoint *a, const double4_32a *q, const double4_32a *p, bool grad, double w) {
+void launch_objective(mdg_adjoint *a, const double4_32a *q, const double4_32a *p, bool grad, double w,
+                      double4_32a *tmp = nullptr) {
   const int obj = a->c.objective;
-  if (obj == 0 && !grad) k_objective<0, 0><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w);
-  else if (obj == 0) k_objective<0, 1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w);
-  else if (!grad) k_objective<1, 0><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w);
-  else k_objective<1, 1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w);
+  if (obj == 0 && !grad) k_objective<0, 0><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w, tmp);
+  else if (obj == 0) k_objective<0, 1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w, tmp);
+  else if (!grad) k_objective<1, 0><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w, tmp);
+  else k_objective<1, 1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, q, p, w, tmp);
+}
+
+// The reverse of step n (half-step positions qh, tmp from its second
+// half-drift's reverse), with, when q_obj is given, the objective terms of
+// state n - 1 and the reverse of step n - 1's second half-drift into tmp_out.
+void launch_reverse(mdg_adjoint *a, const double4_32a *qh, const double4_32a *tmp, const double4_32a *q_obj,
+                    const double4_32a *p_obj, double w, double4_32a *tmp_out) {
+  const int obj = a->c.objective;
+  if (!q_obj) k_reverse_hvp<-1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, tmp, nullptr, nullptr, 0.0, nullptr);
+  else if (obj == 0) k_reverse_hvp<0><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, tmp, q_obj, p_obj, w, tmp_out);
+  else k_reverse_hvp<1><<<a->gridp, kT, 0, a->s>>>(a->c, a->d, qh, tmp, q_obj, p_obj, w, tmp_out);
 }
 
 // One step from the half-step positions qh (already drifted from step k - 1)
@@ -683,12 +734,19 @@ int enqueue_backward(mdg_adjoint *a) {
     for (int k = 1; k <= len; k++)
       fwd_step(a, d.segqh + N * k, d.segp + N * (k - 1), d.segq + N * k, d.segp + N * k,
                k < len ? d.segqh + N * (k + 1) : nullptr);
+    // objective terms of the segment's last state and the reverse of the
+    // second half-drift of the step that produced it; then per step k the
+    // rest of its reverse, going on (k > 1) with the objective terms of
+    // state k - 1 and the reverse of step k - 1's second half-drift
+    double4_32a *tmp = d.tmp, *tmp_alt = d.tmp2;
+    launch_objective(a, d.segq + N * len, d.segp + N * len, true, w, tmp);
     for (int k = len; k >= 1; k--) {
-      // objective terms of state (seg_start + k) and the reverse of the
-      // second half-drift of the step that produced it, then the rest of
-      // that step's reverse
-      launch_objective(a, d.segq + N * k, d.segp + N * k, true, w);
-      k_reverse_hvp<<<a->gridp, kT, 0, a->s>>>(a->c, d, d.segqh + N * k);
+      if (k > 1) {
+        launch_reverse(a, d.segqh + N * k, tmp, d.segq + N * (k - 1), d.segp + N * (k - 1), w, tmp_alt);
+        std::swap(tmp, tmp_alt);
+      } else {
+        launch_reverse(a, d.segqh + N * k, tmp, nullptr, nullptr, 0.0, nullptr);
+      }
     }
     seg_end = seg_start;
   }
@@ -787,7 +845,7 @@ int mdg_adjoint_create(const mdg_adjoint_params *p, int32_t n, mdg_adjoint **out
   D &d = a->d;
   cudaError_t e = cudaSetDevice(p->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->s, cudaStreamNonBlocking);
-  double4_32a **vecs[] = {&d.q, &d.q2, &d.p, &d.qh, &d.qh2, &d.aq, &d.ap, &d.aqh, &d.tmp, &d.q0};
+  double4_32a **vecs[] = {&d.q, &d.q2, &d.p, &d.qh, &d.qh2, &d.aq, &d.ap, &d.aqh, &d.tmp, &d.tmp2, &d.q0};
   for (auto v : vecs)
     if (e == cudaSuccess) e = aalloc(v, N);
   if (e == cudaSuccess) e = aalloc(&d.ckq, N * a->nck);
@@ -819,7 +877,7 @@ int mdg_adjoint_destroy(mdg_adjoint *a) {
   if (a->gx_forward) cudaGraphExecDestroy(a->gx_forward);
   if (a->gx_backward) cudaGraphExecDestroy(a->gx_backward);
   D &d = a->d;
-  void *ptrs[] = {d.q, d.q2, d.p, d.qh, d.qh2, d.aq, d.ap, d.aqh, d.tmp, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
+  void *ptrs[] = {d.q, d.q2, d.p, d.qh, d.qh2, d.aq, d.ap, d.aqh, d.tmp, d.tmp2, d.q0, d.ckq, d.ckp, d.segq, d.segp, d.segqh,
                   d.nbr, d.cnt, d.qf, d.part, d.acc, d.flag, d.done};
   for (void *p : ptrs)
     if (p) cudaFree(p);
