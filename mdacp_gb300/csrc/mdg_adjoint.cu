@@ -264,15 +264,16 @@ __global__ void __launch_bounds__(kT) k_build(P c, D d, const double4_32a *q) {
     qz = v.z;
   }
   const float lx = (float)c.L[0], ly = (float)c.L[1], lz = (float)c.L[2];
-  const float ilx = (float)c.inv_L[0], ily = (float)c.inv_L[1], ilz = (float)c.inv_L[2];
   const float sl2f = (float)c.sl2f;
+  // wrapped positions differ by at most L per axis, so the minimum-image
+  // separation is min(|d|, L - |d|): no rounding instruction per candidate
   auto within = [&](int j) {
     const float4 v = d.qf[j];
-    float dx = v.x - qx, dy = v.y - qy, dz = v.z - qz;
-    dx -= lx * rintf(dx * ilx);
-    dy -= ly * rintf(dy * ily);
-    dz -= lz * rintf(dz * ilz);
-    return dx * dx + dy * dy + dz * dz <= sl2f && j != i;
+    float ax = fabsf(v.x - qx), ay = fabsf(v.y - qy), az = fabsf(v.z - qz);
+    ax = fminf(ax, lx - ax);
+    ay = fminf(ay, ly - ay);
+    az = fminf(az, lz - az);
+    return ax * ax + ay * ay + az * az <= sl2f && j != i;
   };
   int m = 0;
   if (active)
