@@ -99,3 +99,29 @@ def test_adjoint_create_checks_before_device_use(lib):
     p.checkpoint_every = 0
     assert L.mdg_adjoint_create(ctypes.byref(p), 4000, ctypes.byref(h)) == 1
     assert not h.value
+
+
+def test_batch_create_checks_before_device_use(lib):
+    # box sizes against 2 (cutoff + margin), particle counts and the cell
+    # limit are checked before any device call; the switches refuse a null
+    # handle
+    import numpy as np
+    import mdacp_gb300.batch as bt
+    L = bt._lib()
+    p = bt.BatchParams()
+    L.mdg_batch_params_default(ctypes.byref(p))
+    p.margin = 0.4
+    h = ctypes.c_void_p()
+
+    def create(ns, boxes):
+        n = np.asarray(ns, dtype=np.int32)
+        b = np.asarray(boxes, dtype=np.float64).reshape(-1, 3)
+        return L.mdg_batch_create(ctypes.byref(p), len(n), n.ctypes.data_as(bt._I), bt._dp(b), ctypes.byref(h))
+
+    assert create([100], [[5.7, 10.0, 10.0]]) == 1      # an edge below 2 (2.5 + 0.4)
+    assert create([0], [[10.0, 10.0, 10.0]]) == 1       # an empty box
+    assert create([100, -1], [[10.0] * 3, [10.0] * 3]) == 1
+    assert create([100], [[100.0, 100.0, 100.0]]) == 3  # 34^3 cells > the per-box limit
+    assert not h.value
+    assert L.mdg_batch_set_inner(None, 1) == 1
+    assert L.mdg_batch_set_shape(None, 512, 1, 4) == 1
