@@ -110,7 +110,11 @@ int setup_geometry(mdg_handle *h) {
   long long ncell = 1;
   for (int k = 0; k < 3; k++) {
     g.L[k] = p.box[k];
-    int nc = (int)(p.box[k] / sl);
+    // bounded before the conversion: the cell coordinates have 11 or 10 bits
+    const double ratio = p.box[k] / sl;
+    if (!std::isfinite(p.box[k]) || !(ratio < (double)(1 << mdg::kCellXBits)))
+      return fail(h, MDG_ERR_INVALID, "more than 2047 x 2047 x 1023 cells along the box sides");
+    int nc = (int)ratio;
     // every pair within sl must lie in neighbouring cells even after rounding
     while (nc > 0 && p.box[k] / (double)nc < sl * (1.0 + 1e-12)) nc--;
     if (nc < 2 || p.box[k] <= 2.0 * sl)

@@ -20,6 +20,8 @@
 // first call; nothing is allocated or freed, ever.
 #include <cuda_runtime.h>
 
+#include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 
@@ -232,6 +234,11 @@ extern "C" int mdg_observe_noalloc(const double *q4_dev, const double *p4_dev, i
                                    double cutoff, double *out3_dev, void *stream) {
   using namespace mdg::noalloc;
   if (!q4_dev || !p4_dev || !box || !out3_dev || n <= 0 || !(cutoff > 0.0)) return MDG_ERR_INVALID;
+  // the state is read as 32-byte vectors, the sums written as doubles
+  if ((((uintptr_t)q4_dev | (uintptr_t)p4_dev) & 31u) != 0 || ((uintptr_t)out3_dev & 7u) != 0) {
+    fprintf(stderr, "mdg_observe_noalloc: q4_dev and p4_dev must be 32-byte aligned, out3_dev 8-byte aligned\n");
+    return MDG_ERR_INVALID;
+  }
   if (n > kMaxParticles) {
     fprintf(stderr, "mdg_observe_noalloc: %d particles exceed the fixed maximum of %d\n", n, kMaxParticles);
     return MDG_ERR_CAPACITY;
@@ -239,13 +246,24 @@ extern "C" int mdg_observe_noalloc(const double *q4_dev, const double *p4_dev, i
   Box b;
   long long ncell = 1;
   for (int k = 0; k < 3; k++) {
-    if (!(box[k] > 2.0 * cutoff)) return MDG_ERR_INVALID;
-    int nc = (int)(box[k] / cutoff);
+    if (!(box[k] > 2.0 * cutoff) || !std::isfinite(box[k])) return MDG_ERR_INVALID;
+    // the cell count is bounded before any conversion or product can overflow
+    const double ratio = box[k] / cutoff;
+    if (!(ratio <= (double)kMaxCells)) {
+      fprintf(stderr, "mdg_observe_noalloc: box side %g / cutoff %g exceeds the fixed maximum of %d cells\n",
+              box[k], cutoff, kMaxCells);
+      return MDG_ERR_CAPACITY;
+    }
+    int nc = (int)ratio;
     while (nc > 0 && box[k] / (double)nc < cutoff * (1.0 + 1e-12)) nc--;
     if (nc < 2) return MDG_ERR_INVALID;
     b.L[k] = box[k];
     b.nc[k] = nc;
     b.inv_w[k] = 1.0 / (box[k] / (double)nc);
+    if (ncell > kMaxCells / nc) {
+      fprintf(stderr, "mdg_observe_noalloc: more cells than the fixed maximum of %d\n", kMaxCells);
+      return MDG_ERR_CAPACITY;
+    }
     ncell *= nc;
   }
   if (ncell > kMaxCells) {

@@ -125,3 +125,37 @@ def test_batch_create_checks_before_device_use(lib):
     assert not h.value
     assert L.mdg_batch_set_inner(None, 1) == 1
     assert L.mdg_batch_set_shape(None, 512, 1, 4) == 1
+
+
+def test_noalloc_limits_checked_before_device_use(lib):
+    # a huge box over a tiny cut-off would overflow the cell count; it is
+    # refused (MDG_ERR_CAPACITY) before any conversion, product or launch, and
+    # state arrays off a 32-byte boundary are refused (MDG_ERR_INVALID).  The
+    # pointers are never dereferenced on these paths.
+    from mdacp_gb300 import native
+    L = native.load()
+    aligned, odd = ctypes.c_void_p(0x10000), ctypes.c_void_p(0x10008)
+    out = ctypes.c_void_p(0x20000)
+    for box in ((1e30, 1e30, 1e30), (3e6, 3e6, 3e6), (2.0 ** 22, 2.0 ** 22, 2.0 ** 22), (600.0, 600.0, 600.0)):
+        b = (ctypes.c_double * 3)(*box)
+        assert L.mdg_observe_noalloc(aligned, aligned, 100, b, 1e-3 if box[0] > 1e6 else 1.0, out, None) == 3
+    b = (ctypes.c_double * 3)(20.0, 20.0, 20.0)
+    assert L.mdg_observe_noalloc(odd, aligned, 100, b, 2.5, out, None) == 1
+    assert L.mdg_observe_noalloc(aligned, odd, 100, b, 2.5, out, None) == 1
+    assert L.mdg_observe_noalloc(aligned, aligned, 100, b, 2.5, ctypes.c_void_p(0x20004), None) == 1
+    b = (ctypes.c_double * 3)(float("inf"), 20.0, 20.0)
+    assert L.mdg_observe_noalloc(aligned, aligned, 100, b, 2.5, out, None) == 1
+
+
+def test_create_refuses_huge_boxes_before_device_use(lib):
+    from mdacp_gb300 import native
+    L = native.load()
+    p = native.Params()
+    L.mdg_params_default(ctypes.byref(p))
+    p.capacity = 100
+    h = ctypes.c_void_p()
+    for side in (1e30, 2.0 ** 40, float("inf")):
+        p.box[0] = side
+        assert L.mdg_create(ctypes.byref(p), ctypes.byref(h)) == 1
+        assert not h.value
+        assert b"cells" in L.mdg_last_error(None)
