@@ -39,7 +39,12 @@ extern "C" {
 #define MDG_ERR_STATE 4        /* non-finite or escaped particle coordinate */
 #define MDG_ERR_NOT_READY 5    /* no state loaded */
 
-enum mdg_precision { MDG_FP64 = 0, MDG_MIXED = 1 };
+/* MDG_FP64: the reference's arithmetic.  MDG_MIXED: pair distance and force
+ * in FP32 from cell-local positions, per-particle force sums in compensated
+ * (Kahan) FP32, positions, momenta, displacement and the energy/virial
+ * reductions in FP64.  MDG_MIXED_PLAIN: as MDG_MIXED with plain FP32 force
+ * sums (kept for comparison). */
+enum mdg_precision { MDG_FP64 = 0, MDG_MIXED = 1, MDG_MIXED_PLAIN = 2 };
 enum mdg_thermostat { MDG_NVE = 0, MDG_LANGEVIN = 1, MDG_NOSEHOOVER = 2 };
 
 typedef struct mdg_params {
@@ -115,9 +120,11 @@ int mdg_make_pairlist(mdg_handle *h);
 int mdg_calculate(mdg_handle *h, int32_t nsteps);
 /* Waits for and confirms the steps mdg_calculate left outstanding. */
 int mdg_synchronize(mdg_handle *h);
-/* mdg_calculate without graph replay, with a CUDA event pair on the handle's
- * stream around every launch of the fused step kernel; *step_kernel_ms receives
- * the summed device time of those launches (for roofline accounting). */
+/* mdg_calculate with a CUDA event pair around every step kernel: the steps
+ * replay the same step graph as mdg_calculate with event-record nodes added
+ * (plain launches with events when use_graphs = 0), and the call waits for
+ * them.  *step_kernel_ms receives the summed device time of the step kernels
+ * (for roofline accounting). */
 int mdg_calculate_profiled(mdg_handle *h, int32_t nsteps, double *step_kernel_ms);
 /* The phase times of the reference's StopWatch objects (mdmanager.cc:117-147,
  * stopwatch.h:8-37) for nsteps steps run as in mdg_calculate_profiled:

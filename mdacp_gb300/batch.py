@@ -82,7 +82,7 @@ class Batch:
         self.lib = _lib()
         prm = BatchParams()
         self.lib.mdg_batch_params_default(ctypes.byref(prm))
-        prm.precision = {"fp64": native.FP64, "mixed": native.MIXED}[precision]
+        prm.precision = native.PRECISIONS[precision]
         prm.device, prm.cutoff, prm.margin, prm.dt = device, cutoff, margin, dt
         prm.list_capacity, prm.use_graphs = list_capacity, 1 if use_graphs else 0
         if prune_buffer is not None:

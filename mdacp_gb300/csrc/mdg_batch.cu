@@ -433,6 +433,7 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
     const AxisQuad qy = axis_quad(b.w32[1], b.dl32[1], cy == 0, cy == b.nc[1] - 1, li.y, 0.25f);
     const AxisQuad qz = axis_quad(b.w32[2], b.dl32[2], cz == 0, cz == b.nc[2] - 1, li.z, 0.0625f);
     float sx = 0.f, sy = 0.f, sz = 0.f;
+    float cx_ = 0.f, cy_ = 0.f, cz_ = 0.f;  // Kahan corrections (MDG_MIXED)
     const float4 *loc = d.loc[par] + o;
     auto pair = [&](uint32_t e, const float4 &lj) {
       const float tx = step_float(e, 0x03u, 8388609.0f), ty = step_float(e, 0x0Cu, 8388612.0f),
@@ -447,9 +448,15 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
       const float i6 = inv * inv * inv;
       float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + P.c2x8f;
       df = r2 <= P.rc2f ? df : 0.0f;
-      sx = fmaf(df, dx, sx);
-      sy = fmaf(df, dy, sy);
-      sz = fmaf(df, dz, sz);
+      if (MIXED == MDG_MIXED) {  // compensated sums, as the single-box mixed form
+        kahan_fma(sx, cx_, df, dx);
+        kahan_fma(sy, cy_, df, dy);
+        kahan_fma(sz, cz_, df, dz);
+      } else {
+        sx = fmaf(df, dx, sx);
+        sy = fmaf(df, dy, sy);
+        sz = fmaf(df, dz, sz);
+      }
     };
     // this lane's entries lane, lane + LPI, ... in batches of four: the next
     // batch's entries are requested before this batch's positions are used,
@@ -487,9 +494,9 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
 #pragma unroll
       for (int u = 0; u < 3; u++) pair(en[u], l[u]);
     }
-    fx = (double)sx;
-    fy = (double)sy;
-    fz = (double)sz;
+    fx = (double)(sx - cx_);
+    fy = (double)(sy - cy_);
+    fz = (double)(sz - cz_);
   } else {
     const double4_32a qi = d.q_mid[par][o + a];
     const bool edge = cx == 0 || cy == 0 || cz == 0 || cx == b.nc[0] - 1 || cy == b.nc[1] - 1 || cz == b.nc[2] - 1;
@@ -807,7 +814,7 @@ int alloc_batch_list(mdg_batch *b, int cap) {
 
 void launch_batch_step(mdg_batch *b, int par) {
   const int T = b->threads;
-  const bool mixed = b->prm.precision == MDG_MIXED;
+  const int prec = b->prm.precision;
   k_batch_rebuild_set<<<1, 1024, 0, b->stream>>>(b->P, b->d);
   k_batch_bin<<<b->num_sms * 16, 128, 0, b->stream>>>(b->d);
   k_batch_sort<<<b->nbox, kPrepThreads, 0, b->stream>>>(b->d);
@@ -815,9 +822,12 @@ void launch_batch_step(mdg_batch *b, int par) {
   k_batch_list<<<b->num_sms * 16, 128, 0, b->stream>>>(b->P, b->d);
 #define MDG_BSTEP(M, L, I) k_batch_step<M, L, I><<<b->grid, T, 0, b->stream>>>(b->P, b->d, par)
   const bool inner = b->P.inner && b->lpi == 1 && b->use_inner;
-  if (mixed) {
-    if (b->lpi == 4) MDG_BSTEP(1, 4, 0); else if (b->lpi == 2) MDG_BSTEP(1, 2, 0);
-    else if (inner) MDG_BSTEP(1, 1, 1); else MDG_BSTEP(1, 1, 0);
+  if (prec == MDG_MIXED) {
+    if (b->lpi == 4) MDG_BSTEP(MDG_MIXED, 4, 0); else if (b->lpi == 2) MDG_BSTEP(MDG_MIXED, 2, 0);
+    else if (inner) MDG_BSTEP(MDG_MIXED, 1, 1); else MDG_BSTEP(MDG_MIXED, 1, 0);
+  } else if (prec == MDG_MIXED_PLAIN) {
+    if (b->lpi == 4) MDG_BSTEP(MDG_MIXED_PLAIN, 4, 0); else if (b->lpi == 2) MDG_BSTEP(MDG_MIXED_PLAIN, 2, 0);
+    else if (inner) MDG_BSTEP(MDG_MIXED_PLAIN, 1, 1); else MDG_BSTEP(MDG_MIXED_PLAIN, 1, 0);
   } else {
     if (b->lpi == 4) MDG_BSTEP(0, 4, 0); else if (b->lpi == 2) MDG_BSTEP(0, 2, 0);
     else if (inner) MDG_BSTEP(0, 1, 1); else MDG_BSTEP(0, 1, 0);
@@ -882,6 +892,7 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
                      mdg_batch **out) {
   if (!p || !out || nbox <= 0 || !n_per_box || !box_lengths) return MDG_ERR_INVALID;
   *out = nullptr;
+  if (p->precision < MDG_FP64 || p->precision > MDG_MIXED_PLAIN) return MDG_ERR_INVALID;
   mdg_batch *b = new mdg_batch();
   b->prm = *p;
   b->nbox = nbox;

@@ -196,6 +196,16 @@ __device__ __forceinline__ float step_float(uint32_t e, uint32_t mask, float bia
   return __int_as_float((int)((e & mask) | 0x4B000000u)) - bias;
 }
 
+// Compensated float accumulation (Kahan) of a * b into s: c carries the low
+// part each addition lost (with the opposite sign), so the sum is s - c.  The
+// product is fused into the first subtraction.
+__device__ __forceinline__ void kahan_fma(float &s, float &c, float a, float b) {
+  const float y = fmaf(a, b, -c);
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
 // device helpers
 __device__ __forceinline__ void halt_with(DevFlags *f, int code) { atomicCAS(&f->halt, 0, code); }
 

@@ -16,15 +16,17 @@
 // from the hardware reciprocal estimate (rcp.approx.ftz.f64) refined by one
 // Householder step of order three, y <- y (1 + e + e^2), e = 1 - r^2 y, which
 // cubes the relative error of the estimate.
-// Mixed form: particle positions relative to their home-cell centre in
-// float; the pair force and the per-particle sum in float; momentum and
-// position updates in double with fused multiply-adds.  A float sum of about
-// 40 terms adds an error near u sqrt(40) |f_ij| (u = 2^-24), a few times
-// below the error each float pair force already carries (its separation is
-// rounded to a float ulp of the cell width), so compensated summation would
-// buy no accuracy.  GB300 runs double precision at 1/64 of the float rate,
-// so the per-particle double work (momentum, two half-drifts, displacement)
-// is kept to one operation per component each.
+// Mixed form (MDG_MIXED): particle positions relative to their home-cell
+// centre in float; the pair force in float; the per-particle force sum in
+// compensated float (Kahan: each term's lost low part carried in a second
+// float, four float operations per component and pair), so the sum's error
+// does not grow with the number of partners; converted to double once per
+// particle; momentum and position updates in double with fused multiply-adds.
+// MDG_MIXED_PLAIN sums the pair forces in plain float instead (an error near
+// u sqrt(40) |f_ij|, u = 2^-24, over about 40 terms).  GB300 runs double
+// precision at 1/64 of the float rate, so the per-particle double work
+// (momentum, two half-drifts, displacement) is kept to one operation per
+// component each, and the per-pair work stays in float.
 #include "mdg_internal.cuh"
 
 namespace mdg {
@@ -38,6 +40,11 @@ constexpr int kStepThreads = 128;
 // SM) ran 16 % faster than the unconstrained 61-register build at 4M atoms.
 #ifndef MDG_STEP_MIN_BLOCKS
 #define MDG_STEP_MIN_BLOCKS 12
+#endif
+// The same for the compensated mixed form, whose three correction terms do
+// not fit in 40 registers (48 bytes of spills at 12 blocks).
+#ifndef MDG_STEP_MIN_BLOCKS_KAHAN
+#define MDG_STEP_MIN_BLOCKS_KAHAN 10
 #endif
 #ifndef MDG_PRUNE_MIN_BLOCKS
 #define MDG_PRUNE_MIN_BLOCKS 8
@@ -141,7 +148,9 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
 // Mixed form of force_fp64 on home-cell-local float positions.  The offset
 // between the home cells of i and j is ox*w + s*(L - nc*w) per axis, s the
 // periodic wrap of the stencil step, evaluated as the quadratic of axis_quad.
-template <bool PRUNE>
+// KAHAN: the per-particle sums compensated (MDG_MIXED), else plain float
+// (MDG_MIXED_PLAIN).
+template <bool PRUNE, bool KAHAN>
 __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
                                                const CellPos &cp, const uint32_t *__restrict__ list,
                                                const int *__restrict__ counts, int *kept) {
@@ -154,6 +163,7 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
   const uint32_t *row = list + i;
   const size_t stride = (size_t)g.stride;
   float sx = 0.f, sy = 0.f, sz = 0.f;
+  float cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan corrections
   // a partner position (a far one, contributing nothing, for an entry a
   // checked build rejects)
   auto gather = [&](uint32_t e) -> float4 {
@@ -178,9 +188,19 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
     const float i6 = inv * inv * inv;
     float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8;
     df = r2 <= rc2 ? df : 0.0f;
-    sx = fmaf(df, dx, sx);
-    sy = fmaf(df, dy, sy);
-    sz = fmaf(df, dz, sz);
+    if (KAHAN) {
+      // a zero term (a pair beyond rc) leaves s - c unchanged as a real
+      // number (t - s is exact, and so is the new correction), but it moves
+      // the correction into s: lists that differ only by pairs beyond rc give
+      // sums that agree to second order in the float rounding, not bit for bit
+      kahan_fma(sx, cx, df, dx);
+      kahan_fma(sy, cy, df, dy);
+      kahan_fma(sz, cz, df, dz);
+    } else {
+      sx = fmaf(df, dx, sx);
+      sy = fmaf(df, dy, sy);
+      sz = fmaf(df, dz, sz);
+    }
   };
   int k = 0;
   // the next batch's list entries are requested before this batch's partner
@@ -225,6 +245,9 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
     for (int u = 0; u < kTail; u++) pair(en[u], l[u]);
   }
   if (PRUNE) *kept = m;
+  // the compensated sum rounded once to float (relative 6e-8 of the force),
+  // then one conversion per component: GB300 runs double at 1/64 of float
+  if (KAHAN) return make_double3((double)(sx - cx), (double)(sy - cy), (double)(sz - cz));
   return make_double3((double)sx, (double)sy, (double)sz);
 }
 
@@ -269,7 +292,10 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // 1 = ordinary step only, 2 = re-selecting step only (each a no-op when the
 // flag says otherwise, so the graph path can run the lighter variant).
 template <int THERMO, int COMPAT, int MIXED, int PMODE>
-__global__ void __launch_bounds__(kStepThreads, PMODE == 1 ? MDG_STEP_MIN_BLOCKS : MDG_PRUNE_MIN_BLOCKS) k_step(Geom g, Dev d, int par) {
+__global__ void __launch_bounds__(kStepThreads, PMODE != 1          ? MDG_PRUNE_MIN_BLOCKS
+                                                : MIXED == MDG_MIXED ? MDG_STEP_MIN_BLOCKS_KAHAN
+                                                                     : MDG_STEP_MIN_BLOCKS)
+    k_step(Geom g, Dev d, int par) {
   const DevFlags *f = d.flags;
   if (f->halt != 0) return;
   if (PMODE == 1 && f->prune_now != 0) return;
@@ -288,10 +314,10 @@ __global__ void __launch_bounds__(kStepThreads, PMODE == 1 ? MDG_STEP_MIN_BLOCKS
     const CellPos cp = cell_pos_packed(g, lb.w);
     double3 F;
     if (prune)
-      F = MIXED ? force_mixed<true>(g, d, d.loc[par], i, cp, d.nl, d.ncount, &kept)
+      F = MIXED ? force_mixed<true, MIXED == MDG_MIXED>(g, d, d.loc[par], i, cp, d.nl, d.ncount, &kept)
                 : force_fp64<true>(g, d, qm, i, cp, d.nl, d.ncount, &kept);
     else
-      F = MIXED ? force_mixed<false>(g, d, d.loc[par], i, cp, d.pl, d.pcount, nullptr)
+      F = MIXED ? force_mixed<false, MIXED == MDG_MIXED>(g, d, d.loc[par], i, cp, d.pl, d.pcount, nullptr)
                 : force_fp64<false>(g, d, qm, i, cp, d.pl, d.pcount, nullptr);
     double4_32a p = d.p[i];
     if (THERMO == MDG_NOSEHOOVER) {
@@ -450,10 +476,10 @@ __global__ void __launch_bounds__(kStepThreads) k_observe(Geom g, Dev d) {
   }
 }
 
-// Mixed-form observers: the same sums with the pair terms in float (from the
-// home-cell-local float positions of q_end, as the mixed force), each
-// particle's sum converted to double and reduced in double.  The FP64 form
-// keeps k_observe's reference rounding.
+// Mixed-form observers: the same sums with each pair's energy and virial
+// term evaluated in float (from the home-cell-local float positions of q_end,
+// as the mixed force) and every term added in double, per particle and over
+// particles.  The FP64 form keeps k_observe's reference rounding.
 __global__ void __launch_bounds__(kStepThreads) k_observe_mixed(Geom g, Dev d, const float4 *__restrict__ loc) {
   __shared__ double sh[kStepThreads / 32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -467,7 +493,7 @@ __global__ void __launch_bounds__(kStepThreads) k_observe_mixed(Geom g, Dev d, c
     const AxisQuad qy = axis_quad(g.w32[1], g.dl32[1], cp.cy == 0, cp.cy == g.nc[1] - 1, li.y, 0.25f);
     const AxisQuad qz = axis_quad(g.w32[2], g.dl32[2], cp.cz == 0, cp.cz == g.nc[2] - 1, li.z, 0.0625f);
     const float rc2 = g.rc2f, c2 = (float)g.c2, c0 = (float)g.c0, c2x8 = g.c2x8f;
-    float e_sum = 0.f, v_sum = 0.f;
+    double e_sum = 0.0, v_sum = 0.0;
     const int cnt = d.ncount[i];
     for (int k = 0; k < cnt; k++) {
       const uint32_t e = __ldg(d.nl + (size_t)k * g.stride + i);
@@ -484,12 +510,13 @@ __global__ void __launch_bounds__(kStepThreads) k_observe_mixed(Geom g, Dev d, c
       const float i6 = inv * inv * inv;
       const float e_ij = 4.0f * (i6 * i6 - i6 + fmaf(c2, r2, c0));
       const float v_ij = ((i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8) * r2;
-      const bool in = r2 <= rc2;
-      e_sum += in ? e_ij : 0.0f;
-      v_sum += in ? v_ij : 0.0f;
+      if (r2 <= rc2) {
+        e_sum += (double)e_ij;
+        v_sum += (double)v_ij;
+      }
     }
-    pe = 0.5 * (double)e_sum;
-    vir = 0.5 * (double)v_sum;
+    pe = 0.5 * e_sum;
+    vir = 0.5 * v_sum;
   }
   const double a = block_sum(ke, sh);
   const double b = block_sum(pe, sh);
@@ -523,7 +550,7 @@ __global__ void __launch_bounds__(kStepThreads) k_forces(Geom g, Dev d, const fl
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n) return;
   const CellPos cp = cell_pos(g, d.cell[i]);
-  const double3 F = MIXED ? force_mixed<false>(g, d, loc, i, cp, d.nl, d.ncount, nullptr)
+  const double3 F = MIXED ? force_mixed<false, MIXED == MDG_MIXED>(g, d, loc, i, cp, d.nl, d.ncount, nullptr)
                           : force_fp64<false>(g, d, d.q_end, i, cp, d.nl, d.ncount, nullptr);
   d.io4[d.id[i]] = make_double4_32a(F.x, F.y, F.z, 0.0);
 }
@@ -592,24 +619,25 @@ void launch_step_variant(const Geom &g, const Dev &d, int par, int pmode, cudaSt
   if (T == MDG_NOSEHOOVER) k_nh_update<<<1, 1024, 0, s>>>(g, d, grid, 0);
 }
 
+template <int T, int C>
+void launch_step_precision(const Geom &g, const Dev &d, int par, int precision, int pmode, cudaStream_t s) {
+  if (precision == MDG_MIXED) launch_step_variant<T, C, MDG_MIXED>(g, d, par, pmode, s);
+  else if (precision == MDG_MIXED_PLAIN) launch_step_variant<T, C, MDG_MIXED_PLAIN>(g, d, par, pmode, s);
+  else launch_step_variant<T, C, MDG_FP64>(g, d, par, pmode, s);
+}
+
 // pmode: 0 one kernel deciding on the device; 1 / 2 only the ordinary / the
 // re-selecting variant (graph conditional bodies); 3 both variants in turn.
+// mixed: the handle's mdg_precision.
 void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compat, int mixed, cudaStream_t s,
                  int pmode) {
   if (thermostat == MDG_LANGEVIN) {
-    if (compat) {
-      if (mixed) launch_step_variant<MDG_LANGEVIN, 1, 1>(g, d, par, pmode, s);
-      else launch_step_variant<MDG_LANGEVIN, 1, 0>(g, d, par, pmode, s);
-    } else {
-      if (mixed) launch_step_variant<MDG_LANGEVIN, 0, 1>(g, d, par, pmode, s);
-      else launch_step_variant<MDG_LANGEVIN, 0, 0>(g, d, par, pmode, s);
-    }
+    if (compat) launch_step_precision<MDG_LANGEVIN, 1>(g, d, par, mixed, pmode, s);
+    else launch_step_precision<MDG_LANGEVIN, 0>(g, d, par, mixed, pmode, s);
   } else if (thermostat == MDG_NOSEHOOVER) {
-    if (mixed) launch_step_variant<MDG_NOSEHOOVER, 0, 1>(g, d, par, pmode, s);
-    else launch_step_variant<MDG_NOSEHOOVER, 0, 0>(g, d, par, pmode, s);
+    launch_step_precision<MDG_NOSEHOOVER, 0>(g, d, par, mixed, pmode, s);
   } else {
-    if (mixed) launch_step_variant<MDG_NVE, 0, 1>(g, d, par, pmode, s);
-    else launch_step_variant<MDG_NVE, 0, 0>(g, d, par, pmode, s);
+    launch_step_precision<MDG_NVE, 0>(g, d, par, mixed, pmode, s);
   }
 }
 
@@ -636,7 +664,8 @@ void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t
   if (mixed) {
     // the buffer the next step overwrites before reading it
     k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
-    k_forces<1><<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
+    if (mixed == MDG_MIXED_PLAIN) k_forces<MDG_MIXED_PLAIN><<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
+    else k_forces<MDG_MIXED><<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
   } else {
     k_forces<0><<<grid, kStepThreads, 0, s>>>(g, d, nullptr);
   }

@@ -41,7 +41,7 @@ class MDManager:
         prm.box[:] = [float(v) for v in box]
         prm.capacity = int(capacity or n or 1000000)
         prm.cutoff, prm.margin, prm.dt = float(cutoff), float(margin), float(dt)
-        prm.precision = {"fp64": native.FP64, "mixed": native.MIXED}[precision]
+        prm.precision = native.PRECISIONS[precision]
         prm.thermostat = {"nve": native.NVE, "langevin": native.LANGEVIN, "nosehoover": native.NOSEHOOVER}[thermostat]
         prm.temperature, prm.gamma, prm.tau = float(temperature), float(gamma), float(tau)
         prm.seed = int(seed)
@@ -67,7 +67,7 @@ class MDManager:
         kw = dict(box=si.L, capacity=n, cutoff=si.cutoff, margin=si.buffer_length, dt=si.time_step,
                   precision=si.precision, thermostat=si.thermostat, temperature=si.aimed_temperature,
                   gamma=si.heatbath_gamma, tau=si.heatbath_tau, seed=param.get_int("Seed", 1),
-                  langevin_half_drift_compat=si.langevin_half_drift_compat)
+                  langevin_half_drift_compat=si.langevin_half_drift_compat, device=si.device)
         kw.update(overrides)
         return cls(**kw)
 
@@ -137,14 +137,15 @@ class MDManager:
         self._ck(self.lib.mdg_calculate(self._h, int(nsteps)))
 
     def calculate_profiled(self, nsteps):
-        """Steps without graph replay; returns the summed device ms of the fused step kernel."""
+        """Steps as mdg_calculate replays them, with CUDA events around every
+        step kernel; returns the summed device ms of the fused step kernel."""
         ms = ctypes.c_double()
         self._ck(self.lib.mdg_calculate_profiled(self._h, int(nsteps), ctypes.byref(ms)))
         return ms.value
 
     def calculate_phases(self, nsteps):
-        """Steps without graph replay; device ms per phase as the reference's
-        StopWatch objects split Calculate: {"force", "pair", "all"}."""
+        """Steps as mdg_calculate_profiled runs them; device ms per phase as the
+        reference's StopWatch objects split Calculate: {"force", "pair", "all"}."""
         out = np.zeros(3)
         self._ck(self.lib.mdg_calculate_phases(self._h, int(nsteps), _dp(out)))
         return {"force": out[0], "pair": out[1], "all": out[2]}

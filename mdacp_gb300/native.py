@@ -13,7 +13,8 @@ CHECK_LIB_PATH = os.path.join(HERE, "libmdg_check.so")
 
 MDG_OK = 0
 ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "capacity", 4: "bad particle state", 5: "no state"}
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_PLAIN = 0, 1, 2
+PRECISIONS = {"fp64": FP64, "mixed": MIXED, "mixed_plain": MIXED_PLAIN}
 NVE, LANGEVIN, NOSEHOOVER = 0, 1, 2
 
 

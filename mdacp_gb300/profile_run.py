@@ -24,7 +24,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--cells", type=int, default=63)
     ap.add_argument("--density", type=float, default=0.5)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_plain", "fp64"])
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--no-graphs", action="store_true")
     ap.add_argument("--profiled", action="store_true")
