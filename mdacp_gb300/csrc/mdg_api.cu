@@ -306,16 +306,30 @@ int add_conditional(mdg_handle *h, cudaGraph_t g, cudaGraphNode_t dep, cudaGraph
   return MDG_OK;
 }
 
+// Appends an event-record node after `dep`; *node receives it.
+int add_event(mdg_handle *h, cudaGraph_t g, cudaGraphNode_t dep, cudaEvent_t ev, cudaGraphNode_t *node) {
+  MDG_CK(cudaGraphAddEventRecordNode(node, g, &dep, 1, ev));
+  return MDG_OK;
+}
+
 // A graph of nsteps steps starting at parity par.  Per step: a one-thread
 // prelude (counters, inner-list hand-over) that sets the rebuild condition;
 // IF(rebuild) { wrap, bin, reorder, build }; a one-thread select that sets
 // the variant; SWITCH(variant) { ordinary step | re-selecting step }.  Steps
-// without a rebuild therefore run three kernels.
-int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps) {
+// without a rebuild therefore run three kernels.  With `ev` (3 nsteps + 1
+// events) the graph starts by recording ev[3 nsteps], and step k records
+// ev[3k] after its prelude, ev[3k+1] before its step kernel and ev[3k+2]
+// after it, so the device time of each phase of each step is read from the
+// same replay.
+int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps, cudaEvent_t *ev = nullptr) {
   cudaGraph_t g = nullptr;
   MDG_CK(cudaGraphCreate(&g, 0));
   cudaGraphNode_t last = nullptr;
   int rc = MDG_OK;
+  if (ev) {
+    cudaError_t e = cudaGraphAddEventRecordNode(&last, g, nullptr, 0, ev[3 * nsteps]);
+    if (e != cudaSuccess) rc = fail(h, MDG_ERR_CUDA, std::string("cudaGraphAddEventRecordNode: ") + cudaGetErrorString(e));
+  }
   const int lang = lang_on(h) != 0;
   for (int k = 0; k < nsteps && rc == MDG_OK; k++) {
     const int p = par ^ (k & 1);
@@ -328,17 +342,20 @@ int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps) {
     }
     cudaGraphNode_t pre = nullptr, cond = nullptr, sel = nullptr, sw = nullptr;
     rc = append_captured(h, g, last ? &last : nullptr, [&] { mdg::launch_prelude(h->d, lang, c_rb, h->stream); }, &pre);
+    if (rc == MDG_OK && ev) rc = add_event(h, g, pre, ev[3 * k], &pre);
     if (rc) break;
     rc = add_conditional(h, g, pre, c_rb, cudaGraphCondTypeIf, 1, [&](int) {
       mdg::launch_rebuild(h->g, h->d, p, h->num_sms, h->stream, false, false, true);
     }, &cond);
     if (rc) break;
     rc = append_captured(h, g, &cond, [&] { mdg::launch_select(h->d, c_var, h->stream); }, &sel);
+    if (rc == MDG_OK && ev) rc = add_event(h, g, sel, ev[3 * k + 1], &sel);
     if (rc) break;
     rc = add_conditional(h, g, sel, c_var, cudaGraphCondTypeSwitch, 2, [&](int variant) {
       mdg::launch_step(h->g, h->d, p, h->prm.thermostat, h->prm.langevin_half_drift_compat, h->prm.precision,
                        h->stream, variant == 0 ? 1 : 2);
     }, &sw);
+    if (rc == MDG_OK && ev) rc = add_event(h, g, sw, ev[3 * k + 2], &sw);
     last = sw;
   }
   if (rc == MDG_OK) {
@@ -475,7 +492,7 @@ int mdg_create(const mdg_params *p, mdg_handle **out) {
     return create_fail(MDG_ERR_INVALID, "capacity must be in 1 .. " + std::to_string(mdg::kMaxParticles));
   if (!(p->cutoff > 0.0) || !(p->margin >= 0.0) || !(p->dt > 0.0))
     return create_fail(MDG_ERR_INVALID, "cutoff and dt must be > 0, margin >= 0");
-  if (p->precision != MDG_FP64 && p->precision != MDG_MIXED) return create_fail(MDG_ERR_INVALID, "bad precision");
+  if (p->precision < MDG_FP64 || p->precision > MDG_MIXED_PLAIN) return create_fail(MDG_ERR_INVALID, "bad precision");
   if (p->thermostat < MDG_NVE || p->thermostat > MDG_NOSEHOOVER) return create_fail(MDG_ERR_INVALID, "bad thermostat");
   mdg_handle *h = new mdg_handle();
   h->prm = *p;
@@ -692,17 +709,80 @@ int mdg_synchronize(mdg_handle *h) { return check_handle(h, false); }
 
 namespace {
 
-// Steps as plain launches with three events per step on the handle's stream:
-// before the rebuild sequence, before the step kernel, after it.  Sums the
-// device time of the step kernels (force, kick, drifts), of the rebuild
-// sequences (wrap, bin, sort, list build; empty launches when none is due)
-// and of the whole run.
+// Steps replayed as the graph mdg_calculate replays, with event-record nodes
+// around each step's rebuild phase and step kernel (capture(.., ev)); the
+// graph of up to kTimedChunk steps is captured for the call and replayed
+// once.  Sums the device time of the step kernels, of the rebuild phases
+// and of the whole run, and counts the rebuilds that ran.
+constexpr int kTimedChunk = 1024;
+
+int timed_graph_run(mdg_handle *h, int32_t nsteps, double *step_ms, double *rebuild_ms, double *all_ms) {
+  std::vector<cudaEvent_t> ev(3 * (size_t)kTimedChunk + 1, nullptr);
+  for (auto &e : ev) MDG_CK(cudaEventCreate(&e));
+  double t_step = 0.0, t_rebuild = 0.0, t_all = 0.0;
+  long long done = 0;
+  int status = MDG_OK;
+  for (int guard = 0; guard < 4096 && done < nsteps && status == MDG_OK; guard++) {
+    const int m = (int)((nsteps - done) < kTimedChunk ? (nsteps - done) : kTimedChunk);
+    const unsigned long long before = (unsigned long long)h->steps_host, rebuilds0 = h->hflags->rebuilds;
+    cudaGraphExec_t gx = nullptr;
+    status = capture(h, &gx, h->par, m, ev.data());
+    if (status) break;
+    cudaError_t e = cudaGraphLaunch(gx, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaGraphExecDestroy(gx);
+    if (e != cudaSuccess) {
+      status = fail(h, MDG_ERR_CUDA, std::string("timed graph: ") + cudaGetErrorString(e));
+      break;
+    }
+    status = read_flags(h);
+    if (status) break;
+    const long long completed = (long long)(h->hflags->steps - before);
+    h->launches += completed * (2 + mdg::step_kernels(h->prm.thermostat)) +
+                   (long long)(h->hflags->rebuilds - rebuilds0) * mdg::kRebuildKernels;
+    // a halted step and those behind it ran as no-ops: only the steps that
+    // completed are timed
+    const int timed = (int)(h->hflags->halt == 0 ? m : completed - 1);
+    for (int k = 0; k < timed; k++) {
+      float a = 0.f, b = 0.f;
+      if (cudaEventElapsedTime(&a, ev[3 * k], ev[3 * k + 1]) == cudaSuccess) t_rebuild += a;
+      if (cudaEventElapsedTime(&b, ev[3 * k + 1], ev[3 * k + 2]) == cudaSuccess) t_step += b;
+    }
+    float w = 0.f;
+    if (timed > 0 && cudaEventElapsedTime(&w, ev[3 * m], ev[3 * (timed - 1) + 2]) == cudaSuccess) t_all += w;
+    if (h->hflags->halt == 0) {
+      done += completed;
+      h->steps_host = (long long)h->hflags->steps;
+      h->par ^= m & 1;
+    } else if (h->hflags->halt == mdg::kHaltOverflow) {
+      done += completed - 1;
+      status = recover_overflow(h, true);
+      h->steps_host = (long long)h->hflags->steps - 1;
+      h->par ^= (int)((completed - 1) & 1);
+    } else {
+      status = halt_error(h);
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (step_ms) *step_ms = t_step;
+  if (rebuild_ms) *rebuild_ms = t_rebuild;
+  if (all_ms) *all_ms = t_all;
+  if (status == MDG_OK && done != nsteps) return fail(h, MDG_ERR_CAPACITY, "neighbour list could not be sized");
+  return status;
+}
+
+// Steps as plain launches with three events per step on the handle's stream
+// (graphs off): before the rebuild sequence, before the step kernel, after
+// it.  Sums the device time of the step kernels (force, kick, drifts), of
+// the rebuild sequences (wrap, bin, sort, list build; empty launches when none
+// is due) and of the whole run.
 int profiled_run(mdg_handle *h, int32_t nsteps, double *step_ms, double *rebuild_ms, double *all_ms) {
   if (h->prm.thermostat == MDG_NOSEHOOVER && h->nh_init) {
     mdg::launch_nh_init(h->g, h->d, h->stream);
     h->launches += 2;
     h->nh_init = false;
   }
+  if (h->prm.use_graphs) return timed_graph_run(h, nsteps, step_ms, rebuild_ms, all_ms);
   constexpr int kChunk = 64;
   cudaEvent_t ev[3 * kChunk];
   for (int k = 0; k < 3 * kChunk; k++) MDG_CK(cudaEventCreate(&ev[k]));
@@ -772,8 +852,8 @@ int mdg_observe(mdg_handle *h, double out[3]) {
   if (!out) return fail(h, MDG_ERR_INVALID, "null output");
   rc = ensure_list(h, false);
   if (rc) return rc;
-  mdg::launch_observe(h->g, h->d, h->dobs, h->stream, h->prm.precision == MDG_MIXED, h->par);
-  h->launches += h->prm.precision == MDG_MIXED ? 3 : 2;
+  mdg::launch_observe(h->g, h->d, h->dobs, h->stream, h->prm.precision != MDG_FP64, h->par);
+  h->launches += h->prm.precision != MDG_FP64 ? 3 : 2;
   MDG_CK(cudaMemcpyAsync(h->hobs, h->dobs, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   out[0] = h->hobs[0];
@@ -789,7 +869,7 @@ int mdg_forces(mdg_handle *h, double *f4) {
   rc = ensure_list(h, false);
   if (rc) return rc;
   mdg::launch_forces(h->g, h->d, h->prm.precision, h->par, h->stream);
-  h->launches += h->prm.precision == MDG_MIXED ? 2 : 1;
+  h->launches += h->prm.precision != MDG_FP64 ? 2 : 1;
   MDG_CK(cudaMemcpyAsync(f4, h->d.io4, (size_t)h->g.n * sizeof(double4_32a), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   return MDG_OK;
