@@ -8,25 +8,36 @@ step of the whole box: list rebuild when due, fused force/kick/drift kernel.
 Inputs are synthetic (seeded lattice + velocities); they are larger than L2
 (positions, momenta and the neighbour list total > 2 GB), so no flush is needed.
 
-value     mixed-form atom-steps/s over K steps, device time (CUDA events on the
-          library's stream), max over ranks, summed over ranks.
+value     mixed-form atom-steps/s over K steps (pair force in f32, per-atom
+          force sums in compensated f32, state and energy sums in f64), device
+          time: the K steps replay the library's step graph with CUDA event
+          nodes around every step kernel (mdg_calculate_profiled), max over
+          ranks, summed over ranks.  `mixed_plain` (plain f32 force sums) and
+          `fp64` blocks are measured the same way; each reports the list
+          rebuilds inside its window, and when there were none, a
+          rebuild-amortised figure (rebuild time x rebuild rate measured over
+          the next 400 steps, added to the window's time per step).
 e2e       the same through the public C ABI from host memory: pinned host state
           uploaded with mdg_set_state, K calls of mdg_calculate(1), mdg_observe
           every 100 steps (as Benchmark::Run observes), state read back with
           mdg_get_state; wall clock.
-roofline  the fused step kernel (mixed): algorithmic bytes per launch
-          n * (pairs_per_atom * 20 B + 72 B) over its mean launch time from a
-          CUDA-event-bracketed pass of the same workload; pairs_per_atom is the
-          inner list in ordinary steps and the outer list (+ 4 B per inner
-          entry written) in the steps that re-select the inner list, averaged
-          over the pass.  traffic: DRAM bytes per launch from the committed
-          ncu captures of both variants, weighted the same way.
+roofline  the fused step kernel (mixed) over the same K steps: its mean launch
+          time from the window's event nodes; achieved = DRAM bytes per launch
+          (an ncu capture of the same kernel, per atom, scaled by the atoms and
+          weighted by the window's ordinary / re-selecting launches) over that
+          time; frac = achieved / the measured HBM copy bandwidth.  The pair
+          model's algorithmic bytes (20 B per walked pair + 72 B per atom) are
+          reported beside it as algorithmic_gbs / algorithmic_frac: the
+          partner gathers they count are mostly served by L1/L2.
 --impl reference  the reference's CPU implementation on the host cores: the
           reference binary built from its sources when present (oracle/_ref),
           else the oracle's C restatement, with all host threads.
+--workload drift10k  the same box for 10,000 steps in each form with the
+          energy drift per atom per tau.
 
 Multi-GPU: independent replica boxes, one per rank (no collective on the data
-path); scaling is weak.
+path); scaling is weak.  `--gpus N` without torchrun's environment starts N
+ranks itself under torch.distributed.run.
 """
 import argparse
 import json
@@ -56,8 +67,9 @@ def parse():
                     help="number density of the NVE workload (the large configuration runs 0.5 and 0.8)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
     ap.add_argument("--workload", default="nve4m",
-                    choices=["nve4m", "langevin16m", "batch1024", "adjoint4k", "io4m", "init16m"],
-                    help="nve4m: the headline (4M atoms NVE); langevin16m: 160^3 FCC Langevin NVT; "
+                    choices=["nve4m", "drift10k", "langevin16m", "batch1024", "adjoint4k", "io4m", "init16m"],
+                    help="nve4m: the headline (4M atoms NVE); drift10k: the same box 10,000 steps per form with "
+                         "its energy drift; langevin16m: 160^3 FCC Langevin NVT; "
                          "batch1024: 1024 replica boxes; adjoint4k: 4000-atom trajectory gradient; "
                          "io4m: the reference's dump and stream files of the 4M-atom state; "
                          "init16m: the reference's exact-density initial state of the 16.4M-atom box, on the device")
@@ -65,10 +77,15 @@ def parse():
 
 
 class Dist:
+    """The ranks of the job (torchrun's environment; one process when unset).
+    `n` is the rank count asked for with --gpus and must match."""
+
     def __init__(self, n):
         self.rank = int(os.environ.get("RANK", "0"))
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        if n != self.world:
+            raise SystemExit("bench.py: --gpus %d but WORLD_SIZE is %d" % (n, self.world))
         self.pg = None
         if self.world > 1:
             import torch.distributed as dist
@@ -80,11 +97,17 @@ class Dist:
             self.pg.barrier()
 
     def max(self, v):
+        return self._reduce(v, "MAX")
+
+    def sum(self, v):
+        return self._reduce(v, "SUM")
+
+    def _reduce(self, v, op):
         if not self.pg:
             return v
         import torch
         t = torch.tensor([float(v)], dtype=torch.float64)
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        self.pg.all_reduce(t, op=getattr(self.pg.ReduceOp, op))
         return float(t.item())
 
     def close(self):
@@ -160,22 +183,27 @@ def ncu_traffic_per_atom(form):
 
 
 def cpu_sample(q, p, L, budget_s, threads, prefer_reference=True):
-    """Times the reference CPU path on the same workload; returns (atom-steps/s, descr)."""
+    """Times the reference CPU path on the same workload; returns
+    (atom-steps/s, kind, description, threads used)."""
     n = len(q)
     from oracle import refrun
-    if prefer_reference and refrun.available(RC):
-        # the reference itself, timed like Benchmark::Run (list build outside,
-        # observation every ObserveLoop=100 steps inside); a 2-step probe sizes the run
+    if prefer_reference and refrun.available(RC, bench=True):
+        # the reference itself (built from its sources on this host, -O3
+        # -fopenmp), one MDUnit per OpenMP thread on the grid the reference
+        # derives from the thread count, timed like Benchmark::Run (list build
+        # outside, observation every ObserveLoop=100 steps inside); a 2-step
+        # probe sizes the run
         def mups(steps):
             out = refrun.run("bench", q, p, L, rc=RC, margin=MARGIN, dt=DT, steps=steps, observe_every=100,
-                             threads=threads, timeout=max(600, int(budget_s * 20)))
+                             threads=threads, timeout=max(600, int(budget_s * 20)), bench=True)
             line = [x for x in out["stdout"].splitlines() if "[MUPS]" in x][-1]
             return float(line.split("[SEC]")[1].split("[MUPS]")[0])
         probe = mups(2)
-        steps = max(2, min(100, int(budget_s * probe * 1e6 / n)))
+        steps = max(2, min(200, int(budget_s * probe * 1e6 / n)))
         v = mups(steps) * 1e6
-        return v, "reference", "MDACP reference binary, %d steps of the full %d-atom box, %d threads" % (
-            steps, n, threads)
+        return v, "reference", ("MDACP reference binary built here from its sources (g++ -O3 -fopenmp), %d steps "
+                                "of the full %d-atom box, %d OpenMP threads = %d MDUnits" % (
+                                    steps, n, threads, threads)), threads
     from oracle import port
     s = port.System(q, p, L, rc=RC, margin=MARGIN, dt=DT, threads=threads)
     s.make_pairlist()
@@ -188,33 +216,57 @@ def cpu_sample(q, p, L, budget_s, threads, prefer_reference=True):
     dt = time.perf_counter() - t0
     s.close()
     return n * steps / dt, "port", "oracle C restatement (half list, Newton-3), %d steps of the full %d-atom box, %d threads" % (
-        steps, n, threads)
+        steps, n, threads), threads
 
 
 def run_reference(args):
     d = Dist(args.gpus)
+    ranks = d.sum(1)  # every rank joined the job
     if d.rank != 0:
         d.close()
         return
     q, p, L = workload(args.cells, 1, args.density)
     threads = os.cpu_count() or 1
-    value, kind, descr = cpu_sample(q, p, L, args.cpu_seconds, threads)
+    value, kind, descr, cores = cpu_sample(q, p, L, args.cpu_seconds, threads)
     n = len(q)
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / value,
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world,
+            "ranks_joined": int(ranks), "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config_block(args, n),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": descr},
+            "data": "synthetic", "config": config_block(args, n, d.world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": descr},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     d.close()
 
 
-def config_block(args, n):
+def config_block(args, n, world):
     return {"workload": "LJ NVE %d atoms (%d^3 FCC), rho %.1f, rc %.1f, margin %.1f, dt %g, T %.1f" % (
         n, args.cells, args.density, RC, MARGIN, DT, TEMP), "atoms": n, "density": args.density, "cutoff": RC,
-        "margin": MARGIN, "dt": DT, "precision": "mixed (value) / fp64 (fp64 block)",
-        "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas x%d" % args.gpus}
+        "margin": MARGIN, "dt": DT,
+        "precision": "mixed: compensated f32 force sums (value); mixed_plain and fp64 blocks beside it",
+        "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas x%d" % world}
+
+
+DTYPE = {"mixed": "f32 pair distance/force, compensated (Kahan) f32 per-atom force sums, f64 state/integration/"
+                  "energy-virial sums",
+         "mixed_plain": "f32 pair distance/force, plain f32 per-atom force sums, f64 state/integration/energy-virial "
+                        "sums",
+         "fp64": "f64"}
+
+
+def timed_window(m, d, K):
+    """K steps of handle m replayed from the step graph with event nodes around
+    every step kernel (mdg_calculate_profiled's path); returns the window's
+    device ms (max over ranks), the step kernels' summed ms and the counters
+    that moved inside the window."""
+    s0 = m.stats()
+    d.barrier()
+    ph = m.calculate_phases(K)
+    d.barrier()
+    s1 = m.stats()
+    return {"ms": d.max(ph["all"]), "kernel_ms": ph["force"], "rebuild_ms": ph["pair"],
+            "rebuilds": s1["rebuilds"] - s0["rebuilds"], "prunes": s1["prunes"] - s0["prunes"],
+            "launches": s1["kernel_launches"] - s0["kernel_launches"], "stats": s1}
 
 
 def run_mine(args):
@@ -227,67 +279,70 @@ def run_mine(args):
     res = {}
     clk = Clocks(d.local)
     clocks = None
-    for prec in ("mixed", "fp64"):
+    for prec in ("mixed", "mixed_plain", "fp64"):
         m = MDManager(L, capacity=n, cutoff=RC, margin=MARGIN, dt=DT, precision=prec, device=d.local)
         m.set_state(q, p)
         m.make_pairlist()
         m.calculate(W)
         e0 = m.observe()[2]
-        launches0 = m.stats()["kernel_launches"]
-        d.barrier()
         if prec == "mixed":
             clk.start()
-        m.calculate(K)
-        st = m.stats()
+        w = timed_window(m, d, K)
         if prec == "mixed":
             clocks = clk.stop()
-        d.barrier()
-        ms = d.max(st["elapsed_ms"])
         e1 = m.observe()[2]
-        res[prec] = {"ms": ms, "launches": st["kernel_launches"] - launches0, "rebuilds": st["rebuilds"],
-                     "pairs_per_atom": st["listed_pairs"] / n, "drift": (e1 - e0) / (K * DT),
-                     "inner_pairs_per_atom": st["inner_pairs"] / n, "prunes": st["prunes"],
-                     "handle": m, "stats": st}
-    # force error of the mixed form against FP64 at the same (warmed-up) state
-    mf, md = res["mixed"]["handle"], res["fp64"]["handle"]
+        w.update({"drift": (e1 - e0) / (K * DT), "handle": m})
+        if w["rebuilds"] == 0:
+            # no list rebuild fell inside the window: the rebuild cost per step
+            # is measured over a longer continuation of the same run (rebuild
+            # time x rebuild rate) and added to the window's time per step
+            R = 400
+            a = timed_window(m, d, R)
+            w["amortised"] = {"steps": R, "rebuilds": a["rebuilds"], "rebuild_ms_per_step": a["rebuild_ms"] / R,
+                              "ms_per_step": w["ms"] / K + a["rebuild_ms"] / R}
+        res[prec] = w
+    # force error of both mixed forms against FP64 at the same (warmed-up) state
+    md = res["fp64"]["handle"]
     qs, ps = md.state()
-    mf.set_state(qs, ps)
-    f_mixed = mf.forces()
     f_fp64 = md.forces()
-    rel = np.linalg.norm(f_mixed - f_fp64, axis=1) / np.maximum(np.linalg.norm(f_fp64, axis=1), 1e-300)
-    rms_err = float(np.sqrt(np.mean(rel ** 2)))
-    # roofline of the fused step kernel (mixed form)
-    kprof = max(50, min(K, 500))
-    mf.make_pairlist()
-    mf.calculate(W)
-    s0 = mf.stats()
-    kernel_ms = mf.calculate_profiled(kprof) / kprof
-    s1 = mf.stats()
-    # pairs the kernel walks: the inner list in an ordinary step (its size at
-    # the end of the pass), the outer list in a re-selecting step, which also
-    # writes the inner rows (4 B per kept entry)
-    ppa = s1["inner_pairs"] / n
-    opa = s1["listed_pairs"] / n
-    n_sel = min(max(s1["prunes"] - s0["prunes"], 0), kprof)
-    alg_bytes = n * ((kprof - n_sel) * (ppa * 20.0 + 72.0) + n_sel * (opa * 20.0 + ppa * 4.0 + 72.0)) / kprof
+    for prec in ("mixed", "mixed_plain"):
+        mf = res[prec]["handle"]
+        mf.set_state(qs, ps)
+        f = mf.forces()
+        rel = np.linalg.norm(f - f_fp64, axis=1) / np.maximum(np.linalg.norm(f_fp64, axis=1), 1e-300)
+        res[prec]["rms_err"] = float(np.sqrt(np.mean(rel ** 2)))
+    for prec in res:
+        res[prec]["handle"].close()
+    mixed = res["mixed"]
+    # roofline of the fused step kernel (mixed form), from the window itself:
+    # the mean step-kernel time of its K steps against (a) the DRAM bytes an
+    # ncu capture of the same kernel measured per atom and (b) the algorithmic
+    # bytes of the pair model (20 B per walked pair + 72 B per atom), most of
+    # whose partner gathers are served by L1/L2
+    st = mixed["stats"]
+    kernel_ms = mixed["kernel_ms"] / K
+    ppa, opa = st["inner_pairs"] / n, st["listed_pairs"] / n
+    n_sel = min(max(mixed["prunes"], 0), K)
+    alg_bytes = n * ((K - n_sel) * (ppa * 20.0 + 72.0) + n_sel * (opa * 20.0 + ppa * 4.0 + 72.0)) / K
     peak, peak_kind = peaks()
-    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
-    # DRAM bytes per launch from the committed ncu captures of both variants,
-    # weighted by how many steps of the pass re-selected the inner list
     t_ord, t_sel = ncu_traffic_per_atom("mixed"), ncu_traffic_per_atom("mixed_reselect")
     tpa = None
     if t_ord and t_sel and abs(args.density - DENSITY) < 1e-12:  # the captures are of density 0.5
-        tpa = ((kprof - n_sel) * t_ord + n_sel * t_sel) / kprof
-    roof = {"kernel": "k_step<NVE,mixed>", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": (tpa * n) if tpa else None, "algorithmic_bytes": alg_bytes,
-            # the same launch time against the ncu DRAM bytes (what HBM itself moved)
-            "dram_gbs": (tpa * n / (kernel_ms * 1e-3) / 1e9) if tpa else None,
-            "dram_frac": (tpa * n / (kernel_ms * 1e-3) / 1e9 / peak) if tpa else None,
-            "launch_ms": kernel_ms, "pairs_per_atom": ppa, "listed_pairs_per_atom": s1["listed_pairs"] / n,
-            "prunes_in_pass": s1["prunes"] - s0["prunes"], "rebuilds_in_pass": s1["rebuilds"] - s0["rebuilds"]}
-    for prec in ("mixed", "fp64"):
-        res[prec]["handle"].close()
+        tpa = ((K - n_sel) * t_ord + n_sel * t_sel) / K
+    dram_gbs = tpa * n / (kernel_ms * 1e-3) / 1e9 if tpa else None
+    alg_gbs = alg_bytes / (kernel_ms * 1e-3) / 1e9
+    roof = {"kernel": "k_step<NVE,mixed>", "bound": "hbm", "achieved": dram_gbs, "peak": peak, "unit": "GB/s",
+            "frac": dram_gbs / peak if dram_gbs else None,
+            "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": tpa * n if tpa else None,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per atom of one launch "
+                              "(profiles/step_kernel_traffic.json), x atoms, weighted by the window's "
+                              "ordinary/re-selecting launches",
+            "launch_ms": kernel_ms, "launches_timed": K, "window_ms_per_step": mixed["ms"] / K,
+            "algorithmic_bytes": alg_bytes, "algorithmic_gbs": alg_gbs, "algorithmic_frac": alg_gbs / peak,
+            "algorithmic_note": "pair model (20 B per walked pair + 72 B per atom); counts partner gathers "
+                                "served by L1/L2, so it can exceed the DRAM figure",
+            "pairs_per_atom": ppa, "listed_pairs_per_atom": opa, "reselecting_launches": n_sel}
     # end to end through the C ABI with host buffers
     import torch
     qh = torch.zeros((n, 4), dtype=torch.float64).pin_memory().numpy()
@@ -311,30 +366,44 @@ def run_mine(args):
             nobs += 1
     me.state(qo, po)
     t_e2e = d.max(time.perf_counter() - t0)
+    e2e_rebuilds = me.stats()["rebuilds"]
     me.close()
     e2e_value = d.world * n * K / t_e2e
     cpu = None
     if d.rank == 0 and d.world == 1:
-        v, kind, descr = cpu_sample(q, p, L, args.cpu_seconds, os.cpu_count() or 1)
-        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": kind, "sample": descr}
-    mixed, fp64 = res["mixed"], res["fp64"]
+        v, kind, descr, cores = cpu_sample(q, p, L, args.cpu_seconds, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": descr}
     value = d.world * n * K / (mixed["ms"] * 1e-3)
-    v64 = d.world * n * K / (fp64["ms"] * 1e-3)
+
+    def form(r):
+        out = {"value": d.world * n * K / (r["ms"] * 1e-3), "unit": UNIT, "ms_per_step": r["ms"] / K,
+               "step_kernel_ms": r["kernel_ms"] / K, "rebuilds_in_window": r["rebuilds"],
+               "reselections_in_window": r["prunes"],
+               "energy_drift_per_atom_per_tau_window": r["drift"]}
+        if "amortised" in r:
+            a = r["amortised"]
+            out["rebuild_amortised"] = dict(a, value=d.world * n / (a["ms_per_step"] * 1e-3))
+        if "rms_err" in r:
+            out["rms_rel_force_err_vs_fp64"] = r["rms_err"]
+        return out
+
     if d.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world, "steps": K, "warmup": W,
                 "ms_per_step": mixed["ms"] / K, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32 pair force / f64 accumulate-integrate", "data": "synthetic",
-                "config": config_block(args, n),
-                "fp64": {"value": v64, "unit": UNIT, "ms_per_step": fp64["ms"] / K,
-                         "energy_drift_per_atom_per_tau": fp64["drift"], "rebuilds": fp64["rebuilds"]},
-                "mixed_over_fp64": value / v64,
-                "mixed": {"rms_rel_force_err_vs_fp64": rms_err, "energy_drift_per_atom_per_tau": mixed["drift"],
-                          "rebuilds": mixed["rebuilds"], "pairs_per_atom": mixed["pairs_per_atom"],
-                          "inner_pairs_per_atom": mixed["inner_pairs_per_atom"], "prunes": mixed["prunes"]},
+                "vs_baseline": None, "dtype": DTYPE["mixed"], "data": "synthetic",
+                "config": config_block(args, n, d.world),
+                "rebuilds_in_window": mixed["rebuilds"],
+                "mixed": form(mixed), "mixed_plain": form(res["mixed_plain"]), "fp64": form(res["fp64"]),
+                "mixed_over_fp64": res["fp64"]["ms"] / mixed["ms"],
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 32 / K,
-                        "d2h_bytes_per_step": (2 * n * 32 + 24 * nobs) / K},
+                        "d2h_bytes_per_step": (2 * n * 32 + 24 * nobs) / K, "rebuilds": e2e_rebuilds},
                 "gpu_launches": mixed["launches"],
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clocks}
+        if "amortised" in mixed:
+            line["value_rebuild_amortised"] = line["mixed"]["rebuild_amortised"]["value"]
+            line["mixed_over_fp64_rebuild_amortised"] = (res["fp64"]["amortised"]["ms_per_step"] /
+                                                         mixed["amortised"]["ms_per_step"]
+                                                         if "amortised" in res["fp64"] else None)
         print(json.dumps(line), flush=True)
     d.close()
 
@@ -343,6 +412,48 @@ def base_line(metric, value, n_gpus, K, W, ms, config, dtype):
     return {"metric": metric, "value": value, "unit": UNIT, "n_gpus": n_gpus, "steps": K, "warmup": W,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic", "config": config}
+
+
+def run_drift10k(args):
+    """The large NVE configuration run for 10,000 steps in each form (FP64,
+    compensated mixed, plain mixed) from the same state: total energy per atom
+    observed every 100 steps; drift = least-squares slope of E/N against time
+    (per atom per tau) and the end-to-start difference over the run time."""
+    import numpy as np
+    from mdacp_gb300.manager import MDManager
+    q, p, L = workload(args.cells, 1, args.density)
+    n = len(q)
+    K = args.steps if args.steps != 1000 else 10000
+    every = 100
+    out = {}
+    for prec in ("fp64", "mixed", "mixed_plain"):
+        m = MDManager(L, capacity=n, cutoff=RC, margin=MARGIN, dt=DT, precision=prec)
+        m.set_state(q, p)
+        m.make_pairlist()
+        t, E = [0.0], [m.observe()[2]]
+        dev_ms = 0.0
+        for k in range(K // every):
+            m.calculate(every)
+            dev_ms += m.stats()["elapsed_ms"]
+            t.append((k + 1) * every * DT)
+            E.append(m.observe()[2])
+        st = m.stats()
+        m.close()
+        t, E = np.array(t), np.array(E)
+        slope = float(np.polyfit(t, E, 1)[0])
+        out[prec] = {"energy_drift_per_atom_per_tau": slope,
+                     "energy_change_per_atom_per_tau": float((E[-1] - E[0]) / (t[-1] - t[0])),
+                     "E_start": float(E[0]), "E_end": float(E[-1]), "E_rms_fluct": float(np.std(E - np.polyval(np.polyfit(t, E, 1), t))),
+                     "value": n * K / (dev_ms * 1e-3), "ms_per_step": dev_ms / K, "rebuilds": st["rebuilds"],
+                     "reselections": st["prunes"]}
+    cfg = {"workload": "LJ NVE %d atoms (%d^3 FCC), rho %.1f, rc %.1f, margin %.1f, dt %g, T %.1f, %d steps, "
+                       "E observed every %d" % (n, args.cells, args.density, RC, MARGIN, DT, TEMP, K, every),
+           "atoms": n, "density": args.density, "l2": "inputs larger than L2 (no flush)"}
+    line = base_line("LJ atom-steps/s over a 10,000-step NVE run with energy drift, 4M atoms", out["mixed"]["value"],
+                     1, K, 0, out["mixed"]["ms_per_step"], cfg, DTYPE["mixed"])
+    line.update(out)
+    line["mixed_over_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    print(json.dumps(line), flush=True)
 
 
 def run_langevin16m(args):
@@ -376,7 +487,7 @@ def run_langevin16m(args):
            % (n, cells), "atoms": n, "l2": "inputs larger than L2 (no flush)"}
     v = n * K / (res["mixed"]["ms"] * 1e-3)
     line = base_line("LJ atom-steps/s, 16.4M atoms Langevin NVT: mixed vs FP64 on 1 GB300", v, 1, K, W,
-                     res["mixed"]["ms"] / K, cfg, "f32 pair force / f64 accumulate-integrate")
+                     res["mixed"]["ms"] / K, cfg, DTYPE["mixed"])
     line.update({"fp64": {"value": n * K / (res["fp64"]["ms"] * 1e-3), "ms_per_step": res["fp64"]["ms"] / K,
                           "rebuilds": res["fp64"]["rebuilds"], "T_end": res["fp64"]["T_end"]},
                  "mixed": res["mixed"], "clocks": clocks})
@@ -404,7 +515,7 @@ def run_batch1024(args):
                        "rc 2.5, margin 0.4, dt 0.002" % n, "atoms": n, "boxes": 1024}
     v = n * K / (res["mixed"]["ms"] * 1e-3)
     line = base_line("LJ atom-steps/s, 1024 batched replicas: mixed vs FP64 on 1 GB300", v, 1, K, W,
-                     res["mixed"]["ms"] / K, cfg, "f32 pair force / f64 accumulate-integrate")
+                     res["mixed"]["ms"] / K, cfg, DTYPE["mixed"])
     line.update({"fp64": {"value": n * K / (res["fp64"]["ms"] * 1e-3), "ms_per_step": res["fp64"]["ms"] / K,
                           "shape": res["fp64"]["shape"]}, "mixed": res["mixed"]})
     print(json.dumps(line), flush=True)
@@ -512,11 +623,28 @@ def run_init16m(args):
     print(json.dumps(line), flush=True)
 
 
+def launch_ranks(n):
+    """Runs this command as n ranks under torch.distributed.run (one process
+    per GPU, rendezvous on 127.0.0.1) and returns its exit status; rank 0
+    prints the JSON line."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args.gpus))
     if args.impl == "mdg" and args.workload != "nve4m":
+        if int(os.environ.get("RANK", "0")) != 0:  # single-GPU workloads: rank 0 runs them
+            return
         {"langevin16m": run_langevin16m, "batch1024": run_batch1024, "adjoint4k": run_adjoint4k,
-         "io4m": run_io4m, "init16m": run_init16m}[args.workload](args)
+         "io4m": run_io4m, "init16m": run_init16m, "drift10k": run_drift10k}[args.workload](args)
         return
     if args.impl == "reference":
         run_reference(args)
