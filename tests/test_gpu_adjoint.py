@@ -67,6 +67,44 @@ def test_adjoint_matches_finite_differences_c5(objective):
         assert abs(gq[i, k] - fd) <= 1e-4 * abs(fd), (i, k, gq[i, k], fd)
 
 
+@pytest.mark.parametrize("objective", ["pe", "pressure"])
+def test_adjoint_finite_differences_margin_half(objective):
+    """The C5 case at the list margin of the large NVE runs (0.5, a new list
+    every 20-step segment): epsilon, sigma, the three largest components of
+    dJ/dq0 and three drawn from the larger half, against central differences
+    (h = 1e-6 for epsilon and sigma, 1e-5 for positions, so the rounding of J
+    stays far below the difference of the smaller components)."""
+    from mdacp_gb300.adjoint import Adjoint
+    q, p, L = _c5(seed=6)
+    n, h = len(q), 1e-6
+    kw = dict(steps=200, checkpoint_every=20, dt=0.002, margin=0.5, objective=objective)
+    a = Adjoint(L, n, **kw)
+    a.forward(q, p)
+    gq, gp, ge, gs = a.backward()
+    a.close()
+
+    def Jp(eps=1.0, sig=1.0, q0=q):
+        b = Adjoint(L, n, epsilon=eps, sigma=sig, **kw)
+        v = b.forward(q0, p)
+        b.close()
+        return v
+
+    fd_e = (Jp(eps=1 + h) - Jp(eps=1 - h)) / (2 * h)
+    fd_s = (Jp(sig=1 + h) - Jp(sig=1 - h)) / (2 * h)
+    assert abs(ge - fd_e) <= 1e-4 * abs(fd_e), (ge, fd_e)
+    assert abs(gs - fd_s) <= 1e-4 * abs(fd_s), (gs, fd_s)
+    order = np.argsort(-np.abs(gq).ravel())
+    picks = list(order[:3]) + list(np.random.default_rng(2).choice(order[3:len(order) // 2], 3, replace=False))
+    hq = 1e-5
+    for f in picks:
+        i, k = divmod(int(f), 3)
+        qp_, qm_ = q.copy(), q.copy()
+        qp_[i, k] += hq
+        qm_[i, k] -= hq
+        fd = (Jp(q0=qp_) - Jp(q0=qm_)) / (2 * hq)
+        assert abs(gq[i, k] - fd) <= 1e-4 * abs(fd), (i, k, gq[i, k], fd)
+
+
 def test_autograd_function_wrapper():
     import torch
     from mdacp_gb300.adjoint import Adjoint

@@ -1,6 +1,7 @@
 """Batched replicas: every box of a batch against the oracle run on that box alone.
 
-Boxes of uneven size (500..2000 atoms here), density 0.3..0.9 (so some boxes
+Boxes of uneven size (500..8000 atoms, the batched configuration's range, in
+the FP64 comparison; 500..2000 elsewhere), density 0.3..0.9 (so some boxes
 have only two cells per side) and temperature 0.7..1.5, rc 2.5, margin 0.4,
 dt 0.002.  FP64: per-box observables rtol 1e-10 after 100 steps; mixed: within
 1e-5 of FP64; overflow regrowth; autotuner leaves the state unchanged.
@@ -15,10 +16,10 @@ pytestmark = pytest.mark.gpu
 RC, MARGIN, DT = 2.5, 0.4, 0.002
 
 
-def _boxes(nbox=12, seed=3):
+def _boxes(nbox=12, seed=3, n_range=(500, 2000)):
     """nbox drawn boxes plus one 500-atom box at density 0.9 (L = 8.2: two cells per side)."""
     from mdacp_gb300.batch import make_replicas
-    return make_replicas(nbox, seed=seed, n_range=(500, 2000)) + make_replicas(
+    return make_replicas(nbox, seed=seed, n_range=n_range) + make_replicas(
         1, seed=seed + 1000, n_range=(500, 500), rho_range=(0.9, 0.9))
 
 
@@ -34,8 +35,9 @@ def _oracle_obs(boxes, steps):
 
 def test_batch_fp64_matches_oracle_per_box():
     from mdacp_gb300.batch import Batch
-    boxes = _boxes()
+    boxes = _boxes(16, n_range=(500, 8000))
     assert any(L[0] < 3 * (RC + MARGIN) for _, _, L in boxes)   # two cells per side occurs
+    assert max(len(q) for q, _, _ in boxes) > 6000
     b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT)
     b.calculate(100)
     np.testing.assert_allclose(b.observe_raw(), _oracle_obs(boxes, 100), rtol=1e-10, atol=1e-10)
@@ -43,11 +45,12 @@ def test_batch_fp64_matches_oracle_per_box():
     assert st["steps"] == 100 and st["rebuilds"] >= len(boxes)
 
 
-def test_batch_mixed_close_to_fp64():
+@pytest.mark.parametrize("precision", ["mixed", "mixed_plain"])
+def test_batch_mixed_close_to_fp64(precision):
     from mdacp_gb300.batch import Batch
-    boxes = _boxes(8, seed=5)
+    boxes = _boxes(8, seed=5, n_range=(500, 8000))
     a = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision="fp64")
-    m = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision="mixed")
+    m = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision=precision)
     a.calculate(50)
     m.calculate(50)
     np.testing.assert_allclose(m.observe_raw(), a.observe_raw(), rtol=1e-5, atol=1e-5)
@@ -89,11 +92,14 @@ def test_autotuner_restores_state():
                                                                  boxes)], 30), rtol=1e-10, atol=1e-10)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed_plain", "mixed"])
 def test_inner_list_changes_nothing(precision):
     # the inner rows keep the outer rows' order and drop only pairs beyond rc,
     # whose terms are exactly zero: the trajectories agree bit for bit, also
-    # when a tiny buffer makes the boxes re-select every few steps
+    # when a tiny buffer makes the boxes re-select every few steps.  With
+    # compensated sums (mixed) a zero term leaves the compensated value
+    # unchanged but re-normalises the correction, so the runs agree to the
+    # rounding of the sums (relative 1e-9 after 80 steps), not bit for bit
     from mdacp_gb300.batch import Batch
     boxes = _boxes(6, seed=13)
     runs = []
@@ -113,4 +119,7 @@ def test_inner_list_changes_nothing(precision):
     runs.append([x.copy() for pair in b.state() for x in pair])
     for other in runs[1:]:
         for u, v in zip(runs[0], other):
-            assert np.array_equal(u, v)
+            if precision == "mixed":
+                np.testing.assert_allclose(v, u, rtol=1e-9, atol=1e-9)
+            else:
+                assert np.array_equal(u, v)
