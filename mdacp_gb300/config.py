@@ -8,13 +8,24 @@ numeric prefix, 0 when none), booleans true only for `yes` / `Yes`.
 SimulationInfo follows simulationinfo.cc:5-51 for the reference keys and adds
 the keys of this engine, whose defaults keep the reference behaviour:
   CutoffLength (3.0, CUTOFF_LENGTH of mdconfig.h:15), BufferLength (0.3,
-  simulationinfo.cc:6), Precision (fp64|mixed), Device (gpu), Replicas,
-  RebuildPolicy (halfmargin), LangevinHalfDriftCompat (yes).
+  simulationinfo.cc:6), Precision (fp64|mixed|mixed_plain), Device (gpu or
+  gpu:<ordinal>), RebuildPolicy (halfmargin, the only policy on the device),
+  LangevinHalfDriftCompat (yes).
 """
 import re
 
 _NUM = re.compile(r"^[ \t\n\v\f\r]*([+-]?(\d+(\.\d*)?|\.\d+)([eE][+-]?\d+)?)")
 _INT = re.compile(r"^[ \t\n\v\f\r]*([+-]?\d+)")
+
+
+def parse_device(value):
+    """Device=gpu or gpu:<ordinal> -> the CUDA device ordinal.  The engine runs
+    only on the GPU; Device=cpu is the reference's own path."""
+    if value == "gpu":
+        return 0
+    if value.startswith("gpu:") and value[4:].isdigit():
+        return int(value[4:])
+    raise ValueError("Device=%s: this engine runs on the GPU (Device=gpu or gpu:<ordinal>)" % value)
 
 
 def atof(s):
@@ -95,11 +106,14 @@ class SimulationInfo:
                 L[k] = param.get_double(key)
         self.L = L
         self.precision = param.get_string("Precision", "fp64")
-        if self.precision not in ("fp64", "mixed"):
-            raise ValueError("Precision must be fp64 or mixed")
-        self.device = param.get_string("Device", "gpu")
-        self.replicas = param.get_int("Replicas", 1)
+        if self.precision not in ("fp64", "mixed", "mixed_plain"):
+            raise ValueError("Precision must be fp64, mixed or mixed_plain")
+        self.device = parse_device(param.get_string("Device", "gpu"))
         self.rebuild_policy = param.get_string("RebuildPolicy", "halfmargin")
+        if self.rebuild_policy != "halfmargin":
+            raise ValueError("RebuildPolicy=%s: the device rebuilds when a particle moved more than half the "
+                             "margin (halfmargin); the reference's buffer-budget policy runs in the reference's "
+                             "own CPU path" % self.rebuild_policy)
         self.langevin_half_drift_compat = param.get_bool("LangevinHalfDriftCompat", True)
 
     @property

@@ -75,8 +75,20 @@ SimulationInfo::SimulationInfo(const Parameter &p) {
   const std::string prec = p.GetStringDef("Precision", "fp64");
   if (prec == "fp64") Precision = MDG_FP64;
   else if (prec == "mixed") Precision = MDG_MIXED;
-  else throw std::runtime_error("Precision must be fp64 or mixed");
+  else if (prec == "mixed_plain") Precision = MDG_MIXED_PLAIN;
+  else throw std::runtime_error("Precision must be fp64, mixed or mixed_plain");
   LangevinHalfDriftCompat = p.GetBooleanDef("LangevinHalfDriftCompat", true);
+  // keys of this engine: the GPU only (Device=cpu is the reference's own
+  // path), and the half-margin rebuild rule only
+  const std::string dev = p.GetStringDef("Device", "gpu");
+  if (dev == "gpu") Device = 0;
+  else if (dev.rfind("gpu:", 0) == 0 && dev.size() > 4 && dev.find_first_not_of("0123456789", 4) == std::string::npos)
+    Device = atoi(dev.c_str() + 4);
+  else throw std::runtime_error("Device=" + dev + ": this engine runs on the GPU (Device=gpu or gpu:<ordinal>)");
+  const std::string policy = p.GetStringDef("RebuildPolicy", "halfmargin");
+  if (policy != "halfmargin")
+    throw std::runtime_error("RebuildPolicy=" + policy +
+                             ": the device rebuilds when a particle moved more than half the margin (halfmargin)");
 }
 
 MDManager::MDManager(const Parameter &param, int capacity) : sinfo_(param) {
@@ -94,7 +106,7 @@ MDManager::MDManager(const Parameter &param, int capacity) : sinfo_(param) {
   p.gamma = sinfo_.HeatbathGamma;
   p.tau = sinfo_.HeatbathTau;
   p.seed = (uint64_t)param.GetIntegerDef("Seed", 1);
-  p.device = param.GetIntegerDef("GpuDevice", 0);
+  p.device = sinfo_.Device;
   const int rc = mdg_create(&p, &h_);
   if (rc != MDG_OK)
     throw std::runtime_error("mdg_create failed (" + std::to_string(rc) + "): " + mdg_last_error(nullptr));

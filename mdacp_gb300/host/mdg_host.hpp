@@ -41,8 +41,9 @@ struct SimulationInfo {
   bool ControlTemperature;
   int HeatbathType;  // 0 NoseHoover, 1 Langevin
   double CutoffLength, BufferLength;
-  int Precision;     // MDG_FP64 / MDG_MIXED
+  int Precision;     // MDG_FP64 / MDG_MIXED / MDG_MIXED_PLAIN
   bool LangevinHalfDriftCompat;
+  int Device;        // CUDA ordinal from Device=gpu (0) or gpu:<ordinal>
 };
 
 // MDManager for one box (mdmanager.h:32-83).  Particles are staged on the

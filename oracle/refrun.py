@@ -14,18 +14,31 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 
 
-def binary(rc=2.5):
-    return os.path.join(REF_DIR, "mdacp_rc%.1f" % rc)
+SRC_DIR = os.path.join(REF_DIR, "src")
 
 
-def available(rc=2.5):
-    return os.path.exists(binary(rc))
+def binary(rc=2.5, bench=False):
+    """The parity binary for cut-off rc (no fused multiply-adds), or with
+    bench=True the timed-baseline build (the compiler's default contraction)."""
+    return os.path.join(REF_DIR, ("mdacp_bench_rc%.1f" if bench else "mdacp_rc%.1f") % rc)
+
+
+def available(rc=2.5, bench=False):
+    return os.path.exists(binary(rc, bench))
+
+
+def sources_available():
+    """The reference sources: MDG_REFERENCE_DIR, or the copy build_ref.sh
+    staged under oracle/_ref/src (which travels with a copy of this tree)."""
+    ref = os.environ.get("MDG_REFERENCE_DIR")
+    if ref and os.path.exists(os.path.join(ref, "mdconfig.h")):
+        return True
+    return os.path.exists(os.path.join(SRC_DIR, "mdconfig.h"))
 
 
 def build():
     """Builds the reference binaries when the reference sources are present."""
-    ref = os.environ.get("MDG_REFERENCE_DIR", "/root/reference")
-    if not os.path.exists(os.path.join(ref, "mdconfig.h")):
+    if not sources_available():
         return False
     subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
     return True
@@ -40,8 +53,10 @@ def write_input(path, q, p):
 
 
 def run(task, q, p, L, rc=2.5, margin=0.5, dt=0.001, steps=100, observe_every=10, threads=1,
-        extra=None, timeout=3600):
-    """Runs one Oracle task; returns a dict of numpy arrays (and 'stdout')."""
+        extra=None, timeout=3600, bench=False):
+    """Runs one Oracle task; returns a dict of numpy arrays (and 'stdout').
+    threads = OpenMP threads = MDUnits (the reference runs one unit per
+    thread, its local grid from MPI_Dims_create, parainfo.cc:29-35)."""
     L = np.broadcast_to(np.asarray(L, dtype=np.float64), (3,))
     with tempfile.TemporaryDirectory(prefix="mdacp_ref_") as d:
         write_input(os.path.join(d, "in.bin"), q, p)
@@ -55,7 +70,7 @@ def run(task, q, p, L, rc=2.5, margin=0.5, dt=0.001, steps=100, observe_every=10
         with open(os.path.join(d, "o.cfg"), "w") as f:
             f.write("\n".join(cfg) + "\n")
         env = dict(os.environ, OMP_NUM_THREADS=str(threads))
-        r = subprocess.run([binary(rc), "o.cfg"], cwd=d, env=env, capture_output=True, text=True,
+        r = subprocess.run([binary(rc, bench), "o.cfg"], cwd=d, env=env, capture_output=True, text=True,
                            timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError("reference failed: %s\n%s" % (r.stdout[-2000:], r.stderr[-2000:]))
