@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--density", type=float, default=DENSITY,
                     help="number density of the NVE workload (the large configuration runs 0.5 and 0.8)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--cpu-threads", type=int, default=0, help="host threads of the CPU baseline (0: all cores)")
     ap.add_argument("--workload", default="nve4m",
                     choices=["nve4m", "drift10k", "langevin16m", "batch1024", "adjoint4k", "io4m", "init16m"],
                     help="nve4m: the headline (4M atoms NVE); drift10k: the same box 10,000 steps per form with "
@@ -226,7 +227,7 @@ def run_reference(args):
         d.close()
         return
     q, p, L = workload(args.cells, 1, args.density)
-    threads = os.cpu_count() or 1
+    threads = args.cpu_threads or os.cpu_count() or 1
     value, kind, descr, cores = cpu_sample(q, p, L, args.cpu_seconds, threads)
     n = len(q)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world,
@@ -371,7 +372,7 @@ def run_mine(args):
     e2e_value = d.world * n * K / t_e2e
     cpu = None
     if d.rank == 0 and d.world == 1:
-        v, kind, descr, cores = cpu_sample(q, p, L, args.cpu_seconds, os.cpu_count() or 1)
+        v, kind, descr, cores = cpu_sample(q, p, L, args.cpu_seconds, args.cpu_threads or os.cpu_count() or 1)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": kind, "sample": descr}
     value = d.world * n * K / (mixed["ms"] * 1e-3)
 

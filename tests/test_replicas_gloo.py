@@ -65,3 +65,35 @@ def test_replicas_two_ranks_gloo():
     assert e0 != e1                                  # independent replicas
     value = 2 * n0 * 20 / m0
     assert np.isfinite(value) and value > 0
+
+
+def test_bench_starts_its_own_ranks():
+    # `bench.py --gpus 2` without torchrun's environment starts two ranks under
+    # torch.distributed.run (rendezvous on 127.0.0.1); both join the gloo group
+    # and rank 0 alone prints the line.  The reference arm runs on the host
+    # cores, so this runs without a GPU.
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR",
+                                                             "MASTER_PORT")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--impl", "reference",
+                        "--cells", "12", "--cpu-seconds", "0.5", "--cpu-threads", "2", "--steps", "3",
+                        "--warmup", "3"], capture_output=True, text=True, timeout=600, env=env, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    line = lines[0]
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["ranks_joined"] == 2
+    assert line["config"]["parallelism"] == "replicas x2" and line["value"] > 0
+
+
+def test_bench_refuses_a_rank_count_that_differs_from_the_job():
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--impl", "reference",
+                        "--cells", "12"], capture_output=True, text=True, timeout=300, env=env, cwd=root)
+    assert r.returncode != 0 and "WORLD_SIZE is 1" in r.stderr
