@@ -49,7 +49,7 @@ enum mdg_thermostat { MDG_NVE = 0, MDG_LANGEVIN = 1, MDG_NOSEHOOVER = 2 };
 
 typedef struct mdg_params {
   int32_t capacity;        /* maximum particles (Variables N, mdconfig.h:11) */
-  int32_t precision;       /* mdg_precision (.cfg Precision=fp64|mixed) */
+  int32_t precision;       /* mdg_precision (.cfg Precision=fp64|mixed|mixed_plain) */
   double box[3];           /* SystemSizeX/Y/Z (simulationinfo.cc:38-57) */
   double cutoff;           /* CutoffLength; CUTOFF_LENGTH (mdconfig.h:15) */
   double margin;           /* BufferLength (simulationinfo.cc:6) */
@@ -206,10 +206,14 @@ int mdg_batch_calculate(mdg_batch *b, int32_t nsteps);
 /* out: nbox x 3 observer sums (as mdg_observe) at the current positions. */
 int mdg_batch_observe(mdg_batch *b, double *out);
 /* Autotuner: times trial_steps for every (threads per CTA, lanes per particle,
- * CTAs per SM) shape from a copy of the current state, keeps the fastest, and
- * restores the state. */
+ * CTAs per SM) shape whose CTAs are all resident at once (occupancy of the
+ * step kernel that shape runs) from a copy of the current state, keeps the
+ * fastest, and restores the state. */
 int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t *lanes_per_particle,
                    int32_t *ctas_per_sm);
+/* Fixes the shape by hand; ctas_per_sm is capped at the CTAs of the step
+ * kernel that fit on one SM at once (mdg_batch_get_stats reports the value
+ * used), so the persistent kernel never runs in waves. */
 int mdg_batch_set_shape(mdg_batch *b, int32_t threads, int32_t lanes_per_particle, int32_t ctas_per_sm);
 /* Whether one lane per particle walks the inner list (1, the default when the
  * buffer is > 0) or every listed pair (0); mdg_batch_tune chooses it too. */

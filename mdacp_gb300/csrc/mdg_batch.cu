@@ -760,8 +760,37 @@ cudaError_t balloc(T **p, size_t count) {
   return cudaMalloc((void **)p, (count ? count : 1) * sizeof(T));
 }
 
+// The persistent step kernel the shape selects (as launch_batch_step does).
+const void *step_kernel_fn(int prec, int lpi, bool inner) {
+#define MDG_BFN(M, L, I) reinterpret_cast<const void *>(&k_batch_step<M, L, I>)
+  if (prec == MDG_MIXED)
+    return lpi == 4 ? MDG_BFN(MDG_MIXED, 4, 0) : lpi == 2 ? MDG_BFN(MDG_MIXED, 2, 0)
+           : inner  ? MDG_BFN(MDG_MIXED, 1, 1) : MDG_BFN(MDG_MIXED, 1, 0);
+  if (prec == MDG_MIXED_PLAIN)
+    return lpi == 4 ? MDG_BFN(MDG_MIXED_PLAIN, 4, 0) : lpi == 2 ? MDG_BFN(MDG_MIXED_PLAIN, 2, 0)
+           : inner  ? MDG_BFN(MDG_MIXED_PLAIN, 1, 1) : MDG_BFN(MDG_MIXED_PLAIN, 1, 0);
+  return lpi == 4 ? MDG_BFN(MDG_FP64, 4, 0) : lpi == 2 ? MDG_BFN(MDG_FP64, 2, 0)
+         : inner  ? MDG_BFN(MDG_FP64, 1, 1) : MDG_BFN(MDG_FP64, 1, 0);
+#undef MDG_BFN
+}
+
+// CTAs of `threads` threads of the selected step kernel that fit on one SM
+// at once (registers, shared memory, thread slots): the persistent kernel's
+// grid must not exceed this, or its CTAs run in waves.
+int resident_ctas(const mdg_batch *b, int threads) {
+  const bool inner = b->P.inner && b->lpi == 1 && b->use_inner;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, step_kernel_fn(b->prm.precision, b->lpi, inner), threads,
+                                                    0) != cudaSuccess)
+    return 1;
+  return nb > 0 ? nb : 1;
+}
+
 // Longest-first assignment of boxes to grid CTAs (work ~ n * list capacity).
+// The CTAs per SM are capped by what is resident at once, so every CTA of the
+// persistent kernel runs from the start.
 int assign(mdg_batch *b) {
+  b->ctas_per_sm = std::min(b->ctas_per_sm, resident_ctas(b, b->threads));
   const int G = b->num_sms * b->ctas_per_sm;
   std::vector<int> idx(b->nbox);
   std::iota(idx.begin(), idx.end(), 0);
@@ -1190,6 +1219,9 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
     for (int Lp : Ls)
       for (int C : Cs) {
         if (T * C > 2048) continue;
+        b->lpi = Lp;
+        b->use_inner = 0;
+        if (C > resident_ctas(b, T)) continue;  // would run in waves (assign would cap it)
         double ms = 0.0;
         int rc = trial(T, Lp, C, 0, trial_steps, &ms);
         if (rc) return rc;

@@ -41,10 +41,12 @@ constexpr int kStepThreads = 128;
 #ifndef MDG_STEP_MIN_BLOCKS
 #define MDG_STEP_MIN_BLOCKS 12
 #endif
-// The same for the compensated mixed form, whose three correction terms do
-// not fit in 40 registers (48 bytes of spills at 12 blocks).
+// The same for the compensated mixed form.  Its three correction terms do
+// not fit in 40 registers (48 bytes of spills at 12 blocks), but 12 blocks
+// with the spills measured 6 % faster than 10 blocks at 48 registers without
+// them (4M atoms, 400 steps: 0.472 against 0.501 ms per step kernel).
 #ifndef MDG_STEP_MIN_BLOCKS_KAHAN
-#define MDG_STEP_MIN_BLOCKS_KAHAN 10
+#define MDG_STEP_MIN_BLOCKS_KAHAN 12
 #endif
 #ifndef MDG_PRUNE_MIN_BLOCKS
 #define MDG_PRUNE_MIN_BLOCKS 8
@@ -191,8 +193,9 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
     if (KAHAN) {
       // a zero term (a pair beyond rc) leaves s - c unchanged as a real
       // number (t - s is exact, and so is the new correction), but it moves
-      // the correction into s: lists that differ only by pairs beyond rc give
-      // sums that agree to second order in the float rounding, not bit for bit
+      // the correction into s and the later additions round differently:
+      // lists that differ only by pairs beyond rc give forces that agree to
+      // about one float rounding, not bit for bit
       kahan_fma(sx, cx, df, dx);
       kahan_fma(sy, cy, df, dy);
       kahan_fma(sz, cz, df, dz);

