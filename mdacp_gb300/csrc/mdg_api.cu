@@ -184,9 +184,6 @@ int estimate_list_cap(const mdg_handle *h, int n) {
 }
 
 int alloc_list(mdg_handle *h, int list_cap) {
-  // the mixed pair loop indexes list entries in 32 bits
-  if ((unsigned long long)list_cap * (unsigned long long)h->cap >= (1ULL << 32))
-    return fail(h, MDG_ERR_CAPACITY, "capacity x neighbour slots per particle must stay below 2^32");
   if (h->d.nl) cudaFree(h->d.nl);
   if (h->d.pl) cudaFree(h->d.pl);
   h->d.nl = h->d.pl = nullptr;

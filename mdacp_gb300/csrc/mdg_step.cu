@@ -57,11 +57,6 @@ constexpr int kStepThreads = 128;
 #define MDG_STEP_UNROLL 4
 #endif
 constexpr int kUnroll = MDG_STEP_UNROLL;
-// The same for the compensated sums (three more live registers per thread).
-#ifndef MDG_STEP_UNROLL_KAHAN
-#define MDG_STEP_UNROLL_KAHAN 4
-#endif
-constexpr int kUnrollKahan = MDG_STEP_UNROLL_KAHAN;
 
 // List rows requested into L2 this many entries ahead of the pair loop (0:
 // none).  16 measured best at 4M atoms (step kernel 0.476 -> 0.440 ms; 8: 0.472,
@@ -167,11 +162,8 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
   const AxisQuad qz = axis_quad(g.w32[2], g.dl32[2], cp.cz == 0, cp.cz == g.nc[2] - 1, li.z, 0.0625f);
   int cnt = counts[i];
   if (!MDG_IN_RANGE(d.flags, kCheckStepRow, cnt, g.list_cap + 1)) cnt = 0;
-  // entry k of slot i at k * stride + i, indexed in 32 bits (the handle
-  // keeps capacity x list capacity below 2^32): no 64-bit row pointer and
-  // stride held through the loop
-  const uint32_t stride = (uint32_t)g.stride;
-  auto entry = [&](int kk) -> uint32_t { return __ldg(list + ((uint32_t)kk * stride + (uint32_t)i)); };
+  const uint32_t *row = list + i;
+  const size_t stride = (size_t)g.stride;
   float sx = 0.f, sy = 0.f, sz = 0.f;
   float cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan corrections
   // a partner position (a far one, contributing nothing, for an entry a
@@ -191,7 +183,7 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
     const float dy = lj.y + fmaf(fmaf(qy.b, ty, qy.a), ty, qy.c);
     const float dz = lj.z + fmaf(fmaf(qz.b, tz, qz.a), tz, qz.c);
     const float r2 = dx * dx + dy * dy + dz * dz;
-    if (PRUNE && r2 <= thr) d.pl[(uint32_t)(m++) * stride + (uint32_t)i] = e;
+    if (PRUNE && r2 <= thr) d.pl[(size_t)(m++) * stride + i] = e;
     // evaluated for every entry and masked: no divergent branch per pair
     float inv;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
@@ -213,42 +205,41 @@ __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, cons
       sz = fmaf(df, dz, sz);
     }
   };
-  constexpr int U = KAHAN ? kUnrollKahan : kUnroll;
   int k = 0;
   // the next batch's list entries are requested before this batch's partner
   // positions are used, so the entry load (from DRAM) overlaps the gathers;
-  // the last full batch requests the row's remaining (< U) entries
-  const int full = cnt - cnt % U;
-  uint32_t en[U];
+  // the last full batch requests the row's remaining (< kUnroll) entries
+  const int full = cnt - cnt % kUnroll;
+  uint32_t en[kUnroll];
 #pragma unroll
-  for (int u = 0; u < U; u++) en[u] = u < cnt ? entry(u) : 0u;
+  for (int u = 0; u < kUnroll; u++) en[u] = u < cnt ? __ldg(row + (size_t)u * stride) : 0u;
 #pragma unroll 1
-  for (; k < full; k += U) {
-    uint32_t e[U];
-    float4 l[U];
+  for (; k < full; k += kUnroll) {
+    uint32_t e[kUnroll];
+    float4 l[kUnroll];
 #pragma unroll
-    for (int u = 0; u < U; u++) e[u] = en[u];
+    for (int u = 0; u < kUnroll; u++) e[u] = en[u];
 #pragma unroll
-    for (int u = 0; u < U; u++) l[u] = gather(e[u]);
+    for (int u = 0; u < kUnroll; u++) l[u] = gather(e[u]);
 #pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int kn = k + U + u;
-      en[u] = kn < cnt ? entry(kn) : 0u;
+    for (int u = 0; u < kUnroll; u++) {
+      const int kn = k + kUnroll + u;
+      en[u] = kn < cnt ? __ldg(row + (size_t)kn * stride) : 0u;
     }
     if (kEntryAhead > 0) {
       // rows kEntryAhead further on, into L2: lane l requests row
       // k + kEntryAhead + (l mod 4) of its own column, so one instruction
       // covers the warp's four next rows, one 128-byte line each
       const int kp = k + kEntryAhead + (int)(threadIdx.x & 3);
-      if (kp < cnt) asm volatile("prefetch.global.L2 [%0];" ::"l"(list + ((uint32_t)kp * stride + (uint32_t)i)));
+      if (kp < cnt) asm volatile("prefetch.global.L2 [%0];" ::"l"(row + (size_t)kp * stride));
     }
 #pragma unroll
-    for (int u = 0; u < U; u++) pair(e[u], l[u]);
+    for (int u = 0; u < kUnroll; u++) pair(e[u], l[u]);
   }
   if (k < cnt) {
     // the remainder as one batch; missing entries get a partner at 1e30,
     // whose r^2 overflows to +inf and contributes nothing
-    constexpr int kTail = U > 1 ? U - 1 : 1;
+    constexpr int kTail = kUnroll > 1 ? kUnroll - 1 : 1;
     float4 l[kTail];
 #pragma unroll
     for (int u = 0; u < kTail; u++)
