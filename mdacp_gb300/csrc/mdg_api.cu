@@ -171,6 +171,7 @@ int setup_geometry(mdg_handle *h) {
   g.tau = p.tau;
   g.hb_d = std::sqrt(2.0 * p.gamma * p.temperature / p.dt);
   g.seed = p.seed;
+  g.local_pos = p.precision != MDG_FP64 ? 1 : 0;
   return MDG_OK;
 }
 
@@ -655,8 +656,8 @@ int mdg_make_state(mdg_handle *h, int32_t maker, double density, double radius, 
 int mdg_get_state(mdg_handle *h, double *q4, double *p4) {
   int rc = check_handle(h, true);
   if (rc) return rc;
-  mdg::launch_unsort(h->g, h->d, q4 ? h->d.io4 : nullptr, p4 ? h->d.io4b : nullptr, h->stream);
-  h->launches += 1;
+  mdg::launch_unsort(h->g, h->d, h->par, q4 ? h->d.io4 : nullptr, p4 ? h->d.io4b : nullptr, h->stream);
+  h->launches += h->g.local_pos ? 3 : 1;
   const size_t bytes = (size_t)h->g.n * sizeof(double4_32a);
   if (q4) MDG_CK(cudaMemcpyAsync(q4, h->d.io4, bytes, cudaMemcpyDeviceToHost, h->stream));
   if (p4) MDG_CK(cudaMemcpyAsync(p4, h->d.io4b, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -667,7 +668,8 @@ int mdg_get_state(mdg_handle *h, double *q4, double *p4) {
 int mdg_get_state_device(mdg_handle *h, double *q4, double *p4) {
   int rc = check_handle(h, true);
   if (rc) return rc;
-  mdg::launch_unsort(h->g, h->d, (double4_32a *)q4, (double4_32a *)p4, h->stream);
+  mdg::launch_unsort(h->g, h->d, h->par, (double4_32a *)q4, (double4_32a *)p4, h->stream);
+  h->launches += h->g.local_pos ? 3 : 1;
   MDG_CK(cudaGetLastError());
   return MDG_OK;
 }
@@ -853,7 +855,7 @@ int mdg_observe(mdg_handle *h, double out[3]) {
   rc = ensure_list(h, false);
   if (rc) return rc;
   mdg::launch_observe(h->g, h->d, h->dobs, h->stream, h->prm.precision != MDG_FP64, h->par);
-  h->launches += h->prm.precision != MDG_FP64 ? 3 : 2;
+  h->launches += h->prm.precision != MDG_FP64 ? 5 : 2;
   MDG_CK(cudaMemcpyAsync(h->hobs, h->dobs, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   out[0] = h->hobs[0];
@@ -869,7 +871,7 @@ int mdg_forces(mdg_handle *h, double *f4) {
   rc = ensure_list(h, false);
   if (rc) return rc;
   mdg::launch_forces(h->g, h->d, h->prm.precision, h->par, h->stream);
-  h->launches += h->prm.precision != MDG_FP64 ? 2 : 1;
+  h->launches += h->prm.precision != MDG_FP64 ? 4 : 1;
   MDG_CK(cudaMemcpyAsync(f4, h->d.io4, (size_t)h->g.n * sizeof(double4_32a), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   return MDG_OK;

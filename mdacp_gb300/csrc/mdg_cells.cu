@@ -67,15 +67,31 @@ __device__ __forceinline__ void start_step(DevFlags *f, int lang_step) {
   }
 }
 
+// Step-boundary position of slot i in the mixed form from the home-cell-local
+// mid-step position: the centre of the home cell plus (q_mid - p dt/2), the
+// inverse of the step's last half-drift.
+__device__ __forceinline__ double4_32a end_from_mid(const Geom &g, const Dev &d, int i, int mid) {
+  const double4_32a u = d.q_mid[mid][i], p = d.p[i];
+  int cx, cy, cz;
+  cell_unkey(d.cell[i], cx, cy, cz);
+  double4_32a q = u;
+  q.x = cell_centre(g, 0, cx) + fma(-p.x, g.dt2, u.x);
+  q.y = cell_centre(g, 1, cy) + fma(-p.y, g.dt2, u.y);
+  q.z = cell_centre(g, 2, cz) + fma(-p.z, g.dt2, u.z);
+  return q;
+}
+
 // Wraps q_end into the box with the reference rule (one +-L per component),
 // bins it and counts cell occupancy.  Thread 0 also advances the step and
-// Langevin counters of a step that is starting.
-__global__ void k_wrap_bin(Geom g, Dev d, int count_step, int lang_step) {
+// Langevin counters of a step that is starting.  In the mixed form q_end is
+// first taken from q_mid[mid] when the steps left it behind.
+__global__ void k_wrap_bin(Geom g, Dev d, int count_step, int lang_step, int mid) {
   DevFlags *f = d.flags;
   if (count_step && blockIdx.x == 0 && threadIdx.x == 0 && f->halt == 0) start_step(f, lang_step);
   if (rebuild_off(f)) return;
+  const bool from_mid = g.local_pos && f->end_stale;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x) {
-    double4_32a q = d.q_end[i];
+    double4_32a q = from_mid ? end_from_mid(g, d, i, mid) : d.q_end[i];
     double x[3] = {q.x, q.y, q.z};
     int c[3];
     bool bad = false;
@@ -196,10 +212,14 @@ __global__ void k_reorder(Geom g, Dev d) {
 
 // Copies the sorted staging back, records the build positions and derives the
 // positions the next force evaluation uses: q_mid = q + p dt/2 (the first
-// half-drift, fcalculator.cc:21-32, rounded as two separate operations).
+// half-drift, fcalculator.cc:21-32, rounded as two separate operations).  In
+// the mixed form q_mid is kept relative to the centre of the new home cell,
+// (q - centre) + p dt/2, and q_end is current again.
 __global__ void k_finalize(Geom g, Dev d, int q_mid_dst) {
   double4_32a *q_mid = d.q_mid[q_mid_dst];
   if (rebuild_off(d.flags)) return;
+  // k_wrap_bin, the only reader of end_stale in the rebuild, has finished
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.flags->end_stale = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.n; k += gridDim.x * blockDim.x) {
     const double4_32a q = d.t_q[k], p = d.t_p[k];
     const int id = d.t_id[k], c = d.t_cell[k];
@@ -212,18 +232,35 @@ __global__ void k_finalize(Geom g, Dev d, int q_mid_dst) {
     int cx, cy, cz;
     cell_unkey(c, cx, cy, cz);
     const float cw = __int_as_float(c);
-    const double ox = ((double)cx + 0.5) * (double)g.w32[0];
-    const double oy = ((double)cy + 0.5) * (double)g.w32[1];
-    const double oz = ((double)cz + 0.5) * (double)g.w32[2];
+    const double ox = cell_centre(g, 0, cx), oy = cell_centre(g, 1, cy), oz = cell_centre(g, 2, cz);
     d.qf[k] = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), cw);
     double4_32a m = q;
-    m.x = __dadd_rn(q.x, __dmul_rn(p.x, g.dt2));
-    m.y = __dadd_rn(q.y, __dmul_rn(p.y, g.dt2));
-    m.z = __dadd_rn(q.z, __dmul_rn(p.z, g.dt2));
-    q_mid[k] = m;
-    if (d.loc[q_mid_dst]) d.loc[q_mid_dst][k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), cw);
+    if (g.local_pos) {
+      m.x = __dadd_rn(q.x - ox, __dmul_rn(p.x, g.dt2));
+      m.y = __dadd_rn(q.y - oy, __dmul_rn(p.y, g.dt2));
+      m.z = __dadd_rn(q.z - oz, __dmul_rn(p.z, g.dt2));
+      q_mid[k] = m;
+      d.loc[q_mid_dst][k] = make_float4((float)m.x, (float)m.y, (float)m.z, cw);
+    } else {
+      m.x = __dadd_rn(q.x, __dmul_rn(p.x, g.dt2));
+      m.y = __dadd_rn(q.y, __dmul_rn(p.y, g.dt2));
+      m.z = __dadd_rn(q.z, __dmul_rn(p.z, g.dt2));
+      q_mid[k] = m;
+      d.loc[q_mid_dst][k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), cw);
+    }
   }
 }
+
+// Mixed form: q_end from q_mid[mid] and p for every slot while the steps have
+// left it behind; k_end_current then records that it is current (a separate
+// kernel, so no thread clears the flag while others still read it).
+__global__ void k_end_from_mid(Geom g, Dev d, int mid) {
+  if (!d.flags->end_stale) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += gridDim.x * blockDim.x)
+    d.q_end[i] = end_from_mid(g, d, i, mid);
+}
+
+__global__ void k_end_current(DevFlags *f) { f->end_stale = 0; }
 
 __global__ void k_set_rebuild(DevFlags *f) {
   if (f->halt == 0) f->rebuild = 1;
@@ -247,6 +284,14 @@ void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s,
 
 void launch_set_rebuild(const Dev &d, cudaStream_t s) { k_set_rebuild<<<1, 1, 0, s>>>(d.flags); }
 
+void launch_end_from_mid(const Geom &g, const Dev &d, int par, cudaStream_t s) {
+  const int threads = 256;
+  int grid = (g.n + threads - 1) / threads;
+  if (grid < 1) grid = 1;
+  k_end_from_mid<<<grid, threads, 0, s>>>(g, d, par);
+  k_end_current<<<1, 1, 0, s>>>(d.flags);
+}
+
 void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle rebuild_cond, cudaStream_t s) {
   k_prelude<<<1, 1, 0, s>>>(d.flags, lang_step, rebuild_cond);
 }
@@ -265,7 +310,7 @@ void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cud
   int cgrid = (g.nrank + threads - 1) / threads;
   if (cgrid > cap) cgrid = cap;
   const int nb = (g.nrank + kScanTile - 1) / kScanTile;
-  k_wrap_bin<<<grid, threads, 0, s>>>(g, d, count_step ? 1 : 0, lang_step ? 1 : 0);
+  k_wrap_bin<<<grid, threads, 0, s>>>(g, d, count_step ? 1 : 0, lang_step ? 1 : 0, q_mid_dst);
   k_scan_reduce<<<nb, kScanThreads, 0, s>>>(g, d);
   k_scan_top<<<1, kScanThreads, 0, s>>>(nb, d);
   k_scan_apply<<<nb, kScanThreads, 0, s>>>(g, d);

@@ -1,9 +1,12 @@
 // Internal declarations shared by the mdg CUDA translation units.
 //
 // Device data layout (one box, n particles, slots sorted by cell):
-//   q_end[n]   double4_32a  positions at the step boundary (the reference's q)
+//   q_end[n]   double4_32a  positions at the step boundary (the reference's q);
+//                       in the mixed form only current after a rebuild or
+//                       launch_end_from_mid (flags->end_stale says which)
 //   q_mid[2][n] double4_32a positions after the first half-drift; the step kernel
-//                       reads one buffer and writes the other
+//                       reads one buffer and writes the other.  Mixed form:
+//                       relative to the centre of the slot's home cell
 //   p[n]       double4_32a  momenta (= velocities, m = 1)
 //   q_build[n] double4_32a  positions at the last list build (displacement check)
 //   id[n]      int      caller's particle index of each slot; inv[id] = slot
@@ -66,6 +69,7 @@ struct DevFlags {
   int prune_next;               // a particle left its prune buffer: re-select at the next step
   unsigned long long prunes;    // completed prunes
   unsigned long long inner_pairs;  // directed pairs in the inner list at the last prune
+  int end_stale;                // mixed form: q_end is behind the steps (rebuilt from q_mid and p on demand)
 };
 
 struct Geom {
@@ -95,7 +99,16 @@ struct Geom {
   // inner (pruned) list: pairs within rc + prune_buffer at the last prune
   float prune_thr2;   // (rc + buffer)^2 + float slack
   float half_prune2;  // (buffer / 2)^2, displacement that forces a re-prune
+  // mixed form: q_mid holds positions relative to the centre of the slot's
+  // home cell at the last build, and the step kernels do not write q_end
+  int local_pos;
 };
+
+// Centre of home cell (cx, cy, cz) in double, exact: (c + 1/2) w32 has at
+// most 36 significant bits.
+__host__ __device__ __forceinline__ double cell_centre(const Geom &g, int k, int c) {
+  return ((double)c + 0.5) * (double)g.w32[k];
+}
 
 struct Dev {
   double4_32a *q_end, *q_mid[2], *p, *q_build;
@@ -135,10 +148,13 @@ void launch_select(const Dev &d, cudaGraphConditionalHandle variant_cond, cudaSt
 void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s);
 void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s, int mixed, int par);
 void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s);
-void launch_unsort(const Geom &g, const Dev &d, double4_32a *qo, double4_32a *po, cudaStream_t s);
+void launch_unsort(const Geom &g, const Dev &d, int par, double4_32a *qo, double4_32a *po, cudaStream_t s);
 void launch_sort_in(const Geom &g, const Dev &d, const double4_32a *qi, const double4_32a *pi, cudaStream_t s);
 void launch_pairs(const Geom &g, const Dev &d, const long long *row_off, int32_t *rec, cudaStream_t s);
 void launch_set_rebuild(const Dev &d, cudaStream_t s);
+// Mixed form: brings q_end up to date from q_mid[par] and p when the steps
+// left it behind (two kernels; a no-op when it is current).
+void launch_end_from_mid(const Geom &g, const Dev &d, int par, cudaStream_t s);
 
 // Home-cell coordinates of a slot packed in one word: bits 0-10 x, 11-21 y,
 // 22-31 z.  `cell[]` holds this key; the w word of the float4 positions (qf,

@@ -361,20 +361,26 @@ __global__ void __launch_bounds__(kStepThreads, PMODE != 1          ? MDG_PRUNE_
       q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, g.dt2));
       q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, g.dt2));
     }
-    const double4_32a qb = d.q_build[i];
-    const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
-    // displacement since the build in float: the new home-cell-local position
-    // (qf holds the local position at the build) and the inner-list test
-    const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
-    const float4 ln = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, lb.w);
-    d.loc[par ^ 1][i] = ln;
+    float4 ln;
     if (MIXED) {
+      // positions relative to the home-cell centre: the new local position is
+      // one conversion, and the displacement since the build is measured in
+      // float against the build's local position (qf)
+      ln = make_float4((float)q1.x, (float)q1.y, (float)q1.z, lb.w);
+      const float fx = ln.x - lb.x, fy = ln.y - lb.y, fz = ln.z - lb.z;
       if (fx * fx + fy * fy + fz * fz > (float)g.half_margin2 || !(fx == fx && fy == fy && fz == fz))
         d.flags->rebuild = 1;
     } else {
+      const double4_32a qb = d.q_build[i];
+      const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
+      // displacement since the build: in double for the rebuild test, in
+      // float for the new home-cell-local position (qf holds the local
+      // position at the build) and the inner-list test
+      ln = make_float4(lb.x + (float)ux, lb.y + (float)uy, lb.z + (float)uz, lb.w);
       if (ux * ux + uy * uy + uz * uz > g.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
         d.flags->rebuild = 1;
     }
+    d.loc[par ^ 1][i] = ln;
     // prune reference: the positions of this force evaluation when the
     // inner list was re-selected now, else those of the last selection
     float4 lp;
@@ -388,11 +394,14 @@ __global__ void __launch_bounds__(kStepThreads, PMODE != 1          ? MDG_PRUNE_
     const float vx = ln.x - lp.x, vy = ln.y - lp.y, vz = ln.z - lp.z;
     if (vx * vx + vy * vy + vz * vz > g.half_prune2) d.flags->prune_next = 1;
     d.p[i] = p;
-    d.q_end[i] = qe;
+    // the mixed form leaves q_end behind: q_mid - p dt/2 gives it back when a
+    // rebuild or a reader needs it (32 bytes a particle fewer per step)
+    if (!MIXED) d.q_end[i] = qe;
     qn[i] = q1;
     if (THERMO == MDG_NOSEHOOVER)
       ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
   }
+  if (MIXED && i == 0) d.flags->end_stale = 1;
   if (THERMO == MDG_NOSEHOOVER) {
     __shared__ double sh[kStepThreads / 32];
     const double t = block_sum(ke, sh);
@@ -653,6 +662,7 @@ void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s) {
 void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s, int mixed, int par) {
   const int grid = blocks_for(g.n);
   if (mixed) {
+    launch_end_from_mid(g, d, par, s);
     // the buffer the next step overwrites before reading it
     k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
     k_observe_mixed<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
@@ -665,6 +675,7 @@ void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s
 void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s) {
   const int grid = blocks_for(g.n);
   if (mixed) {
+    launch_end_from_mid(g, d, par, s);
     // the buffer the next step overwrites before reading it
     k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
     if (mixed == MDG_MIXED_PLAIN) k_forces<MDG_MIXED_PLAIN><<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
@@ -674,7 +685,8 @@ void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t
   }
 }
 
-void launch_unsort(const Geom &g, const Dev &d, double4_32a *qo, double4_32a *po, cudaStream_t s) {
+void launch_unsort(const Geom &g, const Dev &d, int par, double4_32a *qo, double4_32a *po, cudaStream_t s) {
+  if (g.local_pos) launch_end_from_mid(g, d, par, s);
   k_unsort<<<blocks_for(g.n), kStepThreads, 0, s>>>(g, d, qo, po);
 }
 
