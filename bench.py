@@ -509,8 +509,9 @@ def run_batch1024(args):
         b.calculate(K)
         st = b.stats()
         res[prec] = {"ms": st["elapsed_ms"], "shape": {"threads": shape[0], "lanes_per_particle": shape[1],
-                                                        "ctas_per_sm": shape[2], "inner_list": st["inner_list"]},
-                     "rebuilds": st["rebuilds"], "kernels_per_step": 6}
+                                                        "ctas_per_sm": st["ctas_per_sm"], "inner_list": st["inner_list"],
+                                                        "flat": st["flat"]},
+                     "rebuilds": st["rebuilds"], "kernels_per_step": 7 if st["flat"] else 6}
         b.close()
     cfg = {"workload": "1024 replica boxes, %d atoms total, N~U[500,8000], rho~U[0.3,0.9], T~U[0.7,1.5], "
                        "rc 2.5, margin 0.4, dt 0.002" % n, "atoms": n, "boxes": 1024}

@@ -190,6 +190,8 @@ typedef struct mdg_batch_stats {
   int32_t inner_list;         /* 1: the step walks the inner list (chosen by mdg_batch_tune) */
   double elapsed_ms;          /* device time of the last mdg_batch_calculate */
   int64_t kernel_launches;
+  int32_t flat;               /* 1: flat layout (see mdg_batch_set_flat) */
+  int32_t reserved;
 } mdg_batch_stats;
 
 typedef struct mdg_batch mdg_batch;
@@ -218,6 +220,13 @@ int mdg_batch_set_shape(mdg_batch *b, int32_t threads, int32_t lanes_per_particl
 /* Whether one lane per particle walks the inner list (1, the default when the
  * buffer is > 0) or every listed pair (0); mdg_batch_tune chooses it too. */
 int mdg_batch_set_inner(mdg_batch *b, int32_t on);
+/* Layout of the persistent step kernel: 0 (default) = each CTA steps the
+ * boxes assigned to it in turn; 1 = flat: the resident CTAs stride over the
+ * particles of all boxes, one thread per particle, and a small per-box kernel
+ * after the step applies the boxes' rebuild and re-selection requests.  The
+ * flat layout takes one lane per particle and at most 256 threads per CTA;
+ * mdg_batch_tune times both layouts. */
+int mdg_batch_set_flat(mdg_batch *b, int32_t on);
 int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s);
 
 /* ------------------------------------------------------------------------

@@ -21,7 +21,8 @@ class BatchStats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int64), ("rebuilds", ctypes.c_int64), ("particles", ctypes.c_int64),
                 ("boxes", ctypes.c_int32), ("list_capacity", ctypes.c_int32), ("threads", ctypes.c_int32),
                 ("lanes_per_particle", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("inner_list", ctypes.c_int32),
-                ("elapsed_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64)]
+                ("elapsed_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64), ("flat", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p
@@ -39,6 +40,7 @@ SIGNATURES = {
     "mdg_batch_tune": (ctypes.c_int, [_P, ctypes.c_int32, _I, _I, _I]),
     "mdg_batch_set_shape": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "mdg_batch_set_inner": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "mdg_batch_set_flat": (ctypes.c_int, [_P, ctypes.c_int32]),
     "mdg_batch_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(BatchStats)]),
 }
 
@@ -144,6 +146,11 @@ class Batch:
 
     def set_shape(self, threads, lanes, ctas_per_sm):
         self._ck(self.lib.mdg_batch_set_shape(self._h, threads, lanes, ctas_per_sm))
+
+    def set_flat(self, on):
+        """Flat layout of the step (the grid strides over every box's particles)
+        or each CTA stepping its own boxes (False)."""
+        self._ck(self.lib.mdg_batch_set_flat(self._h, 1 if on else 0))
 
     def stats(self):
         s = BatchStats()

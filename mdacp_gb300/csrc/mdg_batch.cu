@@ -63,6 +63,7 @@ struct Params {
   float acc_lo, acc_hi, rc2f, c2x8f;
   int list_cap;
   int nbox;
+  int total;  // particles of all boxes
   // inner list (one lane per particle): the listed pairs within rc + buffer,
   // re-selected when a particle of the box moved buffer / 2 since the last
   // selection, and after every rebuild
@@ -81,6 +82,9 @@ struct Dev {
   int *ncount, *pcount;
   float4 *loc_p;       // local positions at the last inner-list selection
   int *box_rebuild, *box_err, *box_need, *box_prune;
+  // flat layout: raised (plain stores of 1) by any particle of the box during
+  // the step, applied by k_batch_finish after it
+  int *box_req, *box_preq;
   long long *box_steps, *box_rebuilds, *goal;
   double *partials;  // per box: KE, PE, virial
   const int *box_of_slot;
@@ -310,7 +314,7 @@ __device__ int build_row(const Params &P, const Dev &d, const BoxDesc &b, int bi
 #define MDG_BATCH_PREP_THREADS 1024
 #endif
 constexpr int kPrepThreads = MDG_BATCH_PREP_THREADS;
-constexpr int kBatchKernelsPerStep = 6;  // rebuild set, bin, sort, place, list, step
+constexpr int kBatchKernelsPerStep = 6;  // rebuild set, bin, sort, place, list, step (+ finish in the flat layout)
 
 __global__ void __launch_bounds__(128) k_batch_bin(Dev d) {
   const int nb = *d.rb_count;
@@ -536,6 +540,65 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
   return make_double3(fx, fy, fz);
 }
 
+// Kick, both half-drifts, the displacement and inner-list tests and the
+// stores of slot s after its force F (one lane per particle does this).
+template <int MIXED, bool INNER>
+__device__ __forceinline__ void advance_particle(const Params &P, const Dev &d, int s, const double3 &F, int par,
+                                                 bool sel, int kept, bool &rebuild, bool &reselect) {
+  const bool inner = INNER;
+  double4_32a p = d.p[s];
+  p.x += F.x * P.dt;
+  p.y += F.y * P.dt;
+  p.z += F.z * P.dt;
+  const double4_32a q0 = d.q_mid[par][s];
+  double4_32a qe = q0, q1 = q0;
+  if (MIXED) {  // one rounding per half-drift (fused), as the single-box mixed form
+    qe.x = fma(p.x, P.dt2, q0.x);
+    qe.y = fma(p.y, P.dt2, q0.y);
+    qe.z = fma(p.z, P.dt2, q0.z);
+    q1.x = fma(p.x, P.dt2, qe.x);
+    q1.y = fma(p.y, P.dt2, qe.y);
+    q1.z = fma(p.z, P.dt2, qe.z);
+  } else {
+    qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, P.dt2));
+    qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, P.dt2));
+    qe.z = __dadd_rn(q0.z, __dmul_rn(p.z, P.dt2));
+    q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, P.dt2));
+    q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, P.dt2));
+    q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, P.dt2));
+  }
+  const double4_32a qb = d.q_build[s];
+  const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
+  const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
+  if (MIXED) {
+    if (fx * fx + fy * fy + fz * fz > (float)P.half_margin2 || !(fx == fx && fy == fy && fz == fz))
+      rebuild = true;
+  } else {
+    if (ux * ux + uy * uy + uz * uz > P.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
+      rebuild = true;
+  }
+  const float4 lb = d.qf[s];
+  const float4 ln = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
+  d.loc[par ^ 1][s] = ln;
+  if (inner) {
+    // inner-list reference: this force evaluation's positions when the
+    // rows were re-selected now, else those of the last selection
+    float4 lp;
+    if (sel) {
+      lp = d.loc[par][s];
+      d.loc_p[s] = lp;
+      d.pcount[s] = kept;
+    } else {
+      lp = d.loc_p[s];
+    }
+    const float vx = ln.x - lp.x, vy = ln.y - lp.y, vz = ln.z - lp.z;
+    if (vx * vx + vy * vy + vz * vz > P.half_prune2) reselect = true;
+  }
+  d.p[s] = p;
+  d.q_end[s] = qe;
+  d.q_mid[par ^ 1][s] = q1;
+}
+
 // The advance of every box by one step, one persistent kernel: each CTA
 // steps its boxes in turn.  The lists of the boxes that rebuilt this step
 // were made by the rebuild kernels just before.
@@ -585,57 +648,7 @@ __global__ void __launch_bounds__(512, MIXED ? MDG_BATCH_MIN_BLOCKS : 2) k_batch
         F = box_force<MIXED, LPI, 0>(P, d, b, a, lane, par);
       }
       if (lane != 0 || a0 >= n) continue;
-      double4_32a p = d.p[o + a];
-      p.x += F.x * P.dt;
-      p.y += F.y * P.dt;
-      p.z += F.z * P.dt;
-      const double4_32a q0 = d.q_mid[par][o + a];
-      double4_32a qe = q0, q1 = q0;
-      if (MIXED) {  // one rounding per half-drift (fused), as the single-box mixed form
-        qe.x = fma(p.x, P.dt2, q0.x);
-        qe.y = fma(p.y, P.dt2, q0.y);
-        qe.z = fma(p.z, P.dt2, q0.z);
-        q1.x = fma(p.x, P.dt2, qe.x);
-        q1.y = fma(p.y, P.dt2, qe.y);
-        q1.z = fma(p.z, P.dt2, qe.z);
-      } else {
-        qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, P.dt2));
-        qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, P.dt2));
-        qe.z = __dadd_rn(q0.z, __dmul_rn(p.z, P.dt2));
-        q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, P.dt2));
-        q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, P.dt2));
-        q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, P.dt2));
-      }
-      const double4_32a qb = d.q_build[o + a];
-      const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
-      const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
-      if (MIXED) {
-        if (fx * fx + fy * fy + fz * fz > (float)P.half_margin2 || !(fx == fx && fy == fy && fz == fz))
-          rebuild = true;
-      } else {
-        if (ux * ux + uy * uy + uz * uz > P.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
-          rebuild = true;
-      }
-      const float4 lb = d.qf[o + a];
-      const float4 ln = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
-      d.loc[par ^ 1][o + a] = ln;
-      if (inner) {
-        // inner-list reference: this force evaluation's positions when the
-        // rows were re-selected now, else those of the last selection
-        float4 lp;
-        if (sel) {
-          lp = d.loc[par][o + a];
-          d.loc_p[o + a] = lp;
-          d.pcount[o + a] = kept;
-        } else {
-          lp = d.loc_p[o + a];
-        }
-        const float vx = ln.x - lp.x, vy = ln.y - lp.y, vz = ln.z - lp.z;
-        if (vx * vx + vy * vy + vz * vz > P.half_prune2) reselect = true;
-      }
-      d.p[o + a] = p;
-      d.q_end[o + a] = qe;
-      d.q_mid[par ^ 1][o + a] = q1;
+      advance_particle<MIXED, inner>(P, d, o + a, F, par, sel, kept, rebuild, reselect);
     }
     const int any = __syncthreads_or(rebuild ? 1 : 0);
     const int anyp = __syncthreads_or(reselect ? 1 : 0);
@@ -646,6 +659,67 @@ __global__ void __launch_bounds__(512, MIXED ? MDG_BATCH_MIN_BLOCKS : 2) k_batch
     }
     __syncthreads();
   }
+}
+
+// The same step in the flat layout: the grid (only as many CTAs as are
+// resident at once) strides over the particles of all boxes, one thread per
+// particle, so no CTA waits for the slowest warp of a box before the next,
+// the work of a box spreads over the whole GPU and the kernel holds no box
+// description in registers (its fields are read where they are used, from
+// L1).  A particle whose displacement test fires raises its box's request
+// with a plain store of 1; k_batch_finish applies the requests and counts the
+// box's step after the kernel.  The box state the step reads (error, step
+// count, rebuild and re-selection flags) is not written during it.
+#ifndef MDG_BATCH_FLAT_MIN_BLOCKS
+#define MDG_BATCH_FLAT_MIN_BLOCKS 5
+#endif
+constexpr int kFlatMaxThreads = 256;
+template <int MIXED, int INNER>
+__global__ void __launch_bounds__(kFlatMaxThreads, MDG_BATCH_FLAT_MIN_BLOCKS) k_batch_step_flat(Params P, Dev d,
+                                                                                            int par) {
+  const long long goal = *d.goal;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < P.total; s += gridDim.x * blockDim.x) {
+    const int bi = d.box_of_slot[s];
+    if (d.box_err[bi] != 0 || d.box_steps[bi] >= goal) continue;
+    const BoxDesc &b = d.boxes[bi];
+    const int a = s - b.atom_off;
+    const bool sel = d.box_rebuild[bi] != 0 || d.box_prune[bi] != 0;
+    double3 F;
+    int kept = 0;
+    if constexpr (INNER != 0) {
+      if (sel) F = box_force<MIXED, 1, 1>(P, d, b, a, 0, par, true, &kept);
+      else F = box_force<MIXED, 1, 2>(P, d, b, a, 0, par);
+    } else {
+      F = box_force<MIXED, 1, 0>(P, d, b, a, 0, par);
+    }
+    bool rebuild = false, reselect = false;
+    advance_particle<MIXED, INNER != 0>(P, d, s, F, par, sel, kept, rebuild, reselect);
+    if (rebuild) d.box_req[bi] = 1;
+    if (INNER != 0 && reselect) d.box_preq[bi] = 1;
+  }
+}
+
+// After the flat step, one thread per box (the same participation test as
+// the step): the rebuild this step consumed is counted, the requests become
+// the next step's flags, the box's step count advances.
+template <int INNER>
+__global__ void k_batch_finish(Params P, Dev d) {
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bi >= P.nbox) return;
+  if (d.box_err[bi] != 0 || d.box_steps[bi] >= *d.goal) return;
+  if (d.box_rebuild[bi]) {
+    d.box_rebuild[bi] = 0;
+    d.box_rebuilds[bi] += 1;
+  }
+  if (d.box_req[bi]) {
+    d.box_rebuild[bi] = 1;
+    d.box_req[bi] = 0;
+  }
+  if (INNER != 0) {
+    d.box_prune[bi] = d.box_preq[bi];
+    d.box_preq[bi] = 0;
+  }
+  d.box_steps[bi] += 1;
 }
 
 // Per-box observer sums at q_end (observer.cc:5-79 expressions, pairs 1/2 each).
@@ -718,6 +792,7 @@ struct mdg_batch {
   int nbox = 0, total = 0, num_sms = 0;
   int threads = 256, lpi = 1, ctas_per_sm = 2;
   int use_inner = 1;  // one lane per particle walks the inner list (when the buffer is > 0)
+  int flat = 0;       // 1: the flat layout of the step (k_batch_step_flat + k_batch_finish)
   cudaStream_t stream = nullptr;
   Params P;
   Dev d;
@@ -761,7 +836,16 @@ cudaError_t balloc(T **p, size_t count) {
 }
 
 // The persistent step kernel the shape selects (as launch_batch_step does).
-const void *step_kernel_fn(int prec, int lpi, bool inner) {
+const void *step_kernel_fn(int prec, int lpi, bool inner, bool flat) {
+  if (flat) {
+    if (prec == MDG_MIXED) return inner ? reinterpret_cast<const void *>(&k_batch_step_flat<MDG_MIXED, 1>)
+                                        : reinterpret_cast<const void *>(&k_batch_step_flat<MDG_MIXED, 0>);
+    if (prec == MDG_MIXED_PLAIN)
+      return inner ? reinterpret_cast<const void *>(&k_batch_step_flat<MDG_MIXED_PLAIN, 1>)
+                   : reinterpret_cast<const void *>(&k_batch_step_flat<MDG_MIXED_PLAIN, 0>);
+    return inner ? reinterpret_cast<const void *>(&k_batch_step_flat<MDG_FP64, 1>)
+                 : reinterpret_cast<const void *>(&k_batch_step_flat<MDG_FP64, 0>);
+  }
 #define MDG_BFN(M, L, I) reinterpret_cast<const void *>(&k_batch_step<M, L, I>)
   if (prec == MDG_MIXED)
     return lpi == 4 ? MDG_BFN(MDG_MIXED, 4, 0) : lpi == 2 ? MDG_BFN(MDG_MIXED, 2, 0)
@@ -780,7 +864,8 @@ const void *step_kernel_fn(int prec, int lpi, bool inner) {
 int resident_ctas(const mdg_batch *b, int threads) {
   const bool inner = b->P.inner && b->lpi == 1 && b->use_inner;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, step_kernel_fn(b->prm.precision, b->lpi, inner), threads,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, step_kernel_fn(b->prm.precision, b->lpi, inner, b->flat != 0),
+                                                    threads,
                                                     0) != cudaSuccess)
     return 1;
   return nb > 0 ? nb : 1;
@@ -851,6 +936,18 @@ void launch_batch_step(mdg_batch *b, int par) {
   k_batch_list<<<b->num_sms * 16, 128, 0, b->stream>>>(b->P, b->d);
 #define MDG_BSTEP(M, L, I) k_batch_step<M, L, I><<<b->grid, T, 0, b->stream>>>(b->P, b->d, par)
   const bool inner = b->P.inner && b->lpi == 1 && b->use_inner;
+  if (b->flat) {
+#define MDG_FSTEP(M, I) k_batch_step_flat<M, I><<<b->grid, T, 0, b->stream>>>(b->P, b->d, par)
+    if (prec == MDG_MIXED) { if (inner) MDG_FSTEP(MDG_MIXED, 1); else MDG_FSTEP(MDG_MIXED, 0); }
+    else if (prec == MDG_MIXED_PLAIN) { if (inner) MDG_FSTEP(MDG_MIXED_PLAIN, 1); else MDG_FSTEP(MDG_MIXED_PLAIN, 0); }
+    else { if (inner) MDG_FSTEP(MDG_FP64, 1); else MDG_FSTEP(MDG_FP64, 0); }
+#undef MDG_FSTEP
+    const int fg = (b->nbox + 255) / 256;
+    if (inner) k_batch_finish<1><<<fg, 256, 0, b->stream>>>(b->P, b->d);
+    else k_batch_finish<0><<<fg, 256, 0, b->stream>>>(b->P, b->d);
+    b->launches += kBatchKernelsPerStep + 1;
+    return;
+  }
   if (prec == MDG_MIXED) {
     if (b->lpi == 4) MDG_BSTEP(MDG_MIXED, 4, 0); else if (b->lpi == 2) MDG_BSTEP(MDG_MIXED, 2, 0);
     else if (inner) MDG_BSTEP(MDG_MIXED, 1, 1); else MDG_BSTEP(MDG_MIXED, 1, 0);
@@ -890,7 +987,7 @@ int run_steps(mdg_batch *b, int nsteps) {
         if (e != cudaSuccess) return bfail(b, MDG_ERR_CUDA, cudaGetErrorString(e));
       }
       MDG_BCK(cudaGraphLaunch(b->gx[par], b->stream));
-      b->launches += 2 * kBatchKernelsPerStep;
+      b->launches += 2 * (kBatchKernelsPerStep + (b->flat ? 1 : 0));
       left -= 2;
     } else {
       launch_batch_step(b, par);
@@ -987,6 +1084,7 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
   P.dt2 = p->dt * 0.5;
   P.half_margin2 = 0.25 * p->margin * p->margin;
   P.nbox = nbox;
+  P.total = (int)total;
   // inner-list buffer: negative = min(0.1, margin / 2), as the single-box form
   const double buffer = p->prune_buffer < 0.0 ? std::fmin(0.1, 0.5 * p->margin) : p->prune_buffer;
   P.inner = buffer > 0.0 ? 1 : 0;
@@ -1023,6 +1121,10 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
   if (e == cudaSuccess) e = balloc(&d.pcount, n);
   if (e == cudaSuccess) e = balloc(&d.loc_p, n);
   if (e == cudaSuccess) e = balloc(&d.box_prune, nbox);
+  if (e == cudaSuccess) e = balloc(&d.box_req, nbox);
+  if (e == cudaSuccess) e = balloc(&d.box_preq, nbox);
+  if (e == cudaSuccess) e = cudaMemset(d.box_req, 0, nbox * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(d.box_preq, 0, nbox * sizeof(int));
   if (e == cudaSuccess) e = balloc(&d.rb_boxes, nbox);
   if (e == cudaSuccess) e = balloc(&d.rb_start, (size_t)nbox + 1);
   if (e == cudaSuccess) e = balloc(&d.rb_count, 1);
@@ -1059,7 +1161,7 @@ int mdg_batch_destroy(mdg_batch *b) {
   Dev &d = b->d;
   void *ptrs[] = {d.boxes, d.cta_start, d.cta_boxes, d.q_end, d.q_mid[0], d.q_mid[1], d.p, d.q_build, d.t_q, d.t_p,
                   d.qf, d.loc[0], d.loc[1], d.id, d.cell, d.t_id, d.t_cell, d.order, d.cell_start, d.nl, d.ncount,
-                  d.pl, d.pcount, d.loc_p, d.box_prune, d.rb_boxes, d.rb_start, d.rb_count,
+                  d.pl, d.pcount, d.loc_p, d.box_prune, d.box_req, d.box_preq, d.rb_boxes, d.rb_start, d.rb_count,
                   d.box_rebuild, d.box_err, d.box_need, d.box_steps, d.box_rebuilds, d.goal, d.partials,
                   b->d_box_of_slot};
   for (void *p : ptrs)
@@ -1090,6 +1192,8 @@ int mdg_batch_set_state(mdg_batch *b, const double *q4, const double *p4) {
   MDG_BCK(cudaMemcpyAsync(b->d.box_need, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(b->d.box_steps, lz.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(b->d.box_rebuilds, lz.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.box_req, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemcpyAsync(b->d.box_preq, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   MDG_BCK(cudaStreamSynchronize(b->stream));
   b->steps = 0;
   b->par = 0;
@@ -1190,11 +1294,12 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
   const long long steps0 = b->steps;
   // one trial: the shape from the saved state with fresh lists; *ms receives
   // the device time of `steps` steps after the two that build the lists
-  auto trial = [&](int T, int Lp, int C, int I, int steps, double *ms) -> int {
+  auto trial = [&](int T, int Lp, int C, int I, int F, int steps, double *ms) -> int {
     b->threads = T;
     b->lpi = Lp;
     b->ctas_per_sm = C;
     b->use_inner = I;
+    b->flat = F;
     int rc = assign(b);
     if (rc) return rc;
     MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
@@ -1214,33 +1319,52 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
   };
   const int Ts[] = {128, 256, 512}, Ls[] = {1, 2, 4}, Cs[] = {1, 2, 3, 4};
   double best = 1e300;
-  int bt = b->threads, bl = b->lpi, bc = b->ctas_per_sm, bi = 0;
+  int bt = b->threads, bl = b->lpi, bc = b->ctas_per_sm, bi = 0, bf = 0;
   for (int T : Ts)
     for (int Lp : Ls)
       for (int C : Cs) {
         if (T * C > 2048) continue;
         b->lpi = Lp;
         b->use_inner = 0;
+        b->flat = 0;
         if (C > resident_ctas(b, T)) continue;  // would run in waves (assign would cap it)
         double ms = 0.0;
-        int rc = trial(T, Lp, C, 0, trial_steps, &ms);
+        int rc = trial(T, Lp, C, 0, 0, trial_steps, &ms);
         if (rc) return rc;
         if (ms < best) {
           best = ms;
           bt = T;
           bl = Lp;
           bc = C;
+          bf = 0;
         }
       }
+  // the flat layout, one lane per particle, with every resident CTA
+  for (int T : {128, 256}) {
+    b->lpi = 1;
+    b->use_inner = 0;
+    b->flat = 1;
+    const int C = resident_ctas(b, T);
+    double ms = 0.0;
+    int rc = trial(T, 1, C, 0, 1, trial_steps, &ms);
+    if (rc) return rc;
+    if (ms < best) {
+      best = ms;
+      bt = T;
+      bl = 1;
+      bc = C;
+      bf = 1;
+    }
+  }
   // the inner list (one lane per particle) on and off over longer trials: it
   // pays when the boxes re-select their inner rows rarely (small steps,
   // FP64), which short trials from fresh lists cannot show
   if (bl == 1 && b->P.inner) {
     const int longer = std::max((int)trial_steps, 60);
     double off = 0.0, on = 0.0;
-    int rc = trial(bt, 1, bc, 0, longer, &off);
+    int rc = trial(bt, 1, bc, 0, bf, longer, &off);
     if (rc) return rc;
-    rc = trial(bt, 1, bc, 1, longer, &on);
+    rc = trial(bt, 1, bc, 1, bf, longer, &on);
     if (rc) return rc;
     bi = on < off ? 1 : 0;
   }
@@ -1248,6 +1372,7 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
   b->lpi = bl;
   b->ctas_per_sm = bc;
   b->use_inner = bi;
+  b->flat = bf;
   int rc = assign(b);
   if (rc) return rc;
   MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
@@ -1271,7 +1396,7 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
 int mdg_batch_set_shape(mdg_batch *b, int32_t threads, int32_t lanes_per_particle, int32_t ctas_per_sm) {
   if (!b || (threads != 128 && threads != 256 && threads != 512 && threads != 1024) ||
       (lanes_per_particle != 1 && lanes_per_particle != 2 && lanes_per_particle != 4) || ctas_per_sm < 1 ||
-      threads * ctas_per_sm > 2048)
+      threads * ctas_per_sm > 2048 || (b->flat && (lanes_per_particle != 1 || threads > kFlatMaxThreads)))
     return MDG_ERR_INVALID;
   b->threads = threads;
   b->lpi = lanes_per_particle;
@@ -1283,6 +1408,14 @@ int mdg_batch_set_inner(mdg_batch *b, int32_t on) {
   if (!b) return MDG_ERR_INVALID;
   b->use_inner = on ? 1 : 0;
   return assign(b);  // fresh selections, graphs captured again
+}
+
+int mdg_batch_set_flat(mdg_batch *b, int32_t on) {
+  if (!b) return MDG_ERR_INVALID;
+  if (on && (b->lpi != 1 || b->threads > kFlatMaxThreads))
+    return bfail(b, MDG_ERR_INVALID, "the flat layout takes one lane per particle and at most 256 threads per CTA");
+  b->flat = on ? 1 : 0;
+  return assign(b);
 }
 
 int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s) {
@@ -1299,6 +1432,7 @@ int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s) {
   s->lanes_per_particle = b->lpi;
   s->ctas_per_sm = b->ctas_per_sm;
   s->inner_list = (b->P.inner && b->lpi == 1 && b->use_inner) ? 1 : 0;
+  s->flat = b->flat;
   s->elapsed_ms = b->last_ms;
   s->kernel_launches = b->launches;
   return MDG_OK;

@@ -56,14 +56,44 @@ def test_batch_mixed_close_to_fp64(precision):
     np.testing.assert_allclose(m.observe_raw(), a.observe_raw(), rtol=1e-5, atol=1e-5)
 
 
-@pytest.mark.parametrize("shape", [(128, 1, 4), (256, 2, 2), (512, 4, 1)])
+@pytest.mark.parametrize("shape", [(128, 1, 4), (256, 2, 2), (512, 4, 1), (128, 1, 8, "flat"), (256, 1, 5, "flat")])
 def test_batch_shapes_agree(shape):
+    # per-box CTAs in three shapes and the flat layout (the grid striding over
+    # every box's particles, per-box flags applied after the step) in two
     from mdacp_gb300.batch import Batch
     boxes = _boxes(6, seed=7)
     b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT)
-    b.set_shape(*shape)
+    b.set_shape(*shape[:3])
+    if len(shape) > 3:
+        b.set_flat(True)
+        assert b.stats()["flat"] == 1
     b.calculate(60)
     np.testing.assert_allclose(b.observe_raw(), _oracle_obs(boxes, 60), rtol=1e-10, atol=1e-10)
+    st = b.stats()
+    assert st["steps"] == 60 and st["rebuilds"] >= len(boxes)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_flat_layout_matches_per_box_layout(precision):
+    # the same boxes through both layouts, inner list on, with a tiny buffer so
+    # the boxes re-select every few steps: the per-particle arithmetic and the
+    # per-box rebuild / re-selection schedule are the same, so the states agree
+    # bit for bit
+    from mdacp_gb300.batch import Batch
+    boxes = _boxes(8, seed=17, n_range=(500, 8000))
+    runs = []
+    for flat in (False, True):
+        b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision=precision, prune_buffer=0.02)
+        b.set_shape(256, 1, 2)
+        b.set_flat(flat)
+        b.calculate(70)
+        st = b.stats()
+        assert st["inner_list"] == 1 and st["flat"] == (1 if flat else 0)
+        runs.append(([x.copy() for pair in b.state() for x in pair], st["rebuilds"]))
+    (a, ra), (c, rc) = runs
+    assert ra == rc
+    for u, v in zip(a, c):
+        assert np.array_equal(u, v)
 
 
 def test_batch_overflow_regrows_and_catches_up():
