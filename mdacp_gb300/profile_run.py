@@ -32,7 +32,7 @@ def main():
                     help="run the batched-replica workload instead: this many boxes (N ~ U[500, 8000], "
                          "density ~ U[0.3, 0.9], T ~ U[0.7, 1.5], margin 0.4, dt 0.002), autotuned shape")
     ap.add_argument("--shape", default="",
-                    help="threads,lanes,ctas_per_sm[,inner 0|1] for --boxes instead of the autotuner")
+                    help="threads,lanes,ctas_per_sm[,inner 0|1[,flat 0|1]] for --boxes instead of the autotuner")
     ap.add_argument("--adjoint", action="store_true", help="one adjoint gradient instead (4,000 atoms)")
     a = ap.parse_args()
     if a.adjoint:
@@ -58,6 +58,8 @@ def main():
             b.set_shape(*shape[:3])
             if len(shape) > 3:
                 b.set_inner(shape[3] != 0)
+            if len(shape) > 4:
+                b.set_flat(shape[4] != 0)
         else:
             shape = b.tune(trial_steps=10)
         b.calculate(a.steps)

@@ -77,8 +77,10 @@ def test_batch_shapes_agree(shape):
 def test_batch_flat_layout_matches_per_box_layout(precision):
     # the same boxes through both layouts, inner list on, with a tiny buffer so
     # the boxes re-select every few steps: the per-particle arithmetic and the
-    # per-box rebuild / re-selection schedule are the same, so the states agree
-    # bit for bit
+    # per-box rebuild / re-selection schedule are the same.  The mixed states
+    # agree bit for bit; in FP64 the compiler may fuse the pair expressions
+    # (r^2, the force factor) differently in the two kernels, so the states
+    # agree to the rounding that grows from there (1e-9 after 70 steps)
     from mdacp_gb300.batch import Batch
     boxes = _boxes(8, seed=17, n_range=(500, 8000))
     runs = []
@@ -93,7 +95,10 @@ def test_batch_flat_layout_matches_per_box_layout(precision):
     (a, ra), (c, rc) = runs
     assert ra == rc
     for u, v in zip(a, c):
-        assert np.array_equal(u, v)
+        if precision == "mixed":
+            assert np.array_equal(u, v)
+        else:
+            np.testing.assert_allclose(v, u, rtol=1e-9, atol=1e-9)
 
 
 def test_batch_overflow_regrows_and_catches_up():
@@ -112,7 +117,12 @@ def test_autotuner_restores_state():
     b.calculate(10)
     before = [x.copy() for pair in b.state() for x in pair]
     t, lanes, c = b.tune(trial_steps=4)
-    assert t in (128, 256, 512) and lanes in (1, 2, 4) and c in (1, 2, 3, 4)
+    st = b.stats()
+    assert t in (128, 256, 512) and lanes in (1, 2, 4) and st["flat"] in (0, 1)
+    # every CTA resident: at most 2,048 threads per SM, the flat layout with
+    # one lane per particle and at most 256 threads
+    assert 1 <= st["ctas_per_sm"] and t * st["ctas_per_sm"] <= 2048
+    assert not st["flat"] or (lanes == 1 and t <= 256)
     after = [x for pair in b.state() for x in pair]
     for u, v in zip(before, after):
         assert np.array_equal(u, v)
