@@ -510,7 +510,7 @@ def run_batch1024(args):
         st = b.stats()
         res[prec] = {"ms": st["elapsed_ms"], "shape": {"threads": shape[0], "lanes_per_particle": shape[1],
                                                         "ctas_per_sm": st["ctas_per_sm"], "inner_list": st["inner_list"],
-                                                        "flat": st["flat"]},
+                                                        "flat": st["flat"], "prune_buffer": st["prune_buffer"]},
                      "rebuilds": st["rebuilds"], "kernels_per_step": 7 if st["flat"] else 6}
         b.close()
     cfg = {"workload": "1024 replica boxes, %d atoms total, N~U[500,8000], rho~U[0.3,0.9], T~U[0.7,1.5], "

@@ -192,6 +192,8 @@ typedef struct mdg_batch_stats {
   int64_t kernel_launches;
   int32_t flat;               /* 1: flat layout (see mdg_batch_set_flat) */
   int32_t reserved;
+  double prune_buffer;        /* inner-list buffer in use (mdg_batch_tune may pick margin / 2
+                                 when the parameters left it automatic); 0 without inner list */
 } mdg_batch_stats;
 
 typedef struct mdg_batch mdg_batch;

@@ -22,7 +22,7 @@ class BatchStats(ctypes.Structure):
                 ("boxes", ctypes.c_int32), ("list_capacity", ctypes.c_int32), ("threads", ctypes.c_int32),
                 ("lanes_per_particle", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("inner_list", ctypes.c_int32),
                 ("elapsed_ms", ctypes.c_double), ("kernel_launches", ctypes.c_int64), ("flat", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("reserved", ctypes.c_int32), ("prune_buffer", ctypes.c_double)]
 
 
 _P = ctypes.c_void_p

@@ -793,6 +793,7 @@ struct mdg_batch {
   int threads = 256, lpi = 1, ctas_per_sm = 2;
   int use_inner = 1;  // one lane per particle walks the inner list (when the buffer is > 0)
   int flat = 0;       // 1: the flat layout of the step (k_batch_step_flat + k_batch_finish)
+  double buffer = 0.0;  // inner-list buffer in use
   cudaStream_t stream = nullptr;
   Params P;
   Dev d;
@@ -869,6 +870,18 @@ int resident_ctas(const mdg_batch *b, int threads) {
                                                     0) != cudaSuccess)
     return 1;
   return nb > 0 ? nb : 1;
+}
+
+// The inner-list buffer b: rows keep the listed pairs within rc + b and are
+// re-selected when a particle of the box moved b / 2 since the last selection.
+void set_prune_buffer(mdg_batch *b, double buffer) {
+  Params &P = b->P;
+  const double rb = b->prm.cutoff + buffer;
+  P.prune_thr2d = rb * rb;
+  P.prune_thr2f = (float)(rb * rb + 1e-4);  // float r2 of local positions is within ~1e-5
+  P.half_prune2 = (float)(0.25 * buffer * buffer * (1.0 - 1e-4));
+  b->buffer = buffer;
+  drop_batch_graphs(b);  // the graphs hold the parameters by value
 }
 
 // Longest-first assignment of boxes to grid CTAs (work ~ n * list capacity).
@@ -1085,13 +1098,11 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
   P.half_margin2 = 0.25 * p->margin * p->margin;
   P.nbox = nbox;
   P.total = (int)total;
-  // inner-list buffer: negative = min(0.1, margin / 2), as the single-box form
+  // inner-list buffer: negative = min(0.1, margin / 2), as the single-box
+  // form (the autotuner may then pick margin / 2 instead)
   const double buffer = p->prune_buffer < 0.0 ? std::fmin(0.1, 0.5 * p->margin) : p->prune_buffer;
   P.inner = buffer > 0.0 ? 1 : 0;
-  const double rb = p->cutoff + buffer;
-  P.prune_thr2d = rb * rb;
-  P.prune_thr2f = (float)(rb * rb + 1e-4);  // float r2 of local positions is within ~1e-5
-  P.half_prune2 = (float)(0.25 * buffer * buffer * (1.0 - 1e-4));
+  set_prune_buffer(b, buffer);
   int cap = p->list_capacity > 0 ? p->list_capacity : (int)(max_rho * 4.18879020478639 * sl * sl * sl * 1.5 + 24);
   cap = (cap + 7) & ~7;
   cudaError_t e = cudaSetDevice(p->device);
@@ -1358,15 +1369,30 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
   }
   // the inner list (one lane per particle) on and off over longer trials: it
   // pays when the boxes re-select their inner rows rarely (small steps,
-  // FP64), which short trials from fresh lists cannot show
+  // FP64), which short trials from fresh lists cannot show.  With the
+  // automatic buffer, half the margin is tried beside min(0.1, margin / 2):
+  // a longer inner row, re-selected about half as often
   if (bl == 1 && b->P.inner) {
     const int longer = std::max((int)trial_steps, 60);
-    double off = 0.0, on = 0.0;
+    double off = 0.0, best_on = 1e300;
     int rc = trial(bt, 1, bc, 0, bf, longer, &off);
     if (rc) return rc;
-    rc = trial(bt, 1, bc, 1, bf, longer, &on);
-    if (rc) return rc;
-    bi = on < off ? 1 : 0;
+    const double buf0 = b->buffer;
+    double best_buf = buf0;
+    std::vector<double> bufs{buf0};
+    if (b->prm.prune_buffer < 0.0 && 0.5 * b->prm.margin > buf0 * (1.0 + 1e-9)) bufs.push_back(0.5 * b->prm.margin);
+    for (double buf : bufs) {
+      set_prune_buffer(b, buf);
+      double on = 0.0;
+      rc = trial(bt, 1, bc, 1, bf, longer, &on);
+      if (rc) return rc;
+      if (on < best_on) {
+        best_on = on;
+        best_buf = buf;
+      }
+    }
+    set_prune_buffer(b, best_buf);
+    bi = best_on < off ? 1 : 0;
   }
   b->threads = bt;
   b->lpi = bl;
@@ -1433,6 +1459,7 @@ int mdg_batch_get_stats(mdg_batch *b, mdg_batch_stats *s) {
   s->ctas_per_sm = b->ctas_per_sm;
   s->inner_list = (b->P.inner && b->lpi == 1 && b->use_inner) ? 1 : 0;
   s->flat = b->flat;
+  s->prune_buffer = b->P.inner ? b->buffer : 0.0;
   s->elapsed_ms = b->last_ms;
   s->kernel_launches = b->launches;
   return MDG_OK;

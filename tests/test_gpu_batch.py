@@ -144,7 +144,7 @@ def test_inner_list_changes_nothing(precision):
     from mdacp_gb300.batch import Batch
     boxes = _boxes(6, seed=13)
     runs = []
-    for buf in (0.0, None, 0.02):
+    for buf in (0.0, None, 0.02, 0.2):  # 0.2: half the margin, a choice of the autotuner
         b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision=precision, prune_buffer=buf)
         b.set_shape(256, 1, 2)
         b.calculate(80)
