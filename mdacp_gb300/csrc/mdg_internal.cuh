@@ -8,7 +8,8 @@
 //                       reads one buffer and writes the other.  Mixed form:
 //                       relative to the centre of the slot's home cell
 //   p[n]       double4_32a  momenta (= velocities, m = 1)
-//   q_build[n] double4_32a  positions at the last list build (displacement check)
+//   q_build[n] double4_32a  positions at the last list build (the FP64 form's
+//                       displacement check; the mixed form tests against qf)
 //   id[n]      int      caller's particle index of each slot; inv[id] = slot
 //   cell[n]    int      home cell of each slot at the last build
 //   nl[cap*n]  uint32   neighbour list, ELL layout: entry k of slot i at k*stride+i

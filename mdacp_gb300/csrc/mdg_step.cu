@@ -8,7 +8,7 @@
 //   the second half-drift ForceCalculator::UpdatePositionHalf (fcalculator.cc:21-32)
 //     and the first half-drift of the following step;
 //   the expiry test of PairList::IsPairListExpired (pairlist.cc:26-45), here the
-//     displacement criterion |q - q_build| > margin/2.
+//     displacement criterion: moved more than margin/2 since the build.
 // It is a gather over the full neighbour list: one thread per particle, no
 // atomics, no reaction scatter (the "Reactless" form, fcalculator.cc:504-542).
 //
@@ -21,12 +21,16 @@
 // compensated float (Kahan: each term's lost low part carried in a second
 // float, four float operations per component and pair), so the sum's error
 // does not grow with the number of partners; converted to double once per
-// particle; momentum and position updates in double with fused multiply-adds.
-// MDG_MIXED_PLAIN sums the pair forces in plain float instead (an error near
-// u sqrt(40) |f_ij|, u = 2^-24, over about 40 terms).  GB300 runs double
-// precision at 1/64 of the float rate, so the per-particle double work
-// (momentum, two half-drifts, displacement) is kept to one operation per
-// component each, and the per-pair work stays in float.
+// particle; momentum and position updates in double with fused multiply-adds,
+// the mid-step positions kept relative to the centre of the home cell (so the
+// float position partners gather is one conversion and the displacement since
+// the build is tested in float against the build's local position) and the
+// step-boundary positions not written (the readers rebuild them from q_mid
+// and p).  MDG_MIXED_PLAIN sums the pair forces in plain float instead (an
+// error near u sqrt(40) |f_ij|, u = 2^-24, over about 40 terms).  GB300 runs
+// double precision at 1/64 of the float rate, so the per-particle double work
+// (momentum, two half-drifts) is kept to one operation per component each,
+// and the per-pair work stays in float.
 #include "mdg_internal.cuh"
 
 namespace mdg {
