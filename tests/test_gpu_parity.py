@@ -285,3 +285,33 @@ def test_phase_times_split_the_run():
     ref.make_pairlist()
     ref.calculate(60)
     np.testing.assert_allclose(m.observe(), ref.observe(), rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_plain"])
+def test_mixed_readers_leave_the_trajectory_alone(precision):
+    # the mixed form keeps mid-step positions relative to the home cell and
+    # does not write the step-boundary positions; readers (observers, forces,
+    # get_state) and rebuilds form them from q_mid and p.  Reading between
+    # steps must not perturb the run: 300 steps in one call and the same steps
+    # in chunks with every reader in between end bit for bit in the same
+    # state, with several list rebuilds on the way
+    q, p, L = liquid_like(0.5, 16, seed=37)
+    a = _gpu(L, len(q), precision=precision)
+    b = _gpu(L, len(q), precision=precision)
+    for m in (a, b):
+        m.set_state(q, p)
+        m.make_pairlist()
+    a.calculate(300)
+    done = 0
+    for chunk in (37, 1, 62, 100, 100):
+        b.calculate(chunk)
+        done += chunk
+        b.observe_raw()
+        b.forces()
+        b.state()
+    assert done == 300
+    qa, pa = a.state()
+    qb, pb = b.state()
+    assert np.array_equal(qa, qb) and np.array_equal(pa, pb)
+    assert a.stats()["rebuilds"] == b.stats()["rebuilds"] >= 3
+    np.testing.assert_array_equal(a.observe_raw(), b.observe_raw())
