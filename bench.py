@@ -20,7 +20,7 @@ value     mixed-form atom-steps/s over K steps (pair force in f32, per-atom
 e2e       the same through the public C ABI from host memory: pinned host state
           uploaded with mdg_set_state, K calls of mdg_calculate(1), mdg_observe
           every 100 steps (as Benchmark::Run observes), state read back with
-          mdg_get_state; wall clock.
+          mdg_get_state; wall clock, the median of three such windows.
 roofline  the fused step kernel (mixed) over the same K steps: its mean launch
           time from the window's event nodes; achieved = DRAM bytes per launch
           (an ncu capture of the same kernel, per atom, scaled by the atoms and
@@ -53,6 +53,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LJ atom-steps/s, 4M atoms: mixed vs FP64 on 1 GB300 @ rel force err<=1e-5"
 UNIT = "atom-steps/s"
+E2E_WINDOWS = 3
 RC, MARGIN, DT, TEMP, DENSITY = 2.5, 0.5, 0.001, 1.0, 0.5
 
 
@@ -356,18 +357,25 @@ def run_mine(args):
     me.set_state(qh, ph)
     me.calculate(W)
     me.synchronize()  # the warm-up steps finish before the clock starts
-    d.barrier()
-    t0 = time.perf_counter()
-    me.set_state(qh, ph)
-    nobs = 0
-    for k in range(K):
-        me.calculate(1)
-        if k % 100 == 0:
-            me.observe_raw()
-            nobs += 1
-    me.state(qo, po)
-    t_e2e = d.max(time.perf_counter() - t0)
-    e2e_rebuilds = me.stats()["rebuilds"]
+    # E2E_WINDOWS windows, each from the upload to the read-back; the median
+    # is reported (one window of the short default run lasts ~20 ms, so a
+    # single host-side stall would otherwise decide the figure)
+    windows, window_rebuilds = [], []
+    for _ in range(E2E_WINDOWS):
+        d.barrier()
+        t0 = time.perf_counter()
+        me.set_state(qh, ph)
+        nobs = 0
+        for k in range(K):
+            me.calculate(1)
+            if k % 100 == 0:
+                me.observe_raw()
+                nobs += 1
+        me.state(qo, po)
+        windows.append(d.max(time.perf_counter() - t0))
+        window_rebuilds.append(me.stats()["rebuilds"])  # counted from the upload (mdg_set_state resets it)
+    t_e2e = float(np.median(windows))
+    e2e_rebuilds = window_rebuilds
     me.close()
     e2e_value = d.world * n * K / t_e2e
     cpu = None
@@ -397,7 +405,8 @@ def run_mine(args):
                 "mixed": form(mixed), "mixed_plain": form(res["mixed_plain"]), "fp64": form(res["fp64"]),
                 "mixed_over_fp64": res["fp64"]["ms"] / mixed["ms"],
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * n * 32 / K,
-                        "d2h_bytes_per_step": (2 * n * 32 + 24 * nobs) / K, "rebuilds": e2e_rebuilds},
+                        "d2h_bytes_per_step": (2 * n * 32 + 24 * nobs) / K, "rebuilds_per_window": e2e_rebuilds,
+                        "windows_ms": [round(1e3 * t, 3) for t in windows], "reported": "median window"},
                 "gpu_launches": mixed["launches"],
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clocks}
         if "amortised" in mixed:

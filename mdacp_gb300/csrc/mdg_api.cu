@@ -855,7 +855,7 @@ int mdg_observe(mdg_handle *h, double out[3]) {
   rc = ensure_list(h, false);
   if (rc) return rc;
   mdg::launch_observe(h->g, h->d, h->dobs, h->stream, h->prm.precision != MDG_FP64, h->par);
-  h->launches += h->prm.precision != MDG_FP64 ? 5 : 2;
+  h->launches += h->prm.precision != MDG_FP64 ? 3 : 2;
   MDG_CK(cudaMemcpyAsync(h->hobs, h->dobs, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   out[0] = h->hobs[0];
@@ -871,7 +871,7 @@ int mdg_forces(mdg_handle *h, double *f4) {
   rc = ensure_list(h, false);
   if (rc) return rc;
   mdg::launch_forces(h->g, h->d, h->prm.precision, h->par, h->stream);
-  h->launches += h->prm.precision != MDG_FP64 ? 4 : 1;
+  h->launches += h->prm.precision != MDG_FP64 ? 2 : 1;
   MDG_CK(cudaMemcpyAsync(f4, h->d.io4, (size_t)h->g.n * sizeof(double4_32a), cudaMemcpyDeviceToHost, h->stream));
   MDG_CK(cudaStreamSynchronize(h->stream));
   return MDG_OK;

@@ -151,18 +151,20 @@ __device__ __forceinline__ double3 force_fp64(const Geom &g, const Dev &d, const
   return make_double3(fx, fy, fz);
 }
 
-// Mixed form of force_fp64 on home-cell-local float positions.  The offset
-// between the home cells of i and j is ox*w + s*(L - nc*w) per axis, s the
-// periodic wrap of the stencil step, evaluated as the quadratic of axis_quad.
-// KAHAN: the per-particle sums compensated (MDG_MIXED), else plain float
-// (MDG_MIXED_PLAIN).  EDGE: the home cell touches the periodic boundary, so
-// the offset is the quadratic; otherwise it is linear with the cell width as
+// Walks the row of slot i on home-cell-local float positions and hands each
+// entry's partner offset q_j - q_i and its r^2 to pair(e, dx, dy, dz, r2).
+// The offset between the home cells of i and j is ox*w + s*(L - nc*w) per
+// axis, s the periodic wrap of the stencil step, evaluated as the quadratic
+// of axis_quad.  EDGE: the home cell touches the periodic boundary, so the
+// offset is the quadratic; otherwise it is linear with the cell width as
 // slope (b = 0, a = w: fmaf(fmaf(0, t, a), t, c) = fmaf(a, t, c) exactly), the
 // width coming from the kernel parameters instead of two registers per axis.
-template <bool PRUNE, bool KAHAN, bool EDGE>
-__device__ __forceinline__ double3 pair_loop(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
-                                             const float4 &li, const CellPos &cp, const uint32_t *__restrict__ list,
-                                             const int *__restrict__ counts, int *kept) {
+// An entry whose slot a checked build rejects (code `site`) and the padding of
+// the last batch get a partner at 1e30, whose r^2 overflows to +inf.
+template <bool EDGE, int SITE, class Pair>
+__device__ __forceinline__ void walk_row(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
+                                         const float4 &li, const CellPos &cp, const uint32_t *__restrict__ list,
+                                         int cnt, Pair &&pair) {
   AxisQuad qx, qy, qz;
   if (EDGE) {
     qx = axis_quad(g.w32[0], g.dl32[0], cp.cx == 0, cp.cx == g.nc[0] - 1, li.x, 1.0f);
@@ -177,22 +179,14 @@ __device__ __forceinline__ double3 pair_loop(const Geom &g, const Dev &d, const 
     qy.c = -li.y;
     qz.c = -li.z;
   }
-  int cnt = counts[i];
-  if (!MDG_IN_RANGE(d.flags, kCheckStepRow, cnt, g.list_cap + 1)) cnt = 0;
   const uint32_t *row = list + i;
   const size_t stride = (size_t)g.stride;
-  float sx = 0.f, sy = 0.f, sz = 0.f;
-  float cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan corrections
-  // a partner position (a far one, contributing nothing, for an entry a
-  // checked build rejects)
   auto gather = [&](uint32_t e) -> float4 {
     const int j = entry_slot(e);
-    if (!MDG_IN_RANGE(d.flags, kCheckStepSlot, j, g.n)) return make_float4(1e30f, 1e30f, 1e30f, 0.f);
+    if (!MDG_IN_RANGE(d.flags, SITE, j, g.n)) return make_float4(1e30f, 1e30f, 1e30f, 0.f);
     return __ldg(loc + j);
   };
-  const float rc2 = g.rc2f, c2x8 = g.c2x8f, thr = g.prune_thr2;
-  int m = 0;
-  auto pair = [&](uint32_t e, const float4 &lj) {
+  auto offset = [&](uint32_t e, const float4 &lj) {
     const float tx = step_float(e, 0x03u, 8388609.0f);   // t
     const float ty = step_float(e, 0x0Cu, 8388612.0f);   // 4 t
     const float tz = step_float(e, 0x30u, 8388624.0f);   // 16 t
@@ -206,28 +200,7 @@ __device__ __forceinline__ double3 pair_loop(const Geom &g, const Dev &d, const 
       dy = lj.y + fmaf(qy.a, ty, qy.c);
       dz = lj.z + fmaf(qz.a, tz, qz.c);
     }
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    if (PRUNE && r2 <= thr) d.pl[(size_t)(m++) * stride + i] = e;
-    // evaluated for every entry and masked: no divergent branch per pair
-    float inv;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
-    const float i6 = inv * inv * inv;
-    float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8;
-    df = r2 <= rc2 ? df : 0.0f;
-    if (KAHAN) {
-      // a zero term (a pair beyond rc) leaves s - c unchanged as a real
-      // number (t - s is exact, and so is the new correction), but it moves
-      // the correction into s and the later additions round differently:
-      // lists that differ only by pairs beyond rc give forces that agree to
-      // about one float rounding, not bit for bit
-      kahan_fma(sx, cx, df, dx);
-      kahan_fma(sy, cy, df, dy);
-      kahan_fma(sz, cz, df, dz);
-    } else {
-      sx = fmaf(df, dx, sx);
-      sy = fmaf(df, dy, sy);
-      sz = fmaf(df, dz, sz);
-    }
+    pair(e, dx, dy, dz, dx * dx + dy * dy + dz * dz);
   };
   int k = 0;
   // the next batch's list entries are requested before this batch's partner
@@ -258,19 +231,58 @@ __device__ __forceinline__ double3 pair_loop(const Geom &g, const Dev &d, const 
       if (kp < cnt) asm volatile("prefetch.global.L2 [%0];" ::"l"(row + (size_t)kp * stride));
     }
 #pragma unroll
-    for (int u = 0; u < kUnroll; u++) pair(e[u], l[u]);
+    for (int u = 0; u < kUnroll; u++) offset(e[u], l[u]);
   }
   if (k < cnt) {
-    // the remainder as one batch; missing entries get a partner at 1e30,
-    // whose r^2 overflows to +inf and contributes nothing
+    // the remainder as one batch
     constexpr int kTail = kUnroll > 1 ? kUnroll - 1 : 1;
     float4 l[kTail];
 #pragma unroll
     for (int u = 0; u < kTail; u++)
       l[u] = k + u < cnt ? gather(en[u]) : make_float4(1e30f, 1e30f, 1e30f, 0.f);
 #pragma unroll
-    for (int u = 0; u < kTail; u++) pair(en[u], l[u]);
+    for (int u = 0; u < kTail; u++) offset(en[u], l[u]);
   }
+}
+
+// Mixed form of force_fp64: the sum over the row of slot i of f(r) (q_j - q_i)
+// in float.  KAHAN: the per-particle sums compensated (MDG_MIXED), else plain
+// float (MDG_MIXED_PLAIN).  With PRUNE every entry within the prune radius is
+// copied to the inner row of slot i, as in force_fp64.
+template <bool PRUNE, bool KAHAN, bool EDGE>
+__device__ __forceinline__ double3 pair_loop(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
+                                             const float4 &li, const CellPos &cp, const uint32_t *__restrict__ list,
+                                             const int *__restrict__ counts, int *kept) {
+  int cnt = counts[i];
+  if (!MDG_IN_RANGE(d.flags, kCheckStepRow, cnt, g.list_cap + 1)) cnt = 0;
+  const size_t stride = (size_t)g.stride;
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+  float cx = 0.f, cy = 0.f, cz = 0.f;  // Kahan corrections
+  const float rc2 = g.rc2f, c2x8 = g.c2x8f, thr = g.prune_thr2;
+  int m = 0;
+  walk_row<EDGE, kCheckStepSlot>(g, d, loc, i, li, cp, list, cnt, [&](uint32_t e, float dx, float dy, float dz, float r2) {
+    if (PRUNE && r2 <= thr) d.pl[(size_t)(m++) * stride + i] = e;
+    // evaluated for every entry and masked: no divergent branch per pair
+    float inv;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+    const float i6 = inv * inv * inv;
+    float df = (i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8;
+    df = r2 <= rc2 ? df : 0.0f;
+    if (KAHAN) {
+      // a zero term (a pair beyond rc) leaves s - c unchanged as a real
+      // number (t - s is exact, and so is the new correction), but it moves
+      // the correction into s and the later additions round differently:
+      // lists that differ only by pairs beyond rc give forces that agree to
+      // about one float rounding, not bit for bit
+      kahan_fma(sx, cx, df, dx);
+      kahan_fma(sy, cy, df, dy);
+      kahan_fma(sz, cz, df, dz);
+    } else {
+      sx = fmaf(df, dx, sx);
+      sy = fmaf(df, dy, sy);
+      sz = fmaf(df, dz, sz);
+    }
+  });
   if (PRUNE) *kept = m;
   // the compensated sum rounded once to float (relative 6e-8 of the force),
   // then one conversion per component: GB300 runs double at 1/64 of float
@@ -528,8 +540,34 @@ __global__ void __launch_bounds__(kStepThreads) k_observe(Geom g, Dev d) {
 
 // Mixed-form observers: the same sums with each pair's energy and virial
 // term evaluated in float (from the home-cell-local float positions of q_end,
-// as the mixed force) and every term added in double, per particle and over
-// particles.  The FP64 form keeps k_observe's reference rounding.
+// as the mixed force) and summed over the row in compensated float, walked
+// like the step kernel's row; the rows are added in double.  The FP64 form
+// keeps k_observe's reference rounding.
+template <bool EDGE>
+__device__ __forceinline__ void observe_row(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
+                                            const float4 &li, const CellPos &cp, int cnt, double &pe, double &vir) {
+  const float rc2 = g.rc2f, c2 = (float)g.c2, c0 = (float)g.c0, c2x8 = g.c2x8f;
+  // compensated sums: the error of each row sum stays near one float
+  // rounding of the sum, whatever the row length (GB300 runs double, and
+  // conversions to 64-bit types, at 1/64 of the float rate)
+  float se = 0.f, ce = 0.f, sv = 0.f, cv = 0.f;
+  walk_row<EDGE, kCheckObserve>(g, d, loc, i, li, cp, d.nl, cnt,
+                                [&](uint32_t, float, float, float, float r2) {
+    float inv;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
+    const float i6 = inv * inv * inv;
+    float e_ij = 4.0f * (i6 * i6 - i6 + fmaf(c2, r2, c0));
+    float v_ij = ((i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8) * r2;
+    // masked, not branched; a padding partner's inf / NaN terms drop here
+    e_ij = r2 <= rc2 ? e_ij : 0.0f;
+    v_ij = r2 <= rc2 ? v_ij : 0.0f;
+    kahan_fma(se, ce, e_ij, 1.0f);
+    kahan_fma(sv, cv, v_ij, 1.0f);
+  });
+  pe = 0.5 * (double)(se - ce);
+  vir = 0.5 * (double)(sv - cv);
+}
+
 __global__ void __launch_bounds__(kStepThreads) k_observe_mixed(Geom g, Dev d, const float4 *__restrict__ loc) {
   __shared__ double sh[kStepThreads / 32];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -539,34 +577,11 @@ __global__ void __launch_bounds__(kStepThreads) k_observe_mixed(Geom g, Dev d, c
     ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
     const float4 li = loc[i];
     const CellPos cp = cell_pos_packed(g, li.w);
-    const AxisQuad qx = axis_quad(g.w32[0], g.dl32[0], cp.cx == 0, cp.cx == g.nc[0] - 1, li.x, 1.0f);
-    const AxisQuad qy = axis_quad(g.w32[1], g.dl32[1], cp.cy == 0, cp.cy == g.nc[1] - 1, li.y, 0.25f);
-    const AxisQuad qz = axis_quad(g.w32[2], g.dl32[2], cp.cz == 0, cp.cz == g.nc[2] - 1, li.z, 0.0625f);
-    const float rc2 = g.rc2f, c2 = (float)g.c2, c0 = (float)g.c0, c2x8 = g.c2x8f;
-    double e_sum = 0.0, v_sum = 0.0;
-    const int cnt = d.ncount[i];
-    for (int k = 0; k < cnt; k++) {
-      const uint32_t e = __ldg(d.nl + (size_t)k * g.stride + i);
-      if (!MDG_IN_RANGE(d.flags, kCheckObserve, entry_slot(e), g.n)) continue;
-      const float4 lj = __ldg(loc + entry_slot(e));
-      const float tx = step_float(e, 0x03u, 8388609.0f), ty = step_float(e, 0x0Cu, 8388612.0f),
-                  tz = step_float(e, 0x30u, 8388624.0f);
-      const float dx = lj.x + fmaf(fmaf(qx.b, tx, qx.a), tx, qx.c);
-      const float dy = lj.y + fmaf(fmaf(qy.b, ty, qy.a), ty, qy.c);
-      const float dz = lj.z + fmaf(fmaf(qz.b, tz, qz.a), tz, qz.c);
-      const float r2 = dx * dx + dy * dy + dz * dz;
-      float inv;
-      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv) : "f"(r2));
-      const float i6 = inv * inv * inv;
-      const float e_ij = 4.0f * (i6 * i6 - i6 + fmaf(c2, r2, c0));
-      const float v_ij = ((i6 * inv) * fmaf(-48.0f, i6, 24.0f) + c2x8) * r2;
-      if (r2 <= rc2) {
-        e_sum += (double)e_ij;
-        v_sum += (double)v_ij;
-      }
-    }
-    pe = 0.5 * e_sum;
-    vir = 0.5 * v_sum;
+    int cnt = d.ncount[i];
+    if (!MDG_IN_RANGE(d.flags, kCheckObserve, cnt, g.list_cap + 1)) cnt = 0;
+    // the linear offset for warps with no lane at the periodic boundary
+    if (__all_sync(__activemask(), !cp.edge)) observe_row<false>(g, d, loc, i, li, cp, cnt, pe, vir);
+    else observe_row<true>(g, d, loc, i, li, cp, cnt, pe, vir);
   }
   const double a = block_sum(ke, sh);
   const double b = block_sum(pe, sh);
@@ -606,15 +621,22 @@ __global__ void __launch_bounds__(kStepThreads) k_forces(Geom g, Dev d, const fl
 }
 
 // Float positions of q_end relative to the home-cell centres (k_forces<1> input).
-__global__ void k_loc_from_end(Geom g, Dev d, float4 *loc) {
+// In the mixed form q_mid[par] is already home-cell-local: the step-boundary
+// local position is q_mid - p dt/2, with no box coordinates in between.
+__global__ void k_loc_from_end(Geom g, Dev d, float4 *loc, int par) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n) return;
-  const double4_32a q = d.q_end[i];
   int cx, cy, cz;
   cell_unkey(d.cell[i], cx, cy, cz);
-  loc[i] = make_float4((float)(q.x - ((double)cx + 0.5) * (double)g.w32[0]),
-                         (float)(q.y - ((double)cy + 0.5) * (double)g.w32[1]),
-                         (float)(q.z - ((double)cz + 0.5) * (double)g.w32[2]), cell_pack(cx, cy, cz));
+  if (g.local_pos) {
+    const double4_32a u = d.q_mid[par][i], p = d.p[i];
+    loc[i] = make_float4((float)fma(-p.x, g.dt2, u.x), (float)fma(-p.y, g.dt2, u.y), (float)fma(-p.z, g.dt2, u.z),
+                         cell_pack(cx, cy, cz));
+    return;
+  }
+  const double4_32a q = d.q_end[i];
+  loc[i] = make_float4((float)(q.x - cell_centre(g, 0, cx)), (float)(q.y - cell_centre(g, 1, cy)),
+                       (float)(q.z - cell_centre(g, 2, cz)), cell_pack(cx, cy, cz));
 }
 
 __global__ void k_unsort(Geom g, Dev d, double4_32a *qo, double4_32a *po) {
@@ -700,9 +722,8 @@ void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s) {
 void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s, int mixed, int par) {
   const int grid = blocks_for(g.n);
   if (mixed) {
-    launch_end_from_mid(g, d, par, s);
     // the buffer the next step overwrites before reading it
-    k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
+    k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1], par);
     k_observe_mixed<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
   } else {
     k_observe<<<grid, kStepThreads, 0, s>>>(g, d);
@@ -713,9 +734,8 @@ void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s
 void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s) {
   const int grid = blocks_for(g.n);
   if (mixed) {
-    launch_end_from_mid(g, d, par, s);
     // the buffer the next step overwrites before reading it
-    k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
+    k_loc_from_end<<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1], par);
     if (mixed == MDG_MIXED_PLAIN) k_forces<MDG_MIXED_PLAIN><<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
     else k_forces<MDG_MIXED><<<grid, kStepThreads, 0, s>>>(g, d, d.loc[par ^ 1]);
   } else {
