@@ -670,8 +670,13 @@ __global__ void __launch_bounds__(512, MIXED ? MDG_BATCH_MIN_BLOCKS : 2) k_batch
 // with a plain store of 1; k_batch_finish applies the requests and counts the
 // box's step after the kernel.  The box state the step reads (error, step
 // count, rebuild and re-selection flags) is not written during it.
+// Resident 256-thread CTAs per SM the flat kernel is compiled for: 4 gives
+// 64 registers, where the inner-list variant runs without spills and beats
+// the outer-list walk (1,024 boxes, mixed: 5.18e9 atom-steps/s at 128 x 8
+// with the inner list, against 4.56e9 for the outer list at 48 registers
+// (5 CTAs), where the inner variant lost; 3 CTAs, up to 80 registers: 4.96e9).
 #ifndef MDG_BATCH_FLAT_MIN_BLOCKS
-#define MDG_BATCH_FLAT_MIN_BLOCKS 5
+#define MDG_BATCH_FLAT_MIN_BLOCKS 4
 #endif
 constexpr int kFlatMaxThreads = 256;
 template <int MIXED, int INNER>
