@@ -22,7 +22,15 @@ namespace mdg {
 
 namespace {
 
-constexpr int kListThreads = 128;
+// Threads per block of the list build.  A block's slots are consecutive in
+// cell order, so larger blocks keep more neighbouring cells on one SM and
+// their candidate loads hit L1; at 78 registers two 384-thread blocks fit an
+// SM (forced rebuild of the 4M-atom liquid box: 128 threads 3.70 ms, 256
+// 3.58, 384 3.49, 512 3.81 with one block per SM).
+#ifndef MDG_LIST_THREADS
+#define MDG_LIST_THREADS 384
+#endif
+constexpr int kListThreads = MDG_LIST_THREADS;
 #ifndef MDG_LIST_MIN_BLOCKS
 #define MDG_LIST_MIN_BLOCKS 1
 #endif
@@ -160,9 +168,10 @@ __global__ void k_list_prepare(DevFlags *f) {
 void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s, bool in_step) {
   k_list_prepare<<<1, 1, 0, s>>>(d.flags);
   // one slot per thread: the blocks' work is uneven (denser regions have more
-  // candidates), and many small blocks balance it where a grid of 16 blocks
-  // per SM striding over the slots did not (forced rebuild of the 4M-atom
-  // liquid box: 3.70 against 3.98 ms; one wave of resident blocks: 4.67 ms)
+  // candidates), and many blocks balance it where a grid of 16 blocks per SM
+  // striding over the slots did not (128-thread blocks, forced rebuild of the
+  // 4M-atom liquid box: 3.70 against 3.98 ms; one wave of resident blocks:
+  // 4.67 ms)
   (void)num_sms;
   const int grid = (g.n + kListThreads - 1) / kListThreads;
   k_build_list<<<grid > 0 ? grid : 1, kListThreads, 0, s>>>(g, d);
