@@ -20,7 +20,7 @@ value     mixed-form atom-steps/s over K steps (pair force in f32, per-atom
 e2e       the same through the public C ABI from host memory: pinned host state
           uploaded with mdg_set_state, K calls of mdg_calculate(1), mdg_observe
           every 100 steps (as Benchmark::Run observes), state read back with
-          mdg_get_state; wall clock, the median of three such windows.
+          mdg_get_state; wall clock, the median of seven such windows.
 roofline  the fused step kernel (mixed) over the same K steps: its mean launch
           time from the window's event nodes; achieved = DRAM bytes per launch
           (an ncu capture of the same kernel, per atom, scaled by the atoms and
@@ -53,7 +53,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LJ atom-steps/s, 4M atoms: mixed vs FP64 on 1 GB300 @ rel force err<=1e-5"
 UNIT = "atom-steps/s"
-E2E_WINDOWS = 3
+E2E_WINDOWS = 7
 RC, MARGIN, DT, TEMP, DENSITY = 2.5, 0.5, 0.001, 1.0, 0.5
 
 

@@ -37,7 +37,28 @@ namespace mdg {
 
 namespace {
 
-constexpr int kStepThreads = 128;
+constexpr int kStepThreads = 128;  // observers, forces, state exchange
+// Threads per block of the mixed-form step kernel: 128 for the ordinary
+// variant, 384 for the re-selecting one, which walks the outer rows and
+// writes the inner rows of consecutive slots (4M atoms, mean step kernel of
+// a 20-step window 5 steps after a fresh list / of 400 steps with their
+// rebuilds and re-selections, in ms: ordinary/re-selecting 128/128 0.4314 /
+// 0.4473; 128/128 at 80 registers for the re-selecting variant 0.4278 /
+// 0.4445; 384/384 0.4202 / 0.4322; 256/384 0.4150 / 0.4275; 128/512 0.4132 /
+// 0.4261; 128/384 0.4119 / 0.4238).  The FP64 form (FP64-pipe bound) keeps
+// 128 for both: 5.795 against 5.831 ms at 384.
+#ifndef MDG_STEP_THREADS_MIXED
+#define MDG_STEP_THREADS_MIXED 128
+#endif
+#ifndef MDG_PRUNE_THREADS_MIXED
+#define MDG_PRUNE_THREADS_MIXED 384
+#endif
+// (Nose-Hoover: one size for both variants, whose block sums k_nh_update adds)
+template <int THERMO, int MIXED, int PMODE>
+__host__ __device__ constexpr int step_threads() {
+  return !MIXED ? kStepThreads
+                : (PMODE == 1 || THERMO == MDG_NOSEHOOVER ? MDG_STEP_THREADS_MIXED : MDG_PRUNE_THREADS_MIXED);
+}
 // Resident blocks per SM requested for the ordinary step variant (the
 // register budget follows: 65536 / (blocks * 128) per thread).  The kernel
 // waits on gathers, so occupancy pays: 12 blocks (40 registers, 48 warps per
@@ -345,9 +366,11 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // 1 = ordinary step only, 2 = re-selecting step only (each a no-op when the
 // flag says otherwise, so the graph path can run the lighter variant).
 template <int THERMO, int COMPAT, int MIXED, int PMODE>
-__global__ void __launch_bounds__(kStepThreads, PMODE != 1          ? MDG_PRUNE_MIN_BLOCKS
-                                                : MIXED == MDG_MIXED ? MDG_STEP_MIN_BLOCKS_KAHAN
-                                                                     : MDG_STEP_MIN_BLOCKS)
+// The resident-block counts of the launch bounds are for 128-thread blocks.
+__global__ void __launch_bounds__(step_threads<THERMO, MIXED, PMODE>(), (PMODE != 1          ? MDG_PRUNE_MIN_BLOCKS
+                                                         : MIXED == MDG_MIXED ? MDG_STEP_MIN_BLOCKS_KAHAN
+                                                                              : MDG_STEP_MIN_BLOCKS) *
+                                                            128 / step_threads<THERMO, MIXED, PMODE>())
     k_step(Geom g, Dev d, int par) {
   const DevFlags *f = d.flags;
   if (f->halt != 0) return;
@@ -453,7 +476,7 @@ __global__ void __launch_bounds__(kStepThreads, PMODE != 1          ? MDG_PRUNE_
   }
   if (MIXED && i == 0) d.flags->end_stale = 1;
   if (THERMO == MDG_NOSEHOOVER) {
-    __shared__ double sh[kStepThreads / 32];
+    __shared__ double sh[step_threads<THERMO, MIXED, PMODE>() / 32];
     const double t = block_sum(ke, sh);
     if (threadIdx.x == 0) d.partials[blockIdx.x] = t;
   }
@@ -684,11 +707,14 @@ inline int blocks_for(int n) { return n > 0 ? (n + kStepThreads - 1) / kStepThre
 
 template <int T, int C, int M>
 void launch_step_variant(const Geom &g, const Dev &d, int par, int pmode, cudaStream_t s) {
-  const int grid = blocks_for(g.n);
-  if (pmode == 0) k_step<T, C, M, 0><<<grid, kStepThreads, 0, s>>>(g, d, par);
-  if (pmode == 1 || pmode == 3) k_step<T, C, M, 1><<<grid, kStepThreads, 0, s>>>(g, d, par);
-  if (pmode == 2 || pmode == 3) k_step<T, C, M, 2><<<grid, kStepThreads, 0, s>>>(g, d, par);
-  if (T == MDG_NOSEHOOVER) k_nh_update<<<1, 1024, 0, s>>>(g, d, grid, 0);
+  constexpr int t0 = step_threads<T, M, 0>(), t1 = step_threads<T, M, 1>(), t2 = step_threads<T, M, 2>();
+  auto grid = [&](int threads) { return g.n > 0 ? (g.n + threads - 1) / threads : 1; };
+  if (pmode == 0) k_step<T, C, M, 0><<<grid(t0), t0, 0, s>>>(g, d, par);
+  if (pmode == 1 || pmode == 3) k_step<T, C, M, 1><<<grid(t1), t1, 0, s>>>(g, d, par);
+  if (pmode == 2 || pmode == 3) k_step<T, C, M, 2><<<grid(t2), t2, 0, s>>>(g, d, par);
+  // the Nose-Hoover block sums of this step: one per block of the variant that ran
+  static_assert(T != MDG_NOSEHOOVER || (t0 == t1 && t1 == t2), "one partial-sum count for every variant");
+  if (T == MDG_NOSEHOOVER) k_nh_update<<<1, 1024, 0, s>>>(g, d, grid(t1), 0);
 }
 
 template <int T, int C>
