@@ -314,14 +314,15 @@ int add_event(mdg_handle *h, cudaGraph_t g, cudaGraphNode_t dep, cudaEvent_t ev,
 }
 
 // A graph of nsteps steps starting at parity par.  Per step: a one-thread
-// prelude (counters, inner-list hand-over) that sets the rebuild condition;
-// IF(rebuild) { wrap, bin, reorder, build }; a one-thread select that sets
-// the variant; SWITCH(variant) { ordinary step | re-selecting step }.  Steps
-// without a rebuild therefore run three kernels.  With `ev` (3 nsteps + 1
-// events) the graph starts by recording ev[3 nsteps], and step k records
-// ev[3k] after its prelude, ev[3k+1] before its step kernel and ev[3k+2]
-// after it, so the device time of each phase of each step is read from the
-// same replay.
+// prelude (counters, inner-list hand-over) that sets the step's conditions,
+// then one SWITCH { ordinary step | re-selecting step | rebuild (wrap, bin,
+// reorder, build) and re-selecting step }: a step without a rebuild runs two
+// kernels.  With `ev` (3 nsteps + 1 events, the timed graphs) the rebuild
+// and the step are separate nodes, IF(rebuild) then SWITCH(variant), since
+// event records cannot sit inside a conditional body: the graph starts by
+// recording ev[3 nsteps], and step k records ev[3k] after its prelude,
+// ev[3k+1] before its step kernel and ev[3k+2] after it, so the device time
+// of each phase of each step is read from the same replay.
 int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps, cudaEvent_t *ev = nullptr) {
   cudaGraph_t g = nullptr;
   MDG_CK(cudaGraphCreate(&g, 0));
@@ -334,29 +335,46 @@ int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps, cudaEvent_
   const int lang = lang_on(h) != 0;
   for (int k = 0; k < nsteps && rc == MDG_OK; k++) {
     const int p = par ^ (k & 1);
-    cudaGraphConditionalHandle c_rb = 0, c_var = 0;
-    cudaError_t e = cudaGraphConditionalHandleCreate(&c_rb, g, 0, cudaGraphCondAssignDefault);
-    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&c_var, g, 2, cudaGraphCondAssignDefault);
-    if (e != cudaSuccess) {
-      rc = fail(h, MDG_ERR_CUDA, std::string("cudaGraphConditionalHandleCreate: ") + cudaGetErrorString(e));
-      break;
-    }
-    cudaGraphNode_t pre = nullptr, cond = nullptr, sel = nullptr, sw = nullptr;
-    rc = append_captured(h, g, last ? &last : nullptr, [&] { mdg::launch_prelude(h->d, lang, c_rb, h->stream); }, &pre);
-    if (rc == MDG_OK && ev) rc = add_event(h, g, pre, ev[3 * k], &pre);
-    if (rc) break;
-    rc = add_conditional(h, g, pre, c_rb, cudaGraphCondTypeIf, 1, [&](int) {
-      mdg::launch_rebuild(h->g, h->d, p, h->num_sms, h->stream, false, false, true);
-    }, &cond);
-    if (rc) break;
-    rc = append_captured(h, g, &cond, [&] { mdg::launch_select(h->d, c_var, h->stream); }, &sel);
-    if (rc == MDG_OK && ev) rc = add_event(h, g, sel, ev[3 * k + 1], &sel);
-    if (rc) break;
-    rc = add_conditional(h, g, sel, c_var, cudaGraphCondTypeSwitch, 2, [&](int variant) {
+    auto step_kernel = [&](int pmode) {
       mdg::launch_step(h->g, h->d, p, h->prm.thermostat, h->prm.langevin_half_drift_compat, h->prm.precision,
-                       h->stream, variant == 0 ? 1 : 2);
-    }, &sw);
-    if (rc == MDG_OK && ev) rc = add_event(h, g, sw, ev[3 * k + 2], &sw);
+                       h->stream, pmode);
+    };
+    auto rebuild = [&] { mdg::launch_rebuild(h->g, h->d, p, h->num_sms, h->stream, false, false, true); };
+    cudaGraphNode_t pre = nullptr, sw = nullptr;
+    if (ev) {
+      cudaGraphConditionalHandle c_rb = 0, c_var = 0;
+      cudaError_t e = cudaGraphConditionalHandleCreate(&c_rb, g, 0, cudaGraphCondAssignDefault);
+      if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&c_var, g, 2, cudaGraphCondAssignDefault);
+      if (e != cudaSuccess) {
+        rc = fail(h, MDG_ERR_CUDA, std::string("cudaGraphConditionalHandleCreate: ") + cudaGetErrorString(e));
+        break;
+      }
+      cudaGraphNode_t cond = nullptr;
+      rc = append_captured(h, g, last ? &last : nullptr,
+                           [&] { mdg::launch_prelude_split(h->d, lang, c_rb, c_var, h->stream); }, &pre);
+      if (rc == MDG_OK) rc = add_event(h, g, pre, ev[3 * k], &pre);
+      if (rc == MDG_OK) rc = add_conditional(h, g, pre, c_rb, cudaGraphCondTypeIf, 1, [&](int) { rebuild(); }, &cond);
+      if (rc == MDG_OK) rc = add_event(h, g, cond, ev[3 * k + 1], &cond);
+      if (rc == MDG_OK)
+        rc = add_conditional(h, g, cond, c_var, cudaGraphCondTypeSwitch, 2,
+                             [&](int variant) { step_kernel(variant == 0 ? 1 : 2); }, &sw);
+      if (rc == MDG_OK) rc = add_event(h, g, sw, ev[3 * k + 2], &sw);
+    } else {
+      cudaGraphConditionalHandle c_step = 0;
+      cudaError_t e = cudaGraphConditionalHandleCreate(&c_step, g, 3, cudaGraphCondAssignDefault);
+      if (e != cudaSuccess) {
+        rc = fail(h, MDG_ERR_CUDA, std::string("cudaGraphConditionalHandleCreate: ") + cudaGetErrorString(e));
+        break;
+      }
+      rc = append_captured(h, g, last ? &last : nullptr, [&] { mdg::launch_prelude(h->d, lang, c_step, h->stream); },
+                           &pre);
+      if (rc == MDG_OK)
+        rc = add_conditional(h, g, pre, c_step, cudaGraphCondTypeSwitch, 3, [&](int body) {
+          if (body == 2) rebuild();
+          step_kernel(body == 0 ? 1 : 2);
+        }, &sw);
+    }
+    if (rc) break;
     last = sw;
   }
   if (rc == MDG_OK) {
@@ -421,8 +439,8 @@ int settle(mdg_handle *h) {
     int rc = read_flags(h);
     if (rc) return rc;
     long long completed = (long long)(h->hflags->steps - before);
-    if (h->prm.use_graphs)  // executed kernels: prelude, select, step (+ NH), and the rebuild bodies that ran
-      h->launches += completed * (2 + mdg::step_kernels(h->prm.thermostat)) +
+    if (h->prm.use_graphs)  // executed kernels: prelude, step (+ NH), and the rebuild bodies that ran
+      h->launches += completed * (1 + mdg::step_kernels(h->prm.thermostat)) +
                      (long long)(h->hflags->rebuilds - rebuilds0) * mdg::kRebuildKernels;
     if (h->hflags->halt == 0) {
       done += completed;
@@ -740,7 +758,7 @@ int timed_graph_run(mdg_handle *h, int32_t nsteps, double *step_ms, double *rebu
     status = read_flags(h);
     if (status) break;
     const long long completed = (long long)(h->hflags->steps - before);
-    h->launches += completed * (2 + mdg::step_kernels(h->prm.thermostat)) +
+    h->launches += completed * (1 + mdg::step_kernels(h->prm.thermostat)) +
                    (long long)(h->hflags->rebuilds - rebuilds0) * mdg::kRebuildKernels;
     // a halted step and those behind it ran as no-ops: only the steps that
     // completed are timed

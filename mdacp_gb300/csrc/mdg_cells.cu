@@ -266,15 +266,26 @@ __global__ void k_set_rebuild(DevFlags *f) {
   if (f->halt == 0) f->rebuild = 1;
 }
 
-// Graph path: the step-start bookkeeping of k_wrap_bin, and the condition that
-// runs the rebuild body.
-__global__ void k_prelude(DevFlags *f, int lang_step, cudaGraphConditionalHandle rebuild_cond) {
+// Graph path: the step-start bookkeeping of k_wrap_bin and the conditions of
+// the step's nodes, all decided before the rebuild: a rebuild inside a step
+// always re-selects the inner list (k_rebuild_done), and after a halt every
+// later kernel is a no-op.  Two forms:
+//   rebuild_cond (IF: run the rebuild body) and variant_cond (SWITCH: 0 the
+//   ordinary step, 1 the re-selecting one, 2 none), for the timed graphs,
+//   which record events between the nodes;
+//   step_cond alone (SWITCH: 0 ordinary, 1 re-selecting, 2 rebuild then
+//   re-selecting, 3 none), one conditional node per step.
+__global__ void k_prelude(DevFlags *f, int lang_step, cudaGraphConditionalHandle rebuild_cond,
+                          cudaGraphConditionalHandle variant_cond, cudaGraphConditionalHandle step_cond, int split) {
   if (f->halt == 0) start_step(f, lang_step);
-  cudaGraphSetConditional(rebuild_cond, (f->halt == 0 && f->rebuild) ? 1u : 0u);
-}
-
-__global__ void k_select(DevFlags *f, cudaGraphConditionalHandle variant_cond) {
-  cudaGraphSetConditional(variant_cond, f->halt != 0 ? 2u : (f->prune_now ? 1u : 0u));
+  const bool run = f->halt == 0, rebuild = run && f->rebuild != 0;
+  const unsigned variant = !run ? 2u : ((rebuild || f->prune_now) ? 1u : 0u);
+  if (split) {
+    cudaGraphSetConditional(rebuild_cond, rebuild ? 1u : 0u);
+    cudaGraphSetConditional(variant_cond, variant);
+  } else {
+    cudaGraphSetConditional(step_cond, !run ? 3u : (rebuild ? 2u : variant));
+  }
 }
 
 }  // namespace
@@ -292,12 +303,13 @@ void launch_end_from_mid(const Geom &g, const Dev &d, int par, cudaStream_t s) {
   k_end_current<<<1, 1, 0, s>>>(d.flags);
 }
 
-void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle rebuild_cond, cudaStream_t s) {
-  k_prelude<<<1, 1, 0, s>>>(d.flags, lang_step, rebuild_cond);
+void launch_prelude_split(const Dev &d, int lang_step, cudaGraphConditionalHandle rebuild_cond,
+                          cudaGraphConditionalHandle variant_cond, cudaStream_t s) {
+  k_prelude<<<1, 1, 0, s>>>(d.flags, lang_step, rebuild_cond, variant_cond, 0, 1);
 }
 
-void launch_select(const Dev &d, cudaGraphConditionalHandle variant_cond, cudaStream_t s) {
-  k_select<<<1, 1, 0, s>>>(d.flags, variant_cond);
+void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle step_cond, cudaStream_t s) {
+  k_prelude<<<1, 1, 0, s>>>(d.flags, lang_step, 0, 0, step_cond, 0);
 }
 
 void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cudaStream_t s, bool count_step,

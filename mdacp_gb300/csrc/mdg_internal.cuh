@@ -141,11 +141,14 @@ void launch_rebuild(const Geom &g, const Dev &d, int q_mid_dst, int num_sms, cud
                     bool lang_step, bool in_step);
 void launch_step(const Geom &g, const Dev &d, int par, int thermostat, int compat, int mixed, cudaStream_t s,
                  int pmode);
-// Graph path: step start (counters, hand-over) and the rebuild condition, then
-// the choice of step variant after the rebuild (0 ordinary, 1 re-selecting,
-// 2 none when halted).
-void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle rebuild_cond, cudaStream_t s);
-void launch_select(const Dev &d, cudaGraphConditionalHandle variant_cond, cudaStream_t s);
+// Graph path: step start (counters, hand-over) and the conditions of the
+// step's nodes.  Split form (timed graphs): the rebuild condition (IF) and
+// the step variant (SWITCH: 0 ordinary, 1 re-selecting, 2 none when halted).
+// One-node form: SWITCH 0 ordinary, 1 re-selecting, 2 rebuild then
+// re-selecting, 3 none.
+void launch_prelude_split(const Dev &d, int lang_step, cudaGraphConditionalHandle rebuild_cond,
+                          cudaGraphConditionalHandle variant_cond, cudaStream_t s);
+void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle step_cond, cudaStream_t s);
 void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s);
 void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s, int mixed, int par);
 void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s);
