@@ -172,6 +172,23 @@ int setup_geometry(mdg_handle *h) {
   g.hb_d = std::sqrt(2.0 * p.gamma * p.temperature / p.dt);
   g.seed = p.seed;
   g.local_pos = p.precision != MDG_FP64 ? 1 : 0;
+  // packed reference positions of the mixed form: a packed coordinate is off
+  // by at most half a unit plus float rounding, so each displacement
+  // threshold is lowered by two units (about 6e-6 at w = 3)
+  double unit_max = 0.0;
+  for (int k = 0; k < 3; k++) {
+    g.ref_scale[k] = (float)(1048575.0 / (double)g.w32[k]);
+    g.ref_unit[k] = (float)((double)g.w32[k] / 1048575.0);
+    unit_max = std::fmax(unit_max, (double)g.ref_unit[k]);
+  }
+  const double hm = 0.5 * p.margin - 2.0 * unit_max;
+  g.half_margin2_ref = (float)(hm > 0.0 ? hm * hm : 0.0);
+  if (buffer > 0.0) {
+    const double hp = 0.5 * buffer - 2.0 * unit_max;
+    g.half_prune2_ref = (float)(hp > 0.0 ? hp * hp * (1.0 - 1e-4) : 0.0);
+  } else {
+    g.half_prune2_ref = 3.0e38f;
+  }
   return MDG_OK;
 }
 

@@ -221,27 +221,35 @@ __global__ void k_finalize(Geom g, Dev d, int q_mid_dst) {
   // k_wrap_bin, the only reader of end_stale in the rebuild, has finished
   if (blockIdx.x == 0 && threadIdx.x == 0) d.flags->end_stale = 0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.n; k += gridDim.x * blockDim.x) {
-    const double4_32a q = d.t_q[k], p = d.t_p[k];
+    const double4_32a q = d.t_q[k];
+    double4_32a p = d.t_p[k];
     const int id = d.t_id[k], c = d.t_cell[k];
     d.q_end[k] = q;
-    d.p[k] = p;
     d.id[k] = id;
     d.cell[k] = c;
     d.inv[id] = k;
-    d.q_build[k] = q;
     int cx, cy, cz;
     cell_unkey(c, cx, cy, cz);
     const float cw = __int_as_float(c);
     const double ox = cell_centre(g, 0, cx), oy = cell_centre(g, 1, cy), oz = cell_centre(g, 2, cz);
-    d.qf[k] = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), cw);
+    const float4 lb = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), cw);
+    d.qf[k] = lb;
     double4_32a m = q;
     if (g.local_pos) {
       m.x = __dadd_rn(q.x - ox, __dmul_rn(p.x, g.dt2));
       m.y = __dadd_rn(q.y - oy, __dmul_rn(p.y, g.dt2));
       m.z = __dadd_rn(q.z - oz, __dmul_rn(p.z, g.dt2));
+      // the build reference (for the rebuild test) in q_mid's padding word, and
+      // the same position as the prune reference in p's until the step's
+      // re-selection records its own
+      m.w = pack_ref(g, lb.x, lb.y, lb.z);
+      p.w = m.w;
       q_mid[k] = m;
+      d.p[k] = p;
       d.loc[q_mid_dst][k] = make_float4((float)m.x, (float)m.y, (float)m.z, cw);
     } else {
+      d.p[k] = p;
+      d.q_build[k] = q;
       m.x = __dadd_rn(q.x, __dmul_rn(p.x, g.dt2));
       m.y = __dadd_rn(q.y, __dmul_rn(p.y, g.dt2));
       m.z = __dadd_rn(q.z, __dmul_rn(p.z, g.dt2));

@@ -103,7 +103,31 @@ struct Geom {
   // mixed form: q_mid holds positions relative to the centre of the slot's
   // home cell at the last build, and the step kernels do not write q_end
   int local_pos;
+  // mixed form: the build and prune reference positions (home-cell-local)
+  // travel in the padding words q_mid.w and p.w as 21-bit fixed point per
+  // axis, ref_unit = w / (2^20 - 1) apart (|position| < w holds for both);
+  // the displacement tests compare against thresholds lowered by twice the
+  // largest rounding of a packed position
+  float ref_scale[3], ref_unit[3];
+  float half_margin2_ref, half_prune2_ref;
 };
+
+// Home-cell-local position (|x| < w per axis) packed into the bits of a
+// double: 21-bit two's complement fields at bits 0, 21, 42.  The value is
+// only ever moved, never used in arithmetic.
+__device__ __forceinline__ double pack_ref(const Geom &g, float x, float y, float z) {
+  const long long a = (long long)__float2int_rn(x * g.ref_scale[0]) & 0x1FFFFF;
+  const long long b = (long long)__float2int_rn(y * g.ref_scale[1]) & 0x1FFFFF;
+  const long long c = (long long)__float2int_rn(z * g.ref_scale[2]) & 0x1FFFFF;
+  return __longlong_as_double(a | (b << 21) | (c << 42));
+}
+
+__device__ __forceinline__ void unpack_ref(const Geom &g, double v, float &x, float &y, float &z) {
+  const long long u = __double_as_longlong(v);
+  x = (float)(int)((u << 43) >> 43) * g.ref_unit[0];
+  y = (float)(int)((u << 22) >> 43) * g.ref_unit[1];
+  z = (float)(int)((u << 1) >> 43) * g.ref_unit[2];
+}
 
 // Centre of home cell (cx, cy, cz) in double, exact: (c + 1/2) w32 has at
 // most 36 significant bits.

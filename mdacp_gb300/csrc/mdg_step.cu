@@ -66,10 +66,11 @@ __host__ __device__ constexpr int step_threads() {
 #ifndef MDG_STEP_MIN_BLOCKS
 #define MDG_STEP_MIN_BLOCKS 12
 #endif
-// The same for the compensated mixed form.  Its three correction terms do
-// not fit in 40 registers (48 bytes of spills at 12 blocks), but 12 blocks
-// with the spills measured 6 % faster than 10 blocks at 48 registers without
-// them (4M atoms, 400 steps: 0.472 against 0.501 ms per step kernel).
+// The same for the compensated mixed form.  Its three correction terms fit
+// in 40 registers since the build reference is no longer held across the
+// pair loop (it travels packed in q_mid.w); before, 12 blocks with a 48-byte
+// spill still measured 6 % faster than 10 blocks at 48 registers without it
+// (4M atoms, 400 steps: 0.472 against 0.501 ms per step kernel).
 #ifndef MDG_STEP_MIN_BLOCKS_KAHAN
 #define MDG_STEP_MIN_BLOCKS_KAHAN 12
 #endif
@@ -110,7 +111,8 @@ __device__ __forceinline__ CellPos cell_pos(const Geom &g, int key) {
   return r;
 }
 
-// The same from the coordinates packed in the w word of qf / loc.
+// The same from the coordinates packed in the w word of qf / loc (equal
+// between the two: both are written with the home cell of the last build).
 __device__ __forceinline__ CellPos cell_pos_packed(const Geom &g, float w) {
   CellPos r;
   cell_unpack(w, r.cx, r.cy, r.cz);
@@ -318,9 +320,8 @@ __device__ __forceinline__ double3 pair_loop(const Geom &g, const Dev &d, const 
 // needs six fewer and runs without the other's spills.
 template <bool PRUNE, bool KAHAN>
 __device__ __forceinline__ double3 force_mixed(const Geom &g, const Dev &d, const float4 *__restrict__ loc, int i,
-                                               const CellPos &cp, const uint32_t *__restrict__ list,
+                                               const float4 &li, const CellPos &cp, const uint32_t *__restrict__ list,
                                                const int *__restrict__ counts, int *kept) {
-  const float4 li = loc[i];
   if (__all_sync(__activemask(), !cp.edge)) return pair_loop<PRUNE, KAHAN, false>(g, d, loc, i, li, cp, list, counts, kept);
   return pair_loop<PRUNE, KAHAN, true>(g, d, loc, i, li, cp, list, counts, kept);
 }
@@ -385,22 +386,26 @@ __global__ void __launch_bounds__(step_threads<THERMO, MIXED, PMODE>(), (PMODE !
   const bool prune = PMODE == 2 ? true : (PMODE == 1 ? false : f->prune_now != 0);
   int kept = 0;
   if (active) {
-    // build-time local position; its w word holds the home-cell coordinates
-    const float4 lb = d.qf[i];
+    // mixed: this force evaluation's local position (partners gather the
+    // same array); FP64: the build-time local position.  The w word of
+    // either holds the home-cell coordinates
+    const float4 lb = MIXED ? d.loc[par][i] : d.qf[i];
     const CellPos cp = cell_pos_packed(g, lb.w);
     double3 F;
     if (prune)
-      F = MIXED ? force_mixed<true, MIXED == MDG_MIXED>(g, d, d.loc[par], i, cp, d.nl, d.ncount, &kept)
+      F = MIXED ? force_mixed<true, MIXED == MDG_MIXED>(g, d, d.loc[par], i, lb, cp, d.nl, d.ncount, &kept)
                 : force_fp64<true>(g, d, qm, i, cp, d.nl, d.ncount, &kept);
     else
-      F = MIXED ? force_mixed<false, MIXED == MDG_MIXED>(g, d, d.loc[par], i, cp, d.pl, d.pcount, nullptr)
+      F = MIXED ? force_mixed<false, MIXED == MDG_MIXED>(g, d, d.loc[par], i, lb, cp, d.pl, d.pcount, nullptr)
                 : force_fp64<false>(g, d, qm, i, cp, d.pl, d.pcount, nullptr);
+    // the w words are padding (zero in the FP64 form, packed reference
+    // positions in the mixed form): never scaled, never in the kinetic energy
     double4_32a p = d.p[i];
     if (THERMO == MDG_NOSEHOOVER) {
       const double e1 = f->exp1;
-      p.x *= e1; p.y *= e1; p.z *= e1; p.w *= e1;
+      p.x *= e1; p.y *= e1; p.z *= e1;
       p.x += F.x * g.dt; p.y += F.y * g.dt; p.z += F.z * g.dt;
-      p.x *= e1; p.y *= e1; p.z *= e1; p.w *= e1;
+      p.x *= e1; p.y *= e1; p.z *= e1;
     } else {
       p.x += F.x * g.dt; p.y += F.y * g.dt; p.z += F.z * g.dt;
     }
@@ -438,10 +443,12 @@ __global__ void __launch_bounds__(step_threads<THERMO, MIXED, PMODE>(), (PMODE !
     if (MIXED) {
       // positions relative to the home-cell centre: the new local position is
       // one conversion, and the displacement since the build is measured in
-      // float against the build's local position (qf)
+      // float against the build's local position, packed in q_mid.w
       ln = make_float4((float)q1.x, (float)q1.y, (float)q1.z, lb.w);
-      const float fx = ln.x - lb.x, fy = ln.y - lb.y, fz = ln.z - lb.z;
-      if (fx * fx + fy * fy + fz * fz > (float)g.half_margin2 || !(fx == fx && fy == fy && fz == fz))
+      float bx, by, bz;
+      unpack_ref(g, q0.w, bx, by, bz);
+      const float fx = ln.x - bx, fy = ln.y - by, fz = ln.z - bz;
+      if (fx * fx + fy * fy + fz * fz > g.half_margin2_ref || !(fx == fx && fy == fy && fz == fz))
         d.flags->rebuild = 1;
     } else {
       const double4_32a qb = d.q_build[i];
@@ -456,23 +463,26 @@ __global__ void __launch_bounds__(step_threads<THERMO, MIXED, PMODE>(), (PMODE !
     d.loc[par ^ 1][i] = ln;
     // prune reference: the positions of this force evaluation when the
     // inner list was re-selected now, else those of the last selection
+    // (mixed: packed in p.w)
     float4 lp;
     if (prune) {
-      lp = d.loc[par][i];
-      d.loc_p[i] = lp;
+      lp = MIXED ? lb : d.loc[par][i];
+      if (MIXED) p.w = pack_ref(g, lp.x, lp.y, lp.z);
+      else d.loc_p[i] = lp;
       d.pcount[i] = kept;
+    } else if (MIXED) {
+      unpack_ref(g, p.w, lp.x, lp.y, lp.z);
     } else {
       lp = d.loc_p[i];
     }
     const float vx = ln.x - lp.x, vy = ln.y - lp.y, vz = ln.z - lp.z;
-    if (vx * vx + vy * vy + vz * vz > g.half_prune2) d.flags->prune_next = 1;
+    if (vx * vx + vy * vy + vz * vz > (MIXED ? g.half_prune2_ref : g.half_prune2)) d.flags->prune_next = 1;
     d.p[i] = p;
     // the mixed form leaves q_end behind: q_mid - p dt/2 gives it back when a
     // rebuild or a reader needs it (32 bytes a particle fewer per step)
     if (!MIXED) d.q_end[i] = qe;
     qn[i] = q1;
-    if (THERMO == MDG_NOSEHOOVER)
-      ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+    if (THERMO == MDG_NOSEHOOVER) ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z;
   }
   if (MIXED && i == 0) d.flags->end_stale = 1;
   if (THERMO == MDG_NOSEHOOVER) {
@@ -515,7 +525,7 @@ __global__ void __launch_bounds__(kStepThreads) k_kinetic(Geom g, Dev d) {
   double ke = 0.0;
   if (i < g.n) {
     const double4_32a p = d.p[i];
-    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z;
   }
   const double t = block_sum(ke, sh);
   if (threadIdx.x == 0) d.partials[blockIdx.x] = t;
@@ -531,7 +541,7 @@ __global__ void __launch_bounds__(kStepThreads) k_observe(Geom g, Dev d) {
   double ke = 0.0, pe = 0.0, vir = 0.0;
   if (i < g.n) {
     const double4_32a p = d.p[i];
-    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z;
     const double4_32a qi = d.q_end[i];
     const CellPos cp = cell_pos(g, d.cell[i]);
     const int cnt = d.ncount[i];
@@ -597,7 +607,7 @@ __global__ void __launch_bounds__(kStepThreads) k_observe_mixed(Geom g, Dev d, c
   double ke = 0.0, pe = 0.0, vir = 0.0;
   if (i < g.n) {
     const double4_32a p = d.p[i];
-    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+    ke = 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z;
     const float4 li = loc[i];
     const CellPos cp = cell_pos_packed(g, li.w);
     int cnt = d.ncount[i];
@@ -638,7 +648,7 @@ __global__ void __launch_bounds__(kStepThreads) k_forces(Geom g, Dev d, const fl
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n) return;
   const CellPos cp = cell_pos(g, d.cell[i]);
-  const double3 F = MIXED ? force_mixed<false, MIXED == MDG_MIXED>(g, d, loc, i, cp, d.nl, d.ncount, nullptr)
+  const double3 F = MIXED ? force_mixed<false, MIXED == MDG_MIXED>(g, d, loc, i, loc[i], cp, d.nl, d.ncount, nullptr)
                           : force_fp64<false>(g, d, d.q_end, i, cp, d.nl, d.ncount, nullptr);
   d.io4[d.id[i]] = make_double4_32a(F.x, F.y, F.z, 0.0);
 }
@@ -662,12 +672,22 @@ __global__ void k_loc_from_end(Geom g, Dev d, float4 *loc, int par) {
                        (float)(q.z - cell_centre(g, 2, cz)), cell_pack(cx, cy, cz));
 }
 
+// The caller's arrays in the caller's order; their fourth lane is padding
+// and comes back zero (the mixed form keeps packed reference positions in it).
 __global__ void k_unsort(Geom g, Dev d, double4_32a *qo, double4_32a *po) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.n) return;
   const int id = d.id[i];
-  if (qo) qo[id] = d.q_end[i];
-  if (po) po[id] = d.p[i];
+  if (qo) {
+    double4_32a q = d.q_end[i];
+    q.w = 0.0;
+    qo[id] = q;
+  }
+  if (po) {
+    double4_32a p = d.p[i];
+    p.w = 0.0;
+    po[id] = p;
+  }
 }
 
 __global__ void k_sort_in(Geom g, Dev d, const double4_32a *qi, const double4_32a *pi) {
