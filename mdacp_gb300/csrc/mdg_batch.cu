@@ -70,6 +70,13 @@ struct Params {
   int inner;
   float prune_thr2f, half_prune2;
   double prune_thr2d;
+  // mixed forms: q_mid relative to the centre of the slot's home cell, the
+  // build and prune references packed in the padding words of q_mid and p
+  // (21-bit fixed point per axis in units of w / (2^20 - 1)), q_end not
+  // written by the step; the displacement thresholds lowered by two units of
+  // the largest cell width
+  int local_pos;
+  float half_margin2_ref, half_prune2_ref;
 };
 
 struct Dev {
@@ -86,6 +93,9 @@ struct Dev {
   // the step, applied by k_batch_finish after it
   int *box_req, *box_preq;
   long long *box_steps, *box_rebuilds, *goal;
+  // mixed forms: -1 when the box's q_end is current, else the q_mid slot
+  // (0 or 1) its last step wrote, from which q_end is formed when needed
+  int *box_mid;
   double *partials;  // per box: KE, PE, virial
   const int *box_of_slot;
   // this step's rebuilding boxes in box order and their first atom in the
@@ -110,6 +120,43 @@ __device__ __forceinline__ void cell_xyz(const BoxDesc &b, int c, int &cx, int &
   const int t = c / b.nc[0];
   cy = t % b.nc[1];
   cz = t / b.nc[1];
+}
+
+// Centre of the box's cell c along axis k, exact in double.
+__device__ __forceinline__ double box_cell_centre(const BoxDesc &b, int k, int c) {
+  return ((double)c + 0.5) * (double)b.w32[k];
+}
+
+// Mixed forms: a home-cell-local position (|x| < w per axis) packed into the
+// bits of a double, 21-bit two's complement fields at bits 0, 21, 42; the
+// value is only ever moved, never used in arithmetic.
+__device__ __forceinline__ double pack_box_ref(const BoxDesc &b, float x, float y, float z) {
+  const long long u = (long long)__float2int_rn(x * (1048575.0f / b.w32[0])) & 0x1FFFFF;
+  const long long v = (long long)__float2int_rn(y * (1048575.0f / b.w32[1])) & 0x1FFFFF;
+  const long long w = (long long)__float2int_rn(z * (1048575.0f / b.w32[2])) & 0x1FFFFF;
+  return __longlong_as_double(u | (v << 21) | (w << 42));
+}
+
+__device__ __forceinline__ void unpack_box_ref(const BoxDesc &b, double r, float &x, float &y, float &z) {
+  const long long u = __double_as_longlong(r);
+  x = (float)(int)((u << 43) >> 43) * (b.w32[0] * (1.0f / 1048575.0f));
+  y = (float)(int)((u << 22) >> 43) * (b.w32[1] * (1.0f / 1048575.0f));
+  z = (float)(int)((u << 1) >> 43) * (b.w32[2] * (1.0f / 1048575.0f));
+}
+
+// Mixed forms: the step-boundary position of slot s from its home-cell-local
+// mid-step position in q_mid[mid]: the cell centre plus (q_mid - p dt/2).
+__device__ __forceinline__ double4_32a box_end_from_mid(const Params &P, const Dev &d, const BoxDesc &b, int s,
+                                                        int mid) {
+  const double4_32a u = d.q_mid[mid][s], p = d.p[s];
+  int cx, cy, cz;
+  cell_xyz(b, d.cell[s], cx, cy, cz);
+  double4_32a q = u;
+  q.x = box_cell_centre(b, 0, cx) + fma(-p.x, P.dt2, u.x);
+  q.y = box_cell_centre(b, 1, cy) + fma(-p.y, P.dt2, u.y);
+  q.z = box_cell_centre(b, 2, cz) + fma(-p.z, P.dt2, u.z);
+  q.w = 0.0;
+  return q;
 }
 
 // Exclusive scan over cnt[0..m) in shared memory by the whole CTA; writes the
@@ -166,9 +213,10 @@ __device__ __forceinline__ int rb_find(const Dev &d, int nb, int t) {
 // work of a rebuild spread over the GPU: at 1/64 of the FP32 rate one SM
 // per box would take ~100 us for 8,000 particles): wrap (one +-L per
 // component) and home cell.  A particle outside [-L, 2L) fails its box.
-__device__ void bin_particle(const Dev &d, const BoxDesc &b, int bi, int a) {
+__device__ void bin_particle(const Params &P, const Dev &d, const BoxDesc &b, int bi, int a) {
   const int o = b.atom_off;
-  double4_32a q = d.q_end[o + a];
+  const int mid = d.box_mid[bi];
+  double4_32a q = mid >= 0 ? box_end_from_mid(P, d, b, o + a, mid) : d.q_end[o + a];
   double x[3] = {q.x, q.y, q.z};
   int ci[3];
   bool bad = false;
@@ -228,26 +276,42 @@ __device__ void sort_box(const Dev &d, const BoxDesc &b, int *s_cnt, int *s_star
 
 // Rebuild part 3, one thread per particle of every rebuilding box: the
 // reordered state back in place, with the build-time and mid-step positions.
-__device__ void place_particle(const Params &P, const Dev &d, const BoxDesc &b, int k, int par) {
+// Mixed forms: q_mid relative to the home-cell centre, (q - c) + p dt/2,
+// with the build position packed in q_mid.w (the rebuild test's reference)
+// and in p.w (the prune reference until the step's re-selection records its
+// own); q_end is current until the box steps.
+__device__ void place_particle(const Params &P, const Dev &d, const BoxDesc &b, int bi, int k, int par) {
   const int o = b.atom_off;
-  const double4_32a q = d.t_q[o + k], p = d.t_p[o + k];
+  const double4_32a q = d.t_q[o + k];
+  double4_32a p = d.t_p[o + k];
   const int c = d.t_cell[o + k];
   d.q_end[o + k] = q;
-  d.p[o + k] = p;
   d.id[o + k] = d.t_id[o + k];
   d.cell[o + k] = c;
-  d.q_build[o + k] = q;
+  if (k == 0) d.box_mid[bi] = -1;
   int cx, cy, cz;
   cell_xyz(b, c, cx, cy, cz);
-  const double ox = ((double)cx + 0.5) * (double)b.w32[0], oy = ((double)cy + 0.5) * (double)b.w32[1],
-               oz = ((double)cz + 0.5) * (double)b.w32[2];
-  d.qf[o + k] = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), 0.0f);
+  const double ox = box_cell_centre(b, 0, cx), oy = box_cell_centre(b, 1, cy), oz = box_cell_centre(b, 2, cz);
+  const float4 lb = make_float4((float)(q.x - ox), (float)(q.y - oy), (float)(q.z - oz), 0.0f);
+  d.qf[o + k] = lb;
   double4_32a m = q;
-  m.x = __dadd_rn(q.x, __dmul_rn(p.x, P.dt2));
-  m.y = __dadd_rn(q.y, __dmul_rn(p.y, P.dt2));
-  m.z = __dadd_rn(q.z, __dmul_rn(p.z, P.dt2));
-  d.q_mid[par][o + k] = m;
-  d.loc[par][o + k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), 0.0f);
+  if (P.local_pos) {
+    m.x = __dadd_rn(q.x - ox, __dmul_rn(p.x, P.dt2));
+    m.y = __dadd_rn(q.y - oy, __dmul_rn(p.y, P.dt2));
+    m.z = __dadd_rn(q.z - oz, __dmul_rn(p.z, P.dt2));
+    m.w = pack_box_ref(b, lb.x, lb.y, lb.z);
+    p.w = m.w;
+    d.q_mid[par][o + k] = m;
+    d.loc[par][o + k] = make_float4((float)m.x, (float)m.y, (float)m.z, 0.0f);
+  } else {
+    d.q_build[o + k] = q;
+    m.x = __dadd_rn(q.x, __dmul_rn(p.x, P.dt2));
+    m.y = __dadd_rn(q.y, __dmul_rn(p.y, P.dt2));
+    m.z = __dadd_rn(q.z, __dmul_rn(p.z, P.dt2));
+    d.q_mid[par][o + k] = m;
+    d.loc[par][o + k] = make_float4((float)(m.x - ox), (float)(m.y - oy), (float)(m.z - oz), 0.0f);
+  }
+  d.p[o + k] = p;
 }
 
 // Pair-list row of local particle a of box b (the box's cell starts and
@@ -316,13 +380,13 @@ __device__ int build_row(const Params &P, const Dev &d, const BoxDesc &b, int bi
 constexpr int kPrepThreads = MDG_BATCH_PREP_THREADS;
 constexpr int kBatchKernelsPerStep = 6;  // rebuild set, bin, sort, place, list, step (+ finish in the flat layout)
 
-__global__ void __launch_bounds__(128) k_batch_bin(Dev d) {
+__global__ void __launch_bounds__(128) k_batch_bin(Params P, Dev d) {
   const int nb = *d.rb_count;
   if (nb == 0) return;
   const int total = d.rb_start[nb];
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const int k = rb_find(d, nb, t), bi = d.rb_boxes[k];
-    bin_particle(d, d.boxes[bi], bi, t - d.rb_start[k]);
+    bin_particle(P, d, d.boxes[bi], bi, t - d.rb_start[k]);
   }
 }
 
@@ -341,7 +405,7 @@ __global__ void __launch_bounds__(128) k_batch_place(Params P, Dev d, int par) {
   const int total = d.rb_start[nb];
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const int k = rb_find(d, nb, t), bi = d.rb_boxes[k];
-    if (d.box_err[bi] == 0) place_particle(P, d, d.boxes[bi], t - d.rb_start[k], par);
+    if (d.box_err[bi] == 0) place_particle(P, d, d.boxes[bi], bi, t - d.rb_start[k], par);
   }
 }
 
@@ -543,8 +607,9 @@ __device__ __forceinline__ double3 box_force(const Params &P, const Dev &d, cons
 // Kick, both half-drifts, the displacement and inner-list tests and the
 // stores of slot s after its force F (one lane per particle does this).
 template <int MIXED, bool INNER>
-__device__ __forceinline__ void advance_particle(const Params &P, const Dev &d, int s, const double3 &F, int par,
-                                                 bool sel, int kept, bool &rebuild, bool &reselect) {
+__device__ __forceinline__ void advance_particle(const Params &P, const Dev &d, const BoxDesc &b, int s,
+                                                 const double3 &F, int par, bool sel, int kept, bool &rebuild,
+                                                 bool &reselect) {
   const bool inner = INNER;
   double4_32a p = d.p[s];
   p.x += F.x * P.dt;
@@ -552,13 +617,23 @@ __device__ __forceinline__ void advance_particle(const Params &P, const Dev &d, 
   p.z += F.z * P.dt;
   const double4_32a q0 = d.q_mid[par][s];
   double4_32a qe = q0, q1 = q0;
-  if (MIXED) {  // one rounding per half-drift (fused), as the single-box mixed form
+  float4 ln;
+  if (MIXED) {
+    // as the single-box mixed form: one rounding per half-drift (fused) on
+    // home-cell-local positions, the new local position one conversion, the
+    // displacement since the build tested in float against the build
+    // position packed in q_mid.w, q_end left for box_end_from_mid
     qe.x = fma(p.x, P.dt2, q0.x);
     qe.y = fma(p.y, P.dt2, q0.y);
     qe.z = fma(p.z, P.dt2, q0.z);
     q1.x = fma(p.x, P.dt2, qe.x);
     q1.y = fma(p.y, P.dt2, qe.y);
     q1.z = fma(p.z, P.dt2, qe.z);
+    ln = make_float4((float)q1.x, (float)q1.y, (float)q1.z, 0.0f);
+    float bx, by, bz;
+    unpack_box_ref(b, q0.w, bx, by, bz);
+    const float fx = ln.x - bx, fy = ln.y - by, fz = ln.z - bz;
+    if (fx * fx + fy * fy + fz * fz > P.half_margin2_ref || !(fx == fx && fy == fy && fz == fz)) rebuild = true;
   } else {
     qe.x = __dadd_rn(q0.x, __dmul_rn(p.x, P.dt2));
     qe.y = __dadd_rn(q0.y, __dmul_rn(p.y, P.dt2));
@@ -566,36 +641,34 @@ __device__ __forceinline__ void advance_particle(const Params &P, const Dev &d, 
     q1.x = __dadd_rn(qe.x, __dmul_rn(p.x, P.dt2));
     q1.y = __dadd_rn(qe.y, __dmul_rn(p.y, P.dt2));
     q1.z = __dadd_rn(qe.z, __dmul_rn(p.z, P.dt2));
-  }
-  const double4_32a qb = d.q_build[s];
-  const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
-  const float fx = (float)ux, fy = (float)uy, fz = (float)uz;
-  if (MIXED) {
-    if (fx * fx + fy * fy + fz * fz > (float)P.half_margin2 || !(fx == fx && fy == fy && fz == fz))
-      rebuild = true;
-  } else {
+    const double4_32a qb = d.q_build[s];
+    const double ux = q1.x - qb.x, uy = q1.y - qb.y, uz = q1.z - qb.z;
     if (ux * ux + uy * uy + uz * uz > P.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
       rebuild = true;
+    const float4 lb = d.qf[s];
+    ln = make_float4(lb.x + (float)ux, lb.y + (float)uy, lb.z + (float)uz, 0.0f);
   }
-  const float4 lb = d.qf[s];
-  const float4 ln = make_float4(lb.x + fx, lb.y + fy, lb.z + fz, 0.0f);
   d.loc[par ^ 1][s] = ln;
   if (inner) {
     // inner-list reference: this force evaluation's positions when the
-    // rows were re-selected now, else those of the last selection
+    // rows were re-selected now, else those of the last selection (mixed:
+    // packed in p.w)
     float4 lp;
     if (sel) {
       lp = d.loc[par][s];
-      d.loc_p[s] = lp;
+      if (MIXED) p.w = pack_box_ref(b, lp.x, lp.y, lp.z);
+      else d.loc_p[s] = lp;
       d.pcount[s] = kept;
+    } else if (MIXED) {
+      unpack_box_ref(b, p.w, lp.x, lp.y, lp.z);
     } else {
       lp = d.loc_p[s];
     }
     const float vx = ln.x - lp.x, vy = ln.y - lp.y, vz = ln.z - lp.z;
-    if (vx * vx + vy * vy + vz * vz > P.half_prune2) reselect = true;
+    if (vx * vx + vy * vy + vz * vz > (MIXED ? P.half_prune2_ref : P.half_prune2)) reselect = true;
   }
   d.p[s] = p;
-  d.q_end[s] = qe;
+  if (!MIXED) d.q_end[s] = qe;
   d.q_mid[par ^ 1][s] = q1;
 }
 
@@ -648,13 +721,14 @@ __global__ void __launch_bounds__(512, MIXED ? MDG_BATCH_MIN_BLOCKS : 2) k_batch
         F = box_force<MIXED, LPI, 0>(P, d, b, a, lane, par);
       }
       if (lane != 0 || a0 >= n) continue;
-      advance_particle<MIXED, inner>(P, d, o + a, F, par, sel, kept, rebuild, reselect);
+      advance_particle<MIXED, inner>(P, d, b, o + a, F, par, sel, kept, rebuild, reselect);
     }
     const int any = __syncthreads_or(rebuild ? 1 : 0);
     const int anyp = __syncthreads_or(reselect ? 1 : 0);
     if (threadIdx.x == 0) {
       if (any) d.box_rebuild[bi] = 1;
       if (inner) d.box_prune[bi] = anyp;
+      if (MIXED) d.box_mid[bi] = par ^ 1;
       d.box_steps[bi] += 1;
     }
     __syncthreads();
@@ -698,7 +772,7 @@ __global__ void __launch_bounds__(kFlatMaxThreads, MDG_BATCH_FLAT_MIN_BLOCKS) k_
       F = box_force<MIXED, 1, 0>(P, d, b, a, 0, par);
     }
     bool rebuild = false, reselect = false;
-    advance_particle<MIXED, INNER != 0>(P, d, s, F, par, sel, kept, rebuild, reselect);
+    advance_particle<MIXED, INNER != 0>(P, d, b, s, F, par, sel, kept, rebuild, reselect);
     if (rebuild) d.box_req[bi] = 1;
     if (INNER != 0 && reselect) d.box_preq[bi] = 1;
   }
@@ -708,7 +782,7 @@ __global__ void __launch_bounds__(kFlatMaxThreads, MDG_BATCH_FLAT_MIN_BLOCKS) k_
 // the step): the rebuild this step consumed is counted, the requests become
 // the next step's flags, the box's step count advances.
 template <int INNER>
-__global__ void k_batch_finish(Params P, Dev d) {
+__global__ void k_batch_finish(Params P, Dev d, int par) {
   const int bi = blockIdx.x * blockDim.x + threadIdx.x;
   if (bi >= P.nbox) return;
   if (d.box_err[bi] != 0 || d.box_steps[bi] >= *d.goal) return;
@@ -724,6 +798,7 @@ __global__ void k_batch_finish(Params P, Dev d) {
     d.box_prune[bi] = d.box_preq[bi];
     d.box_preq[bi] = 0;
   }
+  if (P.local_pos) d.box_mid[bi] = par ^ 1;
   d.box_steps[bi] += 1;
 }
 
@@ -736,7 +811,7 @@ __global__ void k_batch_observe(Params P, Dev d) {
   double ke = 0.0, pe = 0.0, vir = 0.0;
   for (int a = threadIdx.x; a < n; a += blockDim.x) {
     const double4_32a p = d.p[o + a];
-    ke += 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z + 0.5 * p.w * p.w;
+    ke += 0.5 * p.x * p.x + 0.5 * p.y * p.y + 0.5 * p.z * p.z;  // w is padding
     const double4_32a qi = d.q_end[o + a];
     int cx, cy, cz;
     cell_xyz(b, d.cell[o + a], cx, cy, cz);
@@ -776,13 +851,40 @@ __global__ void k_batch_observe(Params P, Dev d) {
   }
 }
 
+// The caller's arrays in the caller's order; the fourth lane is padding and
+// comes back zero (the mixed forms keep packed reference positions in it).
 __global__ void k_batch_unsort(Dev d, int total, double4_32a *qo, double4_32a *po, const int *box_of_slot) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= total) return;
   const int bi = box_of_slot[s];
   const int dst = d.boxes[bi].atom_off + d.id[s];
-  if (qo) qo[dst] = d.q_end[s];
-  if (po) po[dst] = d.p[s];
+  if (qo) {
+    double4_32a q = d.q_end[s];
+    q.w = 0.0;
+    qo[dst] = q;
+  }
+  if (po) {
+    double4_32a p = d.p[s];
+    p.w = 0.0;
+    po[dst] = p;
+  }
+}
+
+// Mixed forms: q_end of every slot whose box has stepped since it was last
+// current, from that box's q_mid slot; k_batch_end_current then records that
+// every box's q_end is current (a separate kernel, so no thread clears a
+// box's slot while others still read it).
+__global__ void k_batch_end_from_mid(Params P, Dev d, const int *box_of_slot) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= P.total) return;
+  const int bi = box_of_slot[s];
+  const int mid = d.box_mid[bi];
+  if (mid >= 0) d.q_end[s] = box_end_from_mid(P, d, d.boxes[bi], s, mid);
+}
+
+__global__ void k_batch_end_current(Params P, Dev d) {
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bi < P.nbox) d.box_mid[bi] = -1;
 }
 
 }  // namespace batch
@@ -799,6 +901,7 @@ struct mdg_batch {
   int use_inner = 1;  // one lane per particle walks the inner list (when the buffer is > 0)
   int flat = 0;       // 1: the flat layout of the step (k_batch_step_flat + k_batch_finish)
   double buffer = 0.0;  // inner-list buffer in use
+  double ref_unit = 0.0;  // mixed forms: the largest packed-position unit, w / (2^20 - 1), over the boxes
   cudaStream_t stream = nullptr;
   Params P;
   Dev d;
@@ -885,8 +988,19 @@ void set_prune_buffer(mdg_batch *b, double buffer) {
   P.prune_thr2d = rb * rb;
   P.prune_thr2f = (float)(rb * rb + 1e-4);  // float r2 of local positions is within ~1e-5
   P.half_prune2 = (float)(0.25 * buffer * buffer * (1.0 - 1e-4));
+  const double hp = 0.5 * buffer - 2.0 * b->ref_unit;
+  P.half_prune2_ref = buffer > 0.0 ? (float)(hp > 0.0 ? hp * hp * (1.0 - 1e-4) : 0.0) : 3.0e38f;
   b->buffer = buffer;
   drop_batch_graphs(b);  // the graphs hold the parameters by value
+}
+
+// Mixed forms: every box's q_end from its last q_mid (the steps leave it
+// behind), before anything reads q_end from outside a rebuild.
+void make_end_current(mdg_batch *b) {
+  if (!b->P.local_pos) return;
+  k_batch_end_from_mid<<<(b->total + 255) / 256, 256, 0, b->stream>>>(b->P, b->d, b->d_box_of_slot);
+  k_batch_end_current<<<(b->nbox + 255) / 256, 256, 0, b->stream>>>(b->P, b->d);
+  b->launches += 2;
 }
 
 // Longest-first assignment of boxes to grid CTAs (work ~ n * list capacity).
@@ -948,7 +1062,7 @@ void launch_batch_step(mdg_batch *b, int par) {
   const int T = b->threads;
   const int prec = b->prm.precision;
   k_batch_rebuild_set<<<1, 1024, 0, b->stream>>>(b->P, b->d);
-  k_batch_bin<<<b->num_sms * 16, 128, 0, b->stream>>>(b->d);
+  k_batch_bin<<<b->num_sms * 16, 128, 0, b->stream>>>(b->P, b->d);
   k_batch_sort<<<b->nbox, kPrepThreads, 0, b->stream>>>(b->d);
   k_batch_place<<<b->num_sms * 16, 128, 0, b->stream>>>(b->P, b->d, par);
   k_batch_list<<<b->num_sms * 16, 128, 0, b->stream>>>(b->P, b->d);
@@ -961,8 +1075,8 @@ void launch_batch_step(mdg_batch *b, int par) {
     else { if (inner) MDG_FSTEP(MDG_FP64, 1); else MDG_FSTEP(MDG_FP64, 0); }
 #undef MDG_FSTEP
     const int fg = (b->nbox + 255) / 256;
-    if (inner) k_batch_finish<1><<<fg, 256, 0, b->stream>>>(b->P, b->d);
-    else k_batch_finish<0><<<fg, 256, 0, b->stream>>>(b->P, b->d);
+    if (inner) k_batch_finish<1><<<fg, 256, 0, b->stream>>>(b->P, b->d, par);
+    else k_batch_finish<0><<<fg, 256, 0, b->stream>>>(b->P, b->d, par);
     b->launches += kBatchKernelsPerStep + 1;
     return;
   }
@@ -1103,6 +1217,11 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
   P.half_margin2 = 0.25 * p->margin * p->margin;
   P.nbox = nbox;
   P.total = (int)total;
+  P.local_pos = p->precision != MDG_FP64 ? 1 : 0;
+  for (const auto &bx : b->boxes)
+    for (int a = 0; a < 3; a++) b->ref_unit = std::fmax(b->ref_unit, (double)bx.w32[a] / 1048575.0);
+  const double hm = 0.5 * p->margin - 2.0 * b->ref_unit;
+  P.half_margin2_ref = (float)(hm > 0.0 ? hm * hm : 0.0);
   // inner-list buffer: negative = min(0.1, margin / 2), as the single-box
   // form (the autotuner may then pick margin / 2 instead)
   const double buffer = p->prune_buffer < 0.0 ? std::fmin(0.1, 0.5 * p->margin) : p->prune_buffer;
@@ -1141,6 +1260,8 @@ int mdg_batch_create(const mdg_batch_params *p, int32_t nbox, const int32_t *n_p
   if (e == cudaSuccess) e = balloc(&d.box_preq, nbox);
   if (e == cudaSuccess) e = cudaMemset(d.box_req, 0, nbox * sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(d.box_preq, 0, nbox * sizeof(int));
+  if (e == cudaSuccess) e = balloc(&d.box_mid, nbox);
+  if (e == cudaSuccess) e = cudaMemset(d.box_mid, 0xFF, nbox * sizeof(int));  // -1: q_end current
   if (e == cudaSuccess) e = balloc(&d.rb_boxes, nbox);
   if (e == cudaSuccess) e = balloc(&d.rb_start, (size_t)nbox + 1);
   if (e == cudaSuccess) e = balloc(&d.rb_count, 1);
@@ -1179,7 +1300,7 @@ int mdg_batch_destroy(mdg_batch *b) {
                   d.qf, d.loc[0], d.loc[1], d.id, d.cell, d.t_id, d.t_cell, d.order, d.cell_start, d.nl, d.ncount,
                   d.pl, d.pcount, d.loc_p, d.box_prune, d.box_req, d.box_preq, d.rb_boxes, d.rb_start, d.rb_count,
                   d.box_rebuild, d.box_err, d.box_need, d.box_steps, d.box_rebuilds, d.goal, d.partials,
-                  b->d_box_of_slot};
+                  d.box_mid, b->d_box_of_slot};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);
@@ -1210,6 +1331,7 @@ int mdg_batch_set_state(mdg_batch *b, const double *q4, const double *p4) {
   MDG_BCK(cudaMemcpyAsync(b->d.box_rebuilds, lz.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(b->d.box_req, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(b->d.box_preq, zeros.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  MDG_BCK(cudaMemsetAsync(b->d.box_mid, 0xFF, b->nbox * sizeof(int), b->stream));  // q_end current
   MDG_BCK(cudaStreamSynchronize(b->stream));
   b->steps = 0;
   b->par = 0;
@@ -1221,6 +1343,7 @@ int mdg_batch_get_state(mdg_batch *b, double *q4, double *p4) {
   if (!b) return MDG_ERR_INVALID;
   cudaSetDevice(b->prm.device);
   double4_32a *tq = b->d.t_q, *tp = b->d.t_p;  // staging (free outside rebuilds)
+  make_end_current(b);
   k_batch_unsort<<<(b->total + 255) / 256, 256, 0, b->stream>>>(b->d, b->total, q4 ? tq : nullptr,
                                                                  p4 ? tp : nullptr, b->d_box_of_slot);
   const size_t bytes = (size_t)b->total * 32;
@@ -1284,6 +1407,7 @@ int mdg_batch_calculate(mdg_batch *b, int32_t nsteps) {
 int mdg_batch_observe(mdg_batch *b, double *out) {
   if (!b || !out) return MDG_ERR_INVALID;
   cudaSetDevice(b->prm.device);
+  make_end_current(b);
   k_batch_observe<<<b->nbox, 256, 0, b->stream>>>(b->P, b->d);
   MDG_BCK(cudaMemcpyAsync(out, b->d.partials, 3 * (size_t)b->nbox * sizeof(double), cudaMemcpyDeviceToHost,
                           b->stream));
@@ -1302,6 +1426,7 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
   MDG_BCK(balloc(&sq, n));
   MDG_BCK(balloc(&sp, n));
   MDG_BCK(balloc(&sid, n));
+  make_end_current(b);
   MDG_BCK(cudaMemcpyAsync(sq, b->d.q_end, n * 32, cudaMemcpyDeviceToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(sp, b->d.p, n * 32, cudaMemcpyDeviceToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(sid, b->d.id, n * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
@@ -1321,6 +1446,7 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
     MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
     MDG_BCK(cudaMemcpyAsync(b->d.p, sp, n * 32, cudaMemcpyDeviceToDevice, b->stream));
     MDG_BCK(cudaMemcpyAsync(b->d.id, sid, n * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
+    MDG_BCK(cudaMemsetAsync(b->d.box_mid, 0xFF, b->nbox * sizeof(int), b->stream));  // q_end restored, current
     std::vector<int> ones(b->nbox, 1);
     MDG_BCK(cudaMemcpyAsync(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
     MDG_BCK(cudaMemcpyAsync(b->d.box_steps, st0.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
@@ -1409,6 +1535,7 @@ int mdg_batch_tune(mdg_batch *b, int32_t trial_steps, int32_t *threads, int32_t 
   MDG_BCK(cudaMemcpyAsync(b->d.q_end, sq, n * 32, cudaMemcpyDeviceToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(b->d.p, sp, n * 32, cudaMemcpyDeviceToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(b->d.id, sid, n * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
+  MDG_BCK(cudaMemsetAsync(b->d.box_mid, 0xFF, b->nbox * sizeof(int), b->stream));  // q_end restored, current
   std::vector<int> ones(b->nbox, 1);
   MDG_BCK(cudaMemcpyAsync(b->d.box_rebuild, ones.data(), b->nbox * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   MDG_BCK(cudaMemcpyAsync(b->d.box_steps, st0.data(), b->nbox * sizeof(long long), cudaMemcpyHostToDevice, b->stream));
