@@ -164,3 +164,33 @@ def test_inner_list_changes_nothing(precision):
                 np.testing.assert_allclose(v, u, rtol=1e-7, atol=1e-7)
             else:
                 assert np.array_equal(u, v)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_plain"])
+def test_batch_mixed_state_readers(precision):
+    # the mixed forms do not write q_end in the step; observers, get_state and
+    # the autotuner's snapshot form it from each box's last q_mid slot, and
+    # the padding lane (packed reference positions inside) comes back zero.
+    # Reading between chunks leaves the run bit for bit where one call takes it
+    import ctypes
+    from mdacp_gb300.batch import Batch
+    boxes = _boxes(6, seed=23)
+    runs = []
+    for chunks in ((70,), (25, 1, 44)):
+        b = Batch(boxes, cutoff=RC, margin=MARGIN, dt=DT, precision=precision)
+        b.set_shape(256, 1, 2)
+        b.set_flat(True)
+        for c in chunks:
+            b.calculate(c)
+            b.observe_raw()
+            b.state()
+        n = sum(len(x[0]) for x in boxes)
+        q4 = np.full((n, 4), 7.0)
+        p4 = np.full((n, 4), 7.0)
+        dp = ctypes.POINTER(ctypes.c_double)
+        assert b.lib.mdg_batch_get_state(b._h, q4.ctypes.data_as(dp), p4.ctypes.data_as(dp)) == 0
+        assert not q4[:, 3].any() and not p4[:, 3].any()
+        runs.append((q4, p4, b.observe_raw()))
+    (qa, pa, oa), (qb, pb, ob) = runs
+    assert np.array_equal(qa, qb) and np.array_equal(pa, pb)
+    np.testing.assert_array_equal(oa, ob)

@@ -315,3 +315,32 @@ def test_mixed_readers_leave_the_trajectory_alone(precision):
     assert np.array_equal(qa, qb) and np.array_equal(pa, pb)
     assert a.stats()["rebuilds"] == b.stats()["rebuilds"] >= 3
     np.testing.assert_array_equal(a.observe_raw(), b.observe_raw())
+
+
+@pytest.mark.parametrize("precision", ["mixed", "mixed_plain"])
+def test_mixed_reference_positions_in_the_padding_lane(precision):
+    # the mixed form carries its build and prune reference positions in the
+    # padding lane of q_mid and p (21-bit fixed point per axis, displacement
+    # thresholds lowered by two units of the packing); the lane comes back
+    # zero from mdg_get_state, and the list rebuilds fall on the steps the
+    # FP64 form takes them (the thresholds move by micro-sigma, the
+    # trajectories differ by float rounding of the forces)
+    q, p, L = liquid_like(0.5, 16, seed=41)
+    a = _gpu(L, len(q), precision=precision)
+    b = _gpu(L, len(q))
+    for m in (a, b):
+        m.set_state(q, p)
+        m.make_pairlist()
+    for chunk in (60, 60, 80):
+        a.calculate(chunk)
+        b.calculate(chunk)
+        sa, sb = a.stats(), b.stats()
+        assert sa["rebuilds"] == sb["rebuilds"]
+        assert abs(sa["prunes"] - sb["prunes"]) <= 1
+    assert a.stats()["rebuilds"] >= 3
+    q4 = np.full((len(q), 4), 7.0)
+    p4 = np.full((len(q), 4), 7.0)
+    a.state(q4, p4)
+    assert not q4[:, 3].any() and not p4[:, 3].any()
+    qb, pb = b.state()
+    np.testing.assert_allclose(q4[:, :3], qb, rtol=0, atol=1e-6 * L[0])
