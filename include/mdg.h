@@ -11,9 +11,10 @@
  *
  * Particle arrays cross the boundary in the reference's layout: `double
  * [n][4]` with the fourth lane as padding (Variables::q / Variables::p,
- * variables.h:16-18), indexed by the caller's particle order.  Internally
- * particles are kept sorted by cell; results are returned in the caller's
- * order.
+ * variables.h:16-18), indexed by the caller's particle order: the lane is
+ * ignored on input (it never enters the kinetic energy) and returned as
+ * zero.  Internally particles are kept sorted by cell; results are returned
+ * in the caller's order.
  *
  * Physics (reference semantics): the smoothly truncated LJ potential
  * V(r) = 4(r^-12 - r^-6 + C2 r^2 + C0) with eps = sigma = m = 1 and C0, C2 from
