@@ -48,6 +48,15 @@ extern "C" {
 enum mdg_precision { MDG_FP64 = 0, MDG_MIXED = 1, MDG_MIXED_PLAIN = 2 };
 enum mdg_thermostat { MDG_NVE = 0, MDG_LANGEVIN = 1, MDG_NOSEHOOVER = 2 };
 
+/* When the pair list is rebuilt (.cfg RebuildPolicy).  HALFMARGIN: as soon
+ * as a particle has moved more than half the margin since the build.
+ * REFERENCE: PairList::IsPairListExpired (pairlist.cc:26-121): a buffer
+ * budget reduced by 2 max|p| dt each step and, once it is spent, the
+ * displacement check of at most check_list_length candidates; a step with
+ * 2 max|p| dt above the margin fails with MDG_ERR_STATE ("too fast
+ * particles", the reference's abort). */
+enum mdg_rebuild_policy { MDG_REBUILD_HALFMARGIN = 0, MDG_REBUILD_REFERENCE = 1 };
+
 typedef struct mdg_params {
   int32_t capacity;        /* maximum particles (Variables N, mdconfig.h:11) */
   int32_t precision;       /* mdg_precision (.cfg Precision=fp64|mixed|mixed_plain) */
@@ -64,11 +73,14 @@ typedef struct mdg_params {
   int32_t list_capacity;   /* neighbour slots per particle; 0 = sized from the first build */
   int32_t device;          /* CUDA device ordinal */
   int32_t use_graphs;      /* 1 = replay steps as CUDA graphs */
-  int32_t reserved;
+  int32_t rebuild_policy;  /* mdg_rebuild_policy (.cfg RebuildPolicy), default HALFMARGIN */
   double prune_buffer;     /* inner-list buffer: the force kernels walk the pairs within
                               cutoff + prune_buffer, re-selected from the list whenever a
                               particle moved prune_buffer/2 (default -1 = automatic,
                               min(0.1, margin / 2); 0 keeps every listed pair) */
+  int32_t check_list_length; /* CheckListLength (simulationinfo.cc:27): the reference
+                                policy's candidate limit, default 500 */
+  int32_t reserved;
 } mdg_params;
 
 typedef struct mdg_stats {

@@ -9,8 +9,9 @@ SimulationInfo follows simulationinfo.cc:5-51 for the reference keys and adds
 the keys of this engine, whose defaults keep the reference behaviour:
   CutoffLength (3.0, CUTOFF_LENGTH of mdconfig.h:15), BufferLength (0.3,
   simulationinfo.cc:6), Precision (fp64|mixed|mixed_plain), Device (gpu or
-  gpu:<ordinal>), RebuildPolicy (halfmargin, the only policy on the device),
-  LangevinHalfDriftCompat (yes).
+  gpu:<ordinal>), RebuildPolicy (halfmargin: rebuild once a particle moved
+  half the margin; reference: the buffer budget and displacement check of
+  pairlist.cc:26-121, with CheckListLength), LangevinHalfDriftCompat (yes).
 """
 import re
 
@@ -110,10 +111,9 @@ class SimulationInfo:
             raise ValueError("Precision must be fp64, mixed or mixed_plain")
         self.device = parse_device(param.get_string("Device", "gpu"))
         self.rebuild_policy = param.get_string("RebuildPolicy", "halfmargin")
-        if self.rebuild_policy != "halfmargin":
-            raise ValueError("RebuildPolicy=%s: the device rebuilds when a particle moved more than half the "
-                             "margin (halfmargin); the reference's buffer-budget policy runs in the reference's "
-                             "own CPU path" % self.rebuild_policy)
+        if self.rebuild_policy not in ("halfmargin", "reference"):
+            raise ValueError("RebuildPolicy=%s: halfmargin (rebuild once a particle moved half the margin) or "
+                             "reference (the buffer budget and displacement check of PairList)" % self.rebuild_policy)
         self.langevin_half_drift_compat = param.get_bool("LangevinHalfDriftCompat", True)
 
     @property

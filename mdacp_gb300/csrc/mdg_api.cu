@@ -93,7 +93,8 @@ void dfree_all(mdg_handle *h) {
   mdg::Dev &d = h->d;
   void *ptrs[] = {d.q_end, d.q_mid[0], d.q_mid[1], d.p, d.q_build, d.t_q, d.t_p, d.qf, d.loc[0], d.loc[1], d.id,
                   d.inv, d.cell, d.t_id, d.t_cell, d.order, d.cell_count, d.cell_fill, d.cell_start, d.block_sums,
-                  d.nl, d.ncount, d.pl, d.pcount, d.loc_p, d.partials, d.flags, d.io4, d.io4b, h->dobs};
+                  d.nl, d.ncount, d.pl, d.pcount, d.loc_p, d.partials, d.vpart, d.cand, d.flags, d.io4, d.io4b,
+                  h->dobs};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   memset(&h->d, 0, sizeof(h->d));
@@ -172,6 +173,10 @@ int setup_geometry(mdg_handle *h) {
   g.hb_d = std::sqrt(2.0 * p.gamma * p.temperature / p.dt);
   g.seed = p.seed;
   g.local_pos = p.precision != MDG_FP64 ? 1 : 0;
+  g.rebuild_policy = p.rebuild_policy;
+  g.check_list = p.check_list_length;
+  g.margin = p.margin;
+  g.sl = p.cutoff + p.margin;
   // packed reference positions of the mixed form: a packed coordinate is off
   // by at most half a unit plus float rounding, so each displacement
   // threshold is lowered by two units (about 6e-6 at w = 3)
@@ -246,6 +251,13 @@ int halt_error(mdg_handle *h) {
   cudaMemsetAsync(h->d.cell_fill, 0, (size_t)h->g.nrank * sizeof(int), h->stream);
   cudaStreamSynchronize(h->stream);
   char buf[160];
+  if (h->hflags->halt == mdg::kHaltTooFast) {
+    snprintf(buf, sizeof buf,
+             "too fast particles: 2 max|p| dt = %g exceeds the margin %g (PairList::IsPairListExpired); try a "
+             "smaller time step",
+             2.0 * h->hflags->vmax * h->prm.dt, h->prm.margin);
+    return fail(h, MDG_ERR_STATE, buf);
+  }
   if (h->hflags->halt == mdg::kHaltCheck) {
     snprintf(buf, sizeof buf, "bounds check failed (site %d, index %d)", h->hflags->check_site,
              h->hflags->bad_slot);
@@ -273,12 +285,28 @@ int ensure_list(mdg_handle *h, bool force) {
   return fail(h, MDG_ERR_CAPACITY, "neighbour list could not be sized");
 }
 
-int kernels_per_step(const mdg_handle *h) { return mdg::kRebuildKernels + mdg::step_kernels(h->prm.thermostat); }
+int kernels_per_step(const mdg_handle *h) {
+  const int policy = h->g.rebuild_policy == MDG_REBUILD_REFERENCE ? mdg::kPolicyKernels + mdg::kPolicyCheckKernels : 0;
+  return policy + mdg::kRebuildKernels + mdg::step_kernels(h->prm.thermostat);
+}
+
+// Kernels the step graphs executed for `completed` steps with `rebuilds`
+// rebuild bodies and `checks` displacement-check bodies: prelude, step
+// (+ NH), the reference policy's budget kernels.
+long long graph_kernels(const mdg_handle *h, long long completed, long long rebuilds, long long checks) {
+  const bool ref = h->g.rebuild_policy == MDG_REBUILD_REFERENCE;
+  return completed * (1 + mdg::step_kernels(h->prm.thermostat) + (ref ? mdg::kPolicyKernels : 0)) +
+         rebuilds * mdg::kRebuildKernels + checks * mdg::kPolicyCheckKernels;
+}
 
 // One step as plain launches: the rebuild sequence (no-ops unless due) and
 // the step kernel deciding its variant on the device (pmode 0), or both
 // variants in turn with optional events around them (pmode 3, profiled runs).
 void enqueue_step(mdg_handle *h, int par, int pmode = 0, cudaEvent_t before = nullptr, cudaEvent_t after = nullptr) {
+  if (h->g.rebuild_policy == MDG_REBUILD_REFERENCE) {  // the check's kernels are no-ops unless it is due
+    mdg::launch_policy(h->g, h->d, h->stream, 0, 0);
+    mdg::launch_policy_check(h->g, h->d, par, h->stream);
+  }
   mdg::launch_rebuild(h->g, h->d, par, h->num_sms, h->stream, true, lang_on(h) != 0, true);
   if (before) cudaEventRecord(before, h->stream);
   mdg::launch_step(h->g, h->d, par, h->prm.thermostat, h->prm.langevin_half_drift_compat, h->prm.precision,
@@ -358,6 +386,24 @@ int capture(mdg_handle *h, cudaGraphExec_t *out, int par, int nsteps, cudaEvent_
     };
     auto rebuild = [&] { mdg::launch_rebuild(h->g, h->d, p, h->num_sms, h->stream, false, false, true); };
     cudaGraphNode_t pre = nullptr, sw = nullptr;
+    if (h->g.rebuild_policy == MDG_REBUILD_REFERENCE) {
+      // the reference policy ahead of the step: the budget, then IF (spent)
+      // { the displacement check }, which may set the rebuild flag
+      cudaGraphConditionalHandle c_chk = 0;
+      cudaError_t e = cudaGraphConditionalHandleCreate(&c_chk, g, 0, cudaGraphCondAssignDefault);
+      if (e != cudaSuccess) {
+        rc = fail(h, MDG_ERR_CUDA, std::string("cudaGraphConditionalHandleCreate: ") + cudaGetErrorString(e));
+        break;
+      }
+      cudaGraphNode_t bud = nullptr, chk = nullptr;
+      rc = append_captured(h, g, last ? &last : nullptr, [&] { mdg::launch_policy(h->g, h->d, h->stream, c_chk, 1); },
+                           &bud);
+      if (rc == MDG_OK)
+        rc = add_conditional(h, g, bud, c_chk, cudaGraphCondTypeIf, 1,
+                             [&](int) { mdg::launch_policy_check(h->g, h->d, p, h->stream); }, &chk);
+      if (rc) break;
+      last = chk;
+    }
     if (ev) {
       cudaGraphConditionalHandle c_rb = 0, c_var = 0;
       cudaError_t e = cudaGraphConditionalHandleCreate(&c_rb, g, 0, cudaGraphCondAssignDefault);
@@ -447,7 +493,7 @@ int settle(mdg_handle *h) {
   long long done = 0;
   for (int attempt = 0; attempt < 64 && done < want; attempt++) {
     const unsigned long long before = (unsigned long long)h->steps_host;
-    const unsigned long long rebuilds0 = h->hflags->rebuilds;
+    const unsigned long long rebuilds0 = h->hflags->rebuilds, checks0 = h->hflags->checks;
     if (attempt > 0) {
       int rc = enqueue_steps(h, (int)(want - done));
       if (rc) return rc;
@@ -456,9 +502,9 @@ int settle(mdg_handle *h) {
     int rc = read_flags(h);
     if (rc) return rc;
     long long completed = (long long)(h->hflags->steps - before);
-    if (h->prm.use_graphs)  // executed kernels: prelude, step (+ NH), and the rebuild bodies that ran
-      h->launches += completed * (1 + mdg::step_kernels(h->prm.thermostat)) +
-                     (long long)(h->hflags->rebuilds - rebuilds0) * mdg::kRebuildKernels;
+    if (h->prm.use_graphs)
+      h->launches += graph_kernels(h, completed, (long long)(h->hflags->rebuilds - rebuilds0),
+                                   (long long)(h->hflags->checks - checks0));
     if (h->hflags->halt == 0) {
       done += completed;
       h->steps_host = (long long)h->hflags->steps;
@@ -518,6 +564,8 @@ void mdg_params_default(mdg_params *p) {
   p->seed = 1;
   p->use_graphs = 1;
   p->prune_buffer = -1.0;  // automatic
+  p->rebuild_policy = MDG_REBUILD_HALFMARGIN;
+  p->check_list_length = 500;  // CheckListLength default (simulationinfo.cc:27)
 }
 
 int mdg_create(const mdg_params *p, mdg_handle **out) {
@@ -530,6 +578,10 @@ int mdg_create(const mdg_params *p, mdg_handle **out) {
     return create_fail(MDG_ERR_INVALID, "cutoff and dt must be > 0, margin >= 0");
   if (p->precision < MDG_FP64 || p->precision > MDG_MIXED_PLAIN) return create_fail(MDG_ERR_INVALID, "bad precision");
   if (p->thermostat < MDG_NVE || p->thermostat > MDG_NOSEHOOVER) return create_fail(MDG_ERR_INVALID, "bad thermostat");
+  if (p->rebuild_policy != MDG_REBUILD_HALFMARGIN && p->rebuild_policy != MDG_REBUILD_REFERENCE)
+    return create_fail(MDG_ERR_INVALID, "bad rebuild policy");
+  if (p->rebuild_policy == MDG_REBUILD_REFERENCE && p->check_list_length < 1)
+    return create_fail(MDG_ERR_INVALID, "check_list_length must be >= 1");
   mdg_handle *h = new mdg_handle();
   h->prm = *p;
   memset(&h->g, 0, sizeof(h->g));
@@ -576,6 +628,9 @@ int mdg_create(const mdg_params *p, mdg_handle **out) {
   if (e == cudaSuccess) e = dalloc(&d.block_sums, 4096);
   if (e == cudaSuccess) e = dalloc(&d.ncount, cap);
   if (e == cudaSuccess) e = dalloc(&d.partials, 3 * nred);
+  if (e == cudaSuccess) e = dalloc(&d.vpart, 2 * ((cap + 255) / 256 + 1));
+  if (e == cudaSuccess)
+    e = dalloc(&d.cand, p->rebuild_policy == MDG_REBUILD_REFERENCE ? 2 * (size_t)p->check_list_length : (size_t)2);
   if (e == cudaSuccess) e = dalloc(&d.flags, 1);
   if (e == cudaSuccess) e = dalloc(&d.io4, cap);
   if (e == cudaSuccess) e = dalloc(&d.io4b, cap);
@@ -761,7 +816,8 @@ int timed_graph_run(mdg_handle *h, int32_t nsteps, double *step_ms, double *rebu
   int status = MDG_OK;
   for (int guard = 0; guard < 4096 && done < nsteps && status == MDG_OK; guard++) {
     const int m = (int)((nsteps - done) < kTimedChunk ? (nsteps - done) : kTimedChunk);
-    const unsigned long long before = (unsigned long long)h->steps_host, rebuilds0 = h->hflags->rebuilds;
+    const unsigned long long before = (unsigned long long)h->steps_host, rebuilds0 = h->hflags->rebuilds,
+                             checks0 = h->hflags->checks;
     cudaGraphExec_t gx = nullptr;
     status = capture(h, &gx, h->par, m, ev.data());
     if (status) break;
@@ -775,8 +831,8 @@ int timed_graph_run(mdg_handle *h, int32_t nsteps, double *step_ms, double *rebu
     status = read_flags(h);
     if (status) break;
     const long long completed = (long long)(h->hflags->steps - before);
-    h->launches += completed * (1 + mdg::step_kernels(h->prm.thermostat)) +
-                   (long long)(h->hflags->rebuilds - rebuilds0) * mdg::kRebuildKernels;
+    h->launches += graph_kernels(h, completed, (long long)(h->hflags->rebuilds - rebuilds0),
+                                 (long long)(h->hflags->checks - checks0));
     // a halted step and those behind it ran as no-ops: only the steps that
     // completed are timed
     const int timed = (int)(h->hflags->halt == 0 ? m : completed - 1);

@@ -218,8 +218,15 @@ __global__ void k_reorder(Geom g, Dev d) {
 __global__ void k_finalize(Geom g, Dev d, int q_mid_dst) {
   double4_32a *q_mid = d.q_mid[q_mid_dst];
   if (rebuild_off(d.flags)) return;
-  // k_wrap_bin, the only reader of end_stale in the rebuild, has finished
-  if (blockIdx.x == 0 && threadIdx.x == 0) d.flags->end_stale = 0;
+  // k_wrap_bin, the only reader of end_stale in the rebuild, has finished;
+  // a new list starts the reference policy's budget (PairList::Init,
+  // pairlist.cc:11-23)
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    d.flags->end_stale = 0;
+    d.flags->buffer_length = g.margin;
+    d.flags->lifetime = 0;
+    d.flags->need_check = 0;
+  }
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.n; k += gridDim.x * blockDim.x) {
     const double4_32a q = d.t_q[k];
     double4_32a p = d.t_p[k];
@@ -297,6 +304,371 @@ __global__ void k_prelude(DevFlags *f, int lang_step, cudaGraphConditionalHandle
 }
 
 }  // namespace
+
+// ----------------------------------------------------------------------------
+// The reference's rebuild policy, PairList::IsPairListExpired with
+// CheckByDisplacement (pairlist.cc:26-121), evaluated at the start of a step
+// (MDManager::Calculate, mdmanager.cc:116-148): the budget starts at the
+// margin at every build (PairList::Init, pairlist.cc:11-23) and loses
+// 2 max|p| dt per step; once it is negative, every step checks the entries
+// displaced by more than (margin - max displacement) since the build: more
+// than min(CheckListLength, entries) of them, or one pair of them that was
+// outside the search length at the build and is now inside the cut-off,
+// expires the list.  The reference runs the check over its local particles
+// and their ghost images (GetTotalParticleNumber): a particle within SL of a
+// face at the build has an image shifted by +-L across it, cascading over the
+// axes (FindBorderParticles, mdunit.cc:125-191).  Ghost positions are
+// refreshed after the first half-drift of a step (SendBorderParticles), so at
+// the next step's check an image stands at its original's previous mid-step
+// position, shifted: here q_mid of the other parity, which the coming step
+// has not yet overwritten.  Each entry is scored on its own positions, every
+// shifted coordinate formed by one addition as the ghost's is.
+namespace {
+
+constexpr int kPolicyThreads = 256;
+
+__device__ __forceinline__ double block_sum_d(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sh[w];
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ double block_max(double v, double *sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = fmax(t, sh[w]);
+  __syncthreads();
+  return t;
+}
+
+// Slot i in box coordinates: at the step boundary (the local entry) and at
+// the last build; at the previous mid-step (its images) only when it has
+// images (`with_mid`).  The mixed forms: home-cell centre plus
+// q_mid - p dt/2, plus qf, plus the other q_mid.
+struct PolicyPos {
+  double end[3], mid[3], bld[3];
+};
+
+__device__ __forceinline__ PolicyPos policy_positions(const Geom &g, const Dev &d, int i, int par) {
+  PolicyPos r;
+  if (g.local_pos) {
+    int cx, cy, cz;
+    cell_unkey(d.cell[i], cx, cy, cz);
+    const double o[3] = {cell_centre(g, 0, cx), cell_centre(g, 1, cy), cell_centre(g, 2, cz)};
+    const double4_32a u = d.q_mid[par][i], p = d.p[i];
+    const float4 b = d.qf[i];
+    r.end[0] = o[0] + fma(-p.x, g.dt2, u.x);
+    r.end[1] = o[1] + fma(-p.y, g.dt2, u.y);
+    r.end[2] = o[2] + fma(-p.z, g.dt2, u.z);
+    r.bld[0] = o[0] + (double)b.x;
+    r.bld[1] = o[1] + (double)b.y;
+    r.bld[2] = o[2] + (double)b.z;
+  } else {
+    const double4_32a q = d.q_end[i], b = d.q_build[i];
+    r.end[0] = q.x; r.end[1] = q.y; r.end[2] = q.z;
+    r.bld[0] = b.x; r.bld[1] = b.y; r.bld[2] = b.z;
+  }
+  r.mid[0] = r.mid[1] = r.mid[2] = 0.0;
+  return r;
+}
+
+__device__ __forceinline__ void with_mid(const Geom &g, const Dev &d, int i, int par, PolicyPos &r) {
+  const double4_32a v = d.q_mid[par ^ 1][i];
+  if (g.local_pos) {
+    int cx, cy, cz;
+    cell_unkey(d.cell[i], cx, cy, cz);
+    r.mid[0] = cell_centre(g, 0, cx) + v.x;
+    r.mid[1] = cell_centre(g, 1, cy) + v.y;
+    r.mid[2] = cell_centre(g, 2, cz) + v.z;
+  } else {
+    r.mid[0] = v.x; r.mid[1] = v.y; r.mid[2] = v.z;
+  }
+}
+
+// Image shifts of a particle along each axis (0, and +1 / -1 when its build
+// position lies within SL of the lower / upper face, strictly inside the
+// box: find_ghosts' inside_edge rule); its entries are the combinations,
+// numbered e = (ax * ny + ay) * nz + az, entry 0 the particle itself.
+struct Images {
+  int s[3][3];
+  int n[3];
+};
+
+__device__ __forceinline__ Images images_of(const Geom &g, const double bld[3]) {
+  Images im;
+  const double sl = g.sl;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    int c = 0;
+    im.s[k][c++] = 0;
+    if (bld[k] > 0.0 && bld[k] < sl) im.s[k][c++] = 1;
+    if (bld[k] > g.L[k] - sl && bld[k] < g.L[k]) im.s[k][c++] = -1;
+    im.n[k] = c;
+  }
+  return im;
+}
+
+// Entry e's build and current positions.
+__device__ __forceinline__ void entry_positions(const Geom &g, const PolicyPos &pp, const Images &im, int e,
+                                                double b[3], double c[3]) {
+  const int az = e % im.n[2], ay = (e / im.n[2]) % im.n[1], ax = e / (im.n[2] * im.n[1]);
+  const int sh[3] = {im.s[0][ax], im.s[1][ay], im.s[2][az]};
+  const double *cur = e == 0 ? pp.end : pp.mid;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    b[k] = sh[k] ? pp.bld[k] + sh[k] * g.L[k] : pp.bld[k];
+    c[k] = sh[k] ? cur[k] + sh[k] * g.L[k] : cur[k];
+  }
+}
+
+__device__ __forceinline__ double entry_disp(const double b[3], const double c[3]) {
+  const double dx = b[0] - c[0], dy = b[1] - c[1], dz = b[2] - c[2];
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// A particle outside the cells at the faces has no image (cells are at least
+// SL wide), and its one entry's displacement needs no box coordinates: the
+// build minus the step-boundary position, home-cell-local in the mixed forms.
+__device__ __forceinline__ bool face_cell(const Geom &g, const Dev &d, int i) {
+  int cx, cy, cz;
+  cell_unkey(d.cell[i], cx, cy, cz);
+  return cx == 0 || cy == 0 || cz == 0 || cx == g.nc[0] - 1 || cy == g.nc[1] - 1 || cz == g.nc[2] - 1;
+}
+
+__device__ __forceinline__ double local_disp(const Geom &g, const Dev &d, int i, int par) {
+  double dx, dy, dz;
+  if (g.local_pos) {
+    const double4_32a u = d.q_mid[par][i], p = d.p[i];
+    const float4 b = d.qf[i];
+    dx = (double)b.x - fma(-p.x, g.dt2, u.x);
+    dy = (double)b.y - fma(-p.y, g.dt2, u.y);
+    dz = (double)b.z - fma(-p.z, g.dt2, u.z);
+  } else {
+    const double4_32a q = d.q_end[i], b = d.q_build[i];
+    dx = b.x - q.x;
+    dy = b.y - q.y;
+    dz = b.z - q.z;
+  }
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// The policy is not evaluated when a rebuild is already due (the reference's
+// uninitialized list) or after a halt.
+__device__ __forceinline__ bool policy_off(const DevFlags *f) { return f->halt != 0 || f->rebuild != 0; }
+
+__global__ void __launch_bounds__(kPolicyThreads) k_policy_vmax(Geom g, Dev d) {
+  __shared__ double sh[kPolicyThreads / 32];
+  if (policy_off(d.flags)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (i < g.n) {
+    const double4_32a p = d.p[i];
+    v = p.x * p.x + p.y * p.y + p.z * p.z;
+  }
+  const double m = block_max(v, sh);
+  if (threadIdx.x == 0) d.vpart[blockIdx.x] = m;
+}
+
+// The budget: lifetime, vmax, the too-fast abort, the budget's decrease, and
+// whether this step checks displacements (pairlist.cc:26-65).
+__global__ void __launch_bounds__(1024) k_policy_budget(Geom g, Dev d, int nparts, cudaGraphConditionalHandle check_cond,
+                                                        int use_cond) {
+  __shared__ double sh[32];
+  DevFlags *f = d.flags;
+  const bool off = policy_off(f);
+  double v = 0.0;
+  if (!off)
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) v = fmax(v, d.vpart[k]);
+  const double vmax2 = block_max(v, sh);
+  if (threadIdx.x != 0) return;
+  int need = 0;
+  if (!off) {
+    f->lifetime += 1;
+    double buf = f->buffer_length;
+    if (buf > 0.0) {
+      const double vmax = sqrt(vmax2);
+      f->vmax = vmax;
+      if (vmax * 2.0 * g.dt > g.margin) {
+        halt_with(f, kHaltTooFast);
+      } else {
+        buf = buf - vmax * 2.0 * g.dt;
+        f->buffer_length = buf;
+      }
+    }
+    need = f->halt == 0 && buf < 0.0;
+    if (need) f->checks += 1;
+  }
+  f->need_check = need;
+  if (use_cond) cudaGraphSetConditional(check_cond, need ? 1u : 0u);
+}
+
+// Per slot the local entry's displacement (t_q.x) and the largest of its
+// images' (t_q.y; the images are scored only for particles that have any);
+// per block the largest displacement and the entry count, the latter in
+// vpart[nparts + block].
+__global__ void __launch_bounds__(kPolicyThreads) k_policy_disp(Geom g, Dev d, int par) {
+  __shared__ double sh[kPolicyThreads / 32];
+  if (!d.flags->need_check) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double dmax = 0.0, entries = 0.0;
+  if (i < g.n && !face_cell(g, d, i)) {
+    const double d0 = local_disp(g, d, i, par);
+    d.t_q[i].x = d0;
+    d.t_q[i].y = 0.0;
+    dmax = d0;
+    entries = 1.0;
+  } else if (i < g.n) {
+    PolicyPos pp = policy_positions(g, d, i, par);
+    const Images im = images_of(g, pp.bld);
+    const int ne = im.n[0] * im.n[1] * im.n[2];
+    if (ne > 1) with_mid(g, d, i, par, pp);
+    double b[3], c[3];
+    entry_positions(g, pp, im, 0, b, c);
+    const double d0 = entry_disp(b, c);
+    double dimg = 0.0;
+    for (int e = 1; e < ne; e++) {
+      entry_positions(g, pp, im, e, b, c);
+      dimg = fmax(dimg, entry_disp(b, c));
+    }
+    d.t_q[i].x = d0;  // staging: free until a rebuild reorders
+    d.t_q[i].y = dimg;
+    dmax = fmax(d0, dimg);
+    entries = (double)ne;
+  }
+  const double m = block_max(dmax, sh);
+  const double t = block_sum_d(entries, sh);
+  if (threadIdx.x == 0) {
+    d.vpart[blockIdx.x] = m;
+    d.vpart[gridDim.x + blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_policy_threshold(Geom g, Dev d, int nparts) {
+  __shared__ double sh[32];
+  DevFlags *f = d.flags;
+  if (!f->need_check) return;
+  double v = 0.0, e = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+    v = fmax(v, d.vpart[k]);
+    e += d.vpart[nparts + k];
+  }
+  const double dr2_max = block_max(v, sh);
+  const double entries = block_sum_d(e, sh);
+  if (threadIdx.x == 0) {
+    f->entries = (int)entries;
+    const double c_distance = g.margin - sqrt(dr2_max);
+    f->c_d2 = c_distance * c_distance;
+    f->cand_count = 0;
+    f->cand_slots = 0;
+  }
+}
+
+// Candidate entries (any order: the outcome depends on their set alone):
+// counted toward the limit; each particle with any is recorded with the mask
+// of its candidate entries.
+__global__ void __launch_bounds__(kPolicyThreads) k_policy_candidates(Geom g, Dev d, int par) {
+  DevFlags *f = d.flags;
+  if (!f->need_check) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n) return;
+  const double c_d2 = f->c_d2;
+  if (!(d.t_q[i].x > c_d2) && !(d.t_q[i].y > c_d2)) return;  // no entry of this particle
+  unsigned mask = 0;
+  if (!face_cell(g, d, i)) {
+    mask = 1u;  // its only entry, scored by k_policy_disp
+  } else {
+    PolicyPos pp = policy_positions(g, d, i, par);
+    const Images im = images_of(g, pp.bld);
+    const int ne = im.n[0] * im.n[1] * im.n[2];
+    if (ne > 1) with_mid(g, d, i, par, pp);
+    for (int e = 0; e < ne; e++) {
+      double b[3], c[3];
+      entry_positions(g, pp, im, e, b, c);
+      if (entry_disp(b, c) > c_d2) mask |= 1u << e;
+    }
+  }
+  if (!mask) return;
+  atomicAdd(&f->cand_count, __popc(mask));
+  const int k = atomicAdd(&f->cand_slots, 1);
+  if (k < g.check_list) {
+    d.cand[k] = i;
+    d.cand[g.check_list + k] = (int)mask;
+  }
+}
+
+// Expired when the candidate entries reached min(CheckListLength, entries),
+// or when a pair of candidate entries outside the search length at the build
+// is inside the cut-off now (two entries of one particle are a box length
+// apart and never are).  Block a takes the pairs (a, b > a) of the recorded
+// candidate particles, its threads striding over b; any block that finds one
+// sets the rebuild flag (a plain store of 1).
+__global__ void __launch_bounds__(kPolicyThreads) k_policy_pairs(Geom g, Dev d, int par) {
+  DevFlags *f = d.flags;
+  if (!f->need_check) return;
+  const int nl = min(g.check_list, f->entries);
+  const int cnt = f->cand_count, np = f->cand_slots;
+  if (cnt >= nl) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) f->rebuild = 1;
+    return;
+  }
+  const int a = blockIdx.x;
+  if (a >= np) return;
+  const int ia = d.cand[a];
+  const unsigned ma = (unsigned)d.cand[g.check_list + a];
+  PolicyPos pa = policy_positions(g, d, ia, par);
+  const Images ima = images_of(g, pa.bld);
+  if (ima.n[0] * ima.n[1] * ima.n[2] > 1) with_mid(g, d, ia, par, pa);
+  int expired = 0;
+  for (int b = a + 1 + threadIdx.x; b < np && !expired; b += blockDim.x) {
+    const int ib = d.cand[b];
+    const unsigned mb = (unsigned)d.cand[g.check_list + b];
+    PolicyPos pb = policy_positions(g, d, ib, par);
+    const Images imb = images_of(g, pb.bld);
+    if (imb.n[0] * imb.n[1] * imb.n[2] > 1) with_mid(g, d, ib, par, pb);
+    for (unsigned xa = ma; xa && !expired; xa &= xa - 1) {
+      double ba[3], ca[3];
+      entry_positions(g, pa, ima, __ffs(xa) - 1, ba, ca);
+      for (unsigned xb = mb; xb && !expired; xb &= xb - 1) {
+        double bb[3], cb[3];
+        entry_positions(g, pb, imb, __ffs(xb) - 1, bb, cb);
+        double dx = ba[0] - bb[0], dy = ba[1] - bb[1], dz = ba[2] - bb[2];
+        if (dx * dx + dy * dy + dz * dz < g.sl2) continue;
+        dx = ca[0] - cb[0];
+        dy = ca[1] - cb[1];
+        dz = ca[2] - cb[2];
+        if (dx * dx + dy * dy + dz * dz < g.rc2) expired = 1;
+      }
+    }
+  }
+  if (expired) f->rebuild = 1;
+}
+
+}  // namespace
+
+void launch_policy(const Geom &g, const Dev &d, cudaStream_t s, cudaGraphConditionalHandle check_cond, int use_cond) {
+  const int grid = g.n > 0 ? (g.n + kPolicyThreads - 1) / kPolicyThreads : 1;
+  k_policy_vmax<<<grid, kPolicyThreads, 0, s>>>(g, d);
+  k_policy_budget<<<1, 1024, 0, s>>>(g, d, grid, check_cond, use_cond);
+}
+
+void launch_policy_check(const Geom &g, const Dev &d, int par, cudaStream_t s) {
+  const int grid = g.n > 0 ? (g.n + kPolicyThreads - 1) / kPolicyThreads : 1;
+  k_policy_disp<<<grid, kPolicyThreads, 0, s>>>(g, d, par);
+  k_policy_threshold<<<1, 1024, 0, s>>>(g, d, grid);
+  k_policy_candidates<<<grid, kPolicyThreads, 0, s>>>(g, d, par);
+  // one block per candidate particle the check can record
+  k_policy_pairs<<<g.check_list, kPolicyThreads, 0, s>>>(g, d, par);
+}
 
 // Declared in mdg_list.cu.
 void launch_build_list(const Geom &g, const Dev &d, int num_sms, cudaStream_t s, bool in_step);

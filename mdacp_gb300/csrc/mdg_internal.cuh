@@ -50,6 +50,7 @@ __device__ __forceinline__ int entry_sz(uint32_t e) { return (int)((e >> 4) & 3u
 constexpr int kHaltOverflow = 1;
 constexpr int kHaltBadState = 2;
 constexpr int kHaltCheck = 3;  // checked builds: a bounds check failed
+constexpr int kHaltTooFast = 4;  // reference rebuild policy: 2 max|p| dt above the margin
 
 struct DevFlags {
   int rebuild;                  // rebuild the list at the start of the next step
@@ -71,6 +72,16 @@ struct DevFlags {
   unsigned long long prunes;    // completed prunes
   unsigned long long inner_pairs;  // directed pairs in the inner list at the last prune
   int end_stale;                // mixed form: q_end is behind the steps (rebuilt from q_mid and p on demand)
+  // reference rebuild policy (PairList, pairlist.cc:26-121)
+  double buffer_length;         // what is left of the margin's budget since the build
+  double c_d2;                  // candidate threshold of the displacement check
+  unsigned long long lifetime;  // steps since the build
+  unsigned long long checks;    // displacement checks run
+  int need_check;               // this step runs the displacement check
+  int cand_count;               // candidate entries (particles and their images) found by it
+  int cand_slots;               // candidate particles recorded
+  int entries;                  // particles and their images (the reference's local + ghost count)
+  double vmax;                  // max |p| at the last policy evaluation
 };
 
 struct Geom {
@@ -110,6 +121,10 @@ struct Geom {
   // largest rounding of a packed position
   float ref_scale[3], ref_unit[3];
   float half_margin2_ref, half_prune2_ref;
+  // rebuild policy (mdg_rebuild_policy); the reference policy's margin and
+  // candidate limit min(CheckListLength, n)
+  int rebuild_policy, check_list;
+  double margin, sl;  // margin, search length rc + margin
 };
 
 // Home-cell-local position (|x| < w per axis) packed into the bits of a
@@ -149,6 +164,8 @@ struct Dev {
   float4 *loc_p;        // home-cell-local position at the last prune
   double *partials;     // reduction scratch
   int nblocks_red;
+  double *vpart;        // reference rebuild policy: per-block maxima
+  int *cand;            // reference rebuild policy: the check's candidate particles, then their entry masks
   DevFlags *flags;
   double4_32a *io4;         // caller-order staging for get/set/forces
   double4_32a *io4b;
@@ -174,6 +191,12 @@ void launch_prelude_split(const Dev &d, int lang_step, cudaGraphConditionalHandl
                           cudaGraphConditionalHandle variant_cond, cudaStream_t s);
 void launch_prelude(const Dev &d, int lang_step, cudaGraphConditionalHandle step_cond, cudaStream_t s);
 void launch_nh_init(const Geom &g, const Dev &d, cudaStream_t s);
+// Reference rebuild policy at the start of a step that reads q_mid[par]: the
+// budget (2 kernels; with a graph handle it sets the check's IF condition)
+// and the displacement check (4 kernels, no-ops unless the budget is spent).
+constexpr int kPolicyKernels = 2, kPolicyCheckKernels = 4;
+void launch_policy(const Geom &g, const Dev &d, cudaStream_t s, cudaGraphConditionalHandle check_cond, int use_cond);
+void launch_policy_check(const Geom &g, const Dev &d, int par, cudaStream_t s);
 void launch_observe(const Geom &g, const Dev &d, double *out_dev, cudaStream_t s, int mixed, int par);
 void launch_forces(const Geom &g, const Dev &d, int mixed, int par, cudaStream_t s);
 void launch_unsort(const Geom &g, const Dev &d, int par, double4_32a *qo, double4_32a *po, cudaStream_t s);

@@ -448,7 +448,10 @@ __global__ void __launch_bounds__(step_threads<THERMO, MIXED, PMODE>(), (PMODE !
       float bx, by, bz;
       unpack_ref(g, q0.w, bx, by, bz);
       const float fx = ln.x - bx, fy = ln.y - by, fz = ln.z - bz;
-      if (fx * fx + fy * fy + fz * fz > g.half_margin2_ref || !(fx == fx && fy == fy && fz == fz))
+      // the half-margin rule, or a non-finite position (the rebuild's wrap
+      // reports it) under either policy
+      if ((g.rebuild_policy == MDG_REBUILD_HALFMARGIN && fx * fx + fy * fy + fz * fz > g.half_margin2_ref) ||
+          !(fx == fx && fy == fy && fz == fz))
         d.flags->rebuild = 1;
     } else {
       const double4_32a qb = d.q_build[i];
@@ -457,7 +460,8 @@ __global__ void __launch_bounds__(step_threads<THERMO, MIXED, PMODE>(), (PMODE !
       // float for the new home-cell-local position (qf holds the local
       // position at the build) and the inner-list test
       ln = make_float4(lb.x + (float)ux, lb.y + (float)uy, lb.z + (float)uz, lb.w);
-      if (ux * ux + uy * uy + uz * uz > g.half_margin2 || !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
+      if ((g.rebuild_policy == MDG_REBUILD_HALFMARGIN && ux * ux + uy * uy + uz * uz > g.half_margin2) ||
+          !(q1.x == q1.x && q1.y == q1.y && q1.z == q1.z))
         d.flags->rebuild = 1;
     }
     d.loc[par ^ 1][i] = ln;

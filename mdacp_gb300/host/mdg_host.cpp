@@ -79,16 +79,21 @@ SimulationInfo::SimulationInfo(const Parameter &p) {
   else throw std::runtime_error("Precision must be fp64, mixed or mixed_plain");
   LangevinHalfDriftCompat = p.GetBooleanDef("LangevinHalfDriftCompat", true);
   // keys of this engine: the GPU only (Device=cpu is the reference's own
-  // path), and the half-margin rebuild rule only
+  // path), and the rebuild rule (the reference's PairList policy or half the
+  // margin)
   const std::string dev = p.GetStringDef("Device", "gpu");
   if (dev == "gpu") Device = 0;
   else if (dev.rfind("gpu:", 0) == 0 && dev.size() > 4 && dev.find_first_not_of("0123456789", 4) == std::string::npos)
     Device = atoi(dev.c_str() + 4);
   else throw std::runtime_error("Device=" + dev + ": this engine runs on the GPU (Device=gpu or gpu:<ordinal>)");
   const std::string policy = p.GetStringDef("RebuildPolicy", "halfmargin");
-  if (policy != "halfmargin")
+  if (policy == "halfmargin") RebuildPolicy = MDG_REBUILD_HALFMARGIN;
+  else if (policy == "reference") RebuildPolicy = MDG_REBUILD_REFERENCE;
+  else
     throw std::runtime_error("RebuildPolicy=" + policy +
-                             ": the device rebuilds when a particle moved more than half the margin (halfmargin)");
+                             ": halfmargin (rebuild once a particle moved half the margin) or reference (the "
+                             "buffer budget and displacement check of PairList)");
+  CheckListLength = p.GetIntegerDef("CheckListLength", 500);
 }
 
 MDManager::MDManager(const Parameter &param, int capacity) : sinfo_(param) {
@@ -107,6 +112,8 @@ MDManager::MDManager(const Parameter &param, int capacity) : sinfo_(param) {
   p.tau = sinfo_.HeatbathTau;
   p.seed = (uint64_t)param.GetIntegerDef("Seed", 1);
   p.device = sinfo_.Device;
+  p.rebuild_policy = sinfo_.RebuildPolicy;
+  p.check_list_length = sinfo_.CheckListLength;
   const int rc = mdg_create(&p, &h_);
   if (rc != MDG_OK)
     throw std::runtime_error("mdg_create failed (" + std::to_string(rc) + "): " + mdg_last_error(nullptr));

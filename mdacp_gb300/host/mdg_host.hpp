@@ -44,6 +44,8 @@ struct SimulationInfo {
   int Precision;     // MDG_FP64 / MDG_MIXED / MDG_MIXED_PLAIN
   bool LangevinHalfDriftCompat;
   int Device;        // CUDA ordinal from Device=gpu (0) or gpu:<ordinal>
+  int RebuildPolicy; // mdg_rebuild_policy from RebuildPolicy=halfmargin|reference
+  int CheckListLength;  // simulationinfo.cc:27, the reference policy's candidate limit
 };
 
 // MDManager for one box (mdmanager.h:32-83).  Particles are staged on the

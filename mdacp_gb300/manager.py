@@ -33,7 +33,8 @@ def _as4(x):
 class MDManager:
     def __init__(self, box, capacity=None, cutoff=3.0, margin=0.3, dt=0.001, precision="fp64",
                  thermostat="nve", temperature=1.0, gamma=0.1, tau=0.1, seed=1, langevin_half_drift_compat=True,
-                 list_capacity=0, device=0, use_graphs=True, n=None, prune_buffer=None):
+                 list_capacity=0, device=0, use_graphs=True, n=None, prune_buffer=None,
+                 rebuild_policy="halfmargin", check_list_length=500):
         self.lib = native.load()
         prm = native.Params()
         self.lib.mdg_params_default(ctypes.byref(prm))
@@ -51,6 +52,8 @@ class MDManager:
         prm.use_graphs = 1 if use_graphs else 0
         if prune_buffer is not None:
             prm.prune_buffer = float(prune_buffer)
+        prm.rebuild_policy = native.REBUILD_POLICIES[rebuild_policy]
+        prm.check_list_length = int(check_list_length)
         self.params = prm
         self.L = np.array(prm.box[:])
         h = ctypes.c_void_p()
@@ -67,7 +70,8 @@ class MDManager:
         kw = dict(box=si.L, capacity=n, cutoff=si.cutoff, margin=si.buffer_length, dt=si.time_step,
                   precision=si.precision, thermostat=si.thermostat, temperature=si.aimed_temperature,
                   gamma=si.heatbath_gamma, tau=si.heatbath_tau, seed=param.get_int("Seed", 1),
-                  langevin_half_drift_compat=si.langevin_half_drift_compat, device=si.device)
+                  langevin_half_drift_compat=si.langevin_half_drift_compat, device=si.device,
+                  rebuild_policy=si.rebuild_policy, check_list_length=si.check_list_length)
         kw.update(overrides)
         return cls(**kw)
 

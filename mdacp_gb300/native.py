@@ -16,6 +16,8 @@ ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "capacity", 4: "bad particl
 FP64, MIXED, MIXED_PLAIN = 0, 1, 2
 PRECISIONS = {"fp64": FP64, "mixed": MIXED, "mixed_plain": MIXED_PLAIN}
 NVE, LANGEVIN, NOSEHOOVER = 0, 1, 2
+REBUILD_HALFMARGIN, REBUILD_REFERENCE = 0, 1
+REBUILD_POLICIES = {"halfmargin": REBUILD_HALFMARGIN, "reference": REBUILD_REFERENCE}
 
 
 class Params(ctypes.Structure):
@@ -24,7 +26,8 @@ class Params(ctypes.Structure):
                 ("thermostat", ctypes.c_int32), ("langevin_half_drift_compat", ctypes.c_int32),
                 ("temperature", ctypes.c_double), ("gamma", ctypes.c_double), ("tau", ctypes.c_double),
                 ("seed", ctypes.c_uint64), ("list_capacity", ctypes.c_int32), ("device", ctypes.c_int32),
-                ("use_graphs", ctypes.c_int32), ("reserved", ctypes.c_int32), ("prune_buffer", ctypes.c_double)]
+                ("use_graphs", ctypes.c_int32), ("rebuild_policy", ctypes.c_int32), ("prune_buffer", ctypes.c_double),
+                ("check_list_length", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):

@@ -34,6 +34,8 @@ def main():
     ap.add_argument("--shape", default="",
                     help="threads,lanes,ctas_per_sm[,inner 0|1[,flat 0|1]] for --boxes instead of the autotuner")
     ap.add_argument("--adjoint", action="store_true", help="one adjoint gradient instead (4,000 atoms)")
+    ap.add_argument("--rebuild-policy", default="halfmargin", choices=["halfmargin", "reference"],
+                    help="single box: the list rebuild rule")
     a = ap.parse_args()
     if a.adjoint:
         import time
@@ -73,7 +75,7 @@ def main():
     q, L = lattice.fcc_cube(a.cells, a.density)
     p = lattice.maxwell(len(q), 1.0, 1)
     m = MDManager(L, capacity=len(q), cutoff=2.5, margin=0.5, dt=0.001, precision=a.precision,
-                  use_graphs=not a.no_graphs)
+                  use_graphs=not a.no_graphs, rebuild_policy=a.rebuild_policy)
     m.set_state(q, p)
     m.make_pairlist()
     if a.profiled:

@@ -38,12 +38,15 @@ def test_simulationinfo_keys():
 
 
 def test_engine_keys_device_and_rebuild_policy():
-    # Device selects the GPU ordinal (the engine has no CPU path); the device
-    # has one rebuild rule (half the margin); Precision takes the plain-sum
-    # mixed form too
+    # Device selects the GPU ordinal (the engine has no CPU path); two rebuild
+    # rules (half the margin, the reference's budget and check with its
+    # CheckListLength); Precision takes the plain-sum mixed form too
     assert SimulationInfo(Parameter("")).device == 0
     assert SimulationInfo(Parameter("Device=gpu:3\n")).device == 3
     assert SimulationInfo(Parameter("Precision=mixed_plain\n")).precision == "mixed_plain"
-    for bad in ("Device=cpu\n", "Device=gpu:x\n", "RebuildPolicy=reference\n", "Precision=f16\n"):
+    assert SimulationInfo(Parameter("")).rebuild_policy == "halfmargin"
+    si = SimulationInfo(Parameter("RebuildPolicy=reference\nCheckListLength=64\n"))
+    assert si.rebuild_policy == "reference" and si.check_list_length == 64
+    for bad in ("Device=cpu\n", "Device=gpu:x\n", "RebuildPolicy=budget\n", "Precision=f16\n"):
         with pytest.raises(ValueError):
             SimulationInfo(Parameter(bad))

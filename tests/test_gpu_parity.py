@@ -344,3 +344,59 @@ def test_mixed_reference_positions_in_the_padding_lane(precision):
     assert not q4[:, 3].any() and not p4[:, 3].any()
     qb, pb = b.state()
     np.testing.assert_allclose(q4[:, :3], qb, rtol=0, atol=1e-6 * L[0])
+
+
+@pytest.mark.parametrize("use_graphs", [True, False])
+def test_reference_rebuild_policy_matches_oracle(use_graphs):
+    # RebuildPolicy=reference: the buffer budget (2 max|p| dt per step) and,
+    # once it is spent, the displacement check of PairList (pairlist.cc:26-121)
+    # over the particles and their ghost images (the images at the previous
+    # mid-step, as the reference refreshes them), evaluated at each step's
+    # start as the oracle does: the rebuilds fall on the same steps, and the
+    # FP64 trajectory matches the oracle's
+    q, p, L = liquid_like(0.5, 10, seed=43)
+    ref = port.System(q, p, L, rc=RC, margin=MARGIN, dt=0.002)
+    ref.make_pairlist()
+    m = _gpu(L, len(q), dt=0.002, rebuild_policy="reference", use_graphs=use_graphs)
+    m.set_state(q, p)
+    m.make_pairlist()
+    r = m.stats()["rebuilds"]
+    ref_steps, gpu_steps = [], []
+    for k in range(300):
+        if ref.calculate(1):
+            ref_steps.append(k + 1)
+        m.calculate(1)
+        r2 = m.stats()["rebuilds"]
+        if r2 != r:
+            gpu_steps.append(k + 1)
+        r = r2
+    assert gpu_steps == ref_steps and len(ref_steps) >= 6
+    np.testing.assert_allclose(m.observe_raw(), ref.observe_raw(), rtol=1e-10, atol=1e-10)
+
+
+def test_reference_rebuild_policy_mixed_and_too_fast():
+    # the mixed form under the reference policy rebuilds on the FP64 form's
+    # steps; a momentum with 2 |p| dt above the margin stops the run with the
+    # reference's "too fast particles" error, and the handle takes a new state
+    from mdacp_gb300 import native
+    q, p, L = liquid_like(0.5, 10, seed=47)
+    a = _gpu(L, len(q), dt=0.002, rebuild_policy="reference", precision="mixed")
+    b = _gpu(L, len(q), dt=0.002, rebuild_policy="reference")
+    for m in (a, b):
+        m.set_state(q, p)
+        m.make_pairlist()
+    for chunk in (100, 100):
+        a.calculate(chunk)
+        b.calculate(chunk)
+        assert a.stats()["rebuilds"] == b.stats()["rebuilds"]
+    assert b.stats()["rebuilds"] >= 3
+    fast = p.copy()
+    fast[0] = [130.0, 0.0, 0.0]  # 2 x 130 x 0.002 = 0.52 > margin 0.5
+    for m in (a, b):
+        m.set_state(q, fast)
+        with pytest.raises(native.MDGError, match="too fast"):
+            m.calculate(3)
+            m.synchronize()
+        m.set_state(q, p)
+        m.calculate(5)
+        m.synchronize()
