@@ -52,6 +52,10 @@ def test_version_and_defaults_without_gpu(lib):
     p = native.Params()
     L.mdg_params_default(ctypes.byref(p))
     assert p.cutoff == 3.0 and abs(p.margin - 0.3) < 1e-15 and p.dt == 0.001 and p.langevin_half_drift_compat == 1
+    # the half-margin rule by default; the reference policy's candidate limit
+    # at CheckListLength's default (simulationinfo.cc:27)
+    assert p.rebuild_policy == native.REBUILD_HALFMARGIN and p.check_list_length == 500
+    assert ctypes.sizeof(native.Params) == 128  # sizeof(mdg_params) on the C side
 
 
 def test_invalid_parameters_rejected_before_device_use(lib):
@@ -70,6 +74,14 @@ def test_invalid_parameters_rejected_before_device_use(lib):
     p.dt = 0.0
     assert L.mdg_create(ctypes.byref(p), ctypes.byref(h)) == 1
     assert b"dt" in L.mdg_last_error(None)
+    p.dt = 0.001
+    p.rebuild_policy = 7
+    assert L.mdg_create(ctypes.byref(p), ctypes.byref(h)) == 1
+    assert b"rebuild policy" in L.mdg_last_error(None)
+    p.rebuild_policy = native.REBUILD_REFERENCE
+    p.check_list_length = 0
+    assert L.mdg_create(ctypes.byref(p), ctypes.byref(h)) == 1
+    assert b"check_list_length" in L.mdg_last_error(None)
 
 
 def test_python_manager_reports_the_create_reason():
