@@ -188,6 +188,7 @@ int print_config(const std::string &path) {
            si.ControlTemperature ? 1 : 0, si.HeatbathType, si.CutoffLength, si.BufferLength);
     printf("Precision %d\nLangevinHalfDriftCompat %d\nMode %s\nlattice %d\n", si.Precision,
            si.LangevinHalfDriftCompat ? 1 : 0, param.GetStringDef("Mode", "").c_str(), lattice_count(param));
+    printf("RebuildPolicy %d\nCheckListLength %d\n", si.RebuildPolicy, si.CheckListLength);
   } catch (const std::exception &e) {
     printf("error %s\n", e.what());
     return 2;

@@ -43,6 +43,21 @@ def test_print_config_matches_python_semantics(host_bin, tmp_path):
     assert int(kv["lattice"]) == 4 * 8 * 8 * 9
 
 
+def test_rebuild_policy_keys(host_bin, tmp_path):
+    # RebuildPolicy (halfmargin by default, or the reference's PairList
+    # policy) and its CheckListLength, read as the Python mirror reads them
+    for text, policy, cl in (("", 0, 500), ("RebuildPolicy=reference\nCheckListLength=64\n", 1, 64)):
+        out = subprocess.run([host_bin, "--print-config", _cfg(tmp_path, text)], capture_output=True, text=True)
+        assert out.returncode == 0, out.stdout
+        kv = dict(line.split(" ", 1) for line in out.stdout.strip().splitlines())
+        si = SimulationInfo(Parameter(text))
+        assert int(kv["RebuildPolicy"]) == policy == {"halfmargin": 0, "reference": 1}[si.rebuild_policy]
+        assert int(kv["CheckListLength"]) == cl == si.check_list_length
+    out = subprocess.run([host_bin, "--print-config", _cfg(tmp_path, "RebuildPolicy=budget\n")], capture_output=True,
+                         text=True)
+    assert out.returncode == 2 and "RebuildPolicy=budget" in out.stdout
+
+
 def test_bad_heatbath_rejected(host_bin, tmp_path):
     out = subprocess.run([host_bin, "--print-config", _cfg(tmp_path, "HeatbathType=Foo\n")], capture_output=True,
                          text=True)
