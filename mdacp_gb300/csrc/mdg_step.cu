@@ -24,9 +24,10 @@
 // particle; momentum and position updates in double with fused multiply-adds,
 // the mid-step positions kept relative to the centre of the home cell (so the
 // float position partners gather is one conversion and the displacement since
-// the build is tested in float against the build's local position) and the
-// step-boundary positions not written (the readers rebuild them from q_mid
-// and p).  MDG_MIXED_PLAIN sums the pair forces in plain float instead (an
+// the build is tested in float against the build's local position, which
+// travels packed in q_mid's padding word, as the prune reference does in p's)
+// and the step-boundary positions not written (the readers rebuild them from
+// q_mid and p).  MDG_MIXED_PLAIN sums the pair forces in plain float instead (an
 // error near u sqrt(40) |f_ij|, u = 2^-24, over about 40 terms).  GB300 runs
 // double precision at 1/64 of the float rate, so the per-particle double work
 // (momentum, two half-drifts) is kept to one operation per component each,
