@@ -66,6 +66,24 @@ def test_port_matches_reference_live(density, cells):
     assert np.array_equal(qf, ref["q"]) and np.array_equal(pf, ref["p"])
 
 
+@pytest.mark.skipif(not refrun.available(2.5), reason="reference binary not built (oracle/build_ref.sh)")
+@pytest.mark.parametrize("density,cells", [(0.5, 10), (0.8, 8)])
+def test_port_matches_reference_over_many_rebuilds(density, cells):
+    """1,000 steps: the buffer-length countdown, the candidate-pair check and
+    the rebuilds they trigger (PairList::UpdatePairListValidity,
+    PairList::CheckByDisplacement, pairlist.cc:48-100; MDManager::Calculate,
+    mdmanager.cc:116-126) fall on the same steps as the reference's, or the
+    final state would not be bit-equal."""
+    q, p, L = liquid_like(density, cells, seed=7 * cells)
+    ref = refrun.run("trace", q, p, L, steps=1000, observe_every=100)
+    s = port.System(q, p, L, rc=2.5, margin=0.5)
+    s.make_pairlist()
+    assert np.array_equal(_trace(s, 1000, 100), ref["trace"][:, 1:])
+    qf, pf = s.state()
+    assert np.array_equal(qf, ref["q"]) and np.array_equal(pf, ref["p"])
+    assert s.rebuilds >= 10
+
+
 @pytest.mark.skipif(not refrun.available(3.0), reason="reference binary not built (oracle/build_ref.sh)")
 def test_port_matches_unpatched_reference_cutoff():
     """The reference's own compile-time constants: rc = 3.0, margin 0.3."""
